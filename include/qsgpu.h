@@ -1,0 +1,283 @@
+/*
+ * qsgpu.h -- C-ABI of the GB300 (sm_103a) block-sparse symmetric tensor
+ * contraction library (libqsgpu.so).
+ *
+ * The library replaces the numerical core behind QSpace's MEX routines
+ * contractQS / permuteQS / eigQS / svdQS and the Davidson re-orthogonalisation
+ * step.  Host code (a MEX shim, a C++ application, or Python through ctypes)
+ * passes block-sparse tensors as plain pointers; nothing in these signatures
+ * is a torch or MATLAB type.
+ *
+ * Conventions
+ *  - Every entry point returns qs_status; on failure qs_last_error() returns a
+ *    thread-local message (the reference throws Wb::LogException, which the
+ *    MEX layer turns into mexErrMsgIdAndTxt, Source/wblib.h:633-660).
+ *  - A QSpace is described by qs_qspace_view (the MATLAB struct {Q,data,info}
+ *    of Source/QSpace.hh:3092): int32 labels, per-block leg dimensions and
+ *    column-major FP64 blocks (complex: interleaved {re,im}, the layout of
+ *    wbcomplex) stored back to back at the given element offsets.
+ *  - Index strings follow the reference ('12*', '1,3', '[2 3]*'): 1-based legs,
+ *    a trailing '*' conjugates that operand (Source/wbindex.cc:482-540).
+ *  - Permutations are 1-based over the output legs (Source/contractQS.cc:
+ *    521-536); nperm = 0 means none.
+ *  - Host buffers are borrowed read-only for the duration of the call.
+ *    Results are owned by the caller and released with qs_result_free /
+ *    qs_tensor_free.
+ *  - One qs_ctx drives one CUDA stream on one device.  Calls on the same
+ *    context must not overlap; different contexts may be used from
+ *    different threads.
+ */
+#ifndef QSGPU_H
+#define QSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define QS_EXPORT __attribute__((visibility("default")))
+#else
+#define QS_EXPORT
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  QS_OK = 0,
+  QS_ERR_ARG = 1,        /* malformed argument (index string, perm, sizes) */
+  QS_ERR_SHAPE = 2,      /* inconsistent block dimensions                 */
+  QS_ERR_LABEL = 3,      /* label / QDIM / itag inconsistency             */
+  QS_ERR_CUDA = 4,       /* a CUDA runtime / library call failed          */
+  QS_ERR_OOM = 5,        /* device memory exhausted or admission refused  */
+  QS_ERR_TIMEOUT = 6,    /* a bounded device wait ran out                  */
+  QS_ERR_UNSUPPORTED = 7,
+  QS_ERR_INTERNAL = 8,
+  QS_ERR_CANCELLED = 9,
+  QS_ERR_NUMERIC = 10    /* e.g. split precision could not meet the tolerance */
+} qs_status;
+
+typedef enum {
+  QS_PREC_FP64 = 0,   /* plain FP64 (DFMA) path: the drop-in                   */
+  QS_PREC_SPLIT = 1   /* FP64 sliced into BF16 digits, tcgen05 products with
+                         exact FP32 accumulation, compensated recombination   */
+} qs_prec;
+
+typedef struct qs_ctx qs_ctx;         /* device + stream + memory pool        */
+typedef struct qs_result qs_result;   /* host-side result of a contraction    */
+typedef struct qs_tensor qs_tensor;   /* device-resident QSpace               */
+
+/* A block-sparse tensor in host memory (or, for qs_tensor_from_device, with
+ * `data` a device pointer). */
+typedef struct {
+  int32_t rank;           /* number of legs r                                  */
+  int32_t qdim;           /* labels per leg (QDIM; e.g. 2 for U(1)xU(1))       */
+  int64_t nblk;           /* number of blocks                                  */
+  const int32_t *q;       /* nblk x (rank*qdim), block-major: block i, leg k,
+                             component j at q[(i*rank + k)*qdim + j]           */
+  const int64_t *dims;    /* nblk x rank leg dimensions                        */
+  const int64_t *offs;    /* nblk element offsets into data (complex: in
+                             complex elements)                                 */
+  const double *data;     /* blocks, column-major, back to back                */
+  int32_t is_complex;     /* 0: float64, 1: complex128 interleaved             */
+} qs_qspace_view;
+
+typedef struct {
+  int32_t prec;       /* qs_prec                                               */
+  int32_t nslices;    /* split path: BF16 digits per operand; 0 = automatic     */
+  double tol;         /* split path: target relative error (default 1e-12)     */
+  int32_t flags;      /* QS_FLAG_*                                              */
+} qs_opts;
+
+#define QS_FLAG_NO_GRAPH 1      /* do not capture/replay the launch in a CUDA graph */
+#define QS_FLAG_DETERMINISTIC 2 /* fixed reduction order (always true today)   */
+
+/* Per-call statistics (optional out-parameter). */
+typedef struct {
+  double flops;           /* FP64-equivalent flops: 2MNK real, 8MNK complex   */
+  double bytes;           /* algorithmic bytes: inputs + output, once          */
+  double device_ms;       /* device time of the contraction kernels            */
+  int64_t npairs;         /* block pairs                                       */
+  int64_t nblk_out;       /* output blocks                                     */
+  int32_t nslices;        /* split path: digits used                           */
+  int32_t digit_bits;     /* split path: bits per digit                        */
+  double err_bound;       /* split path: a-priori relative error bound         */
+  int32_t launches;       /* kernels launched by this call                     */
+  int32_t pad_;
+} qs_stats;
+
+/* ---------------------------------------------------------------- basics */
+
+QS_EXPORT const char *qs_last_error(void);
+QS_EXPORT const char *qs_version(void);
+QS_EXPORT qs_status qs_ctx_create(int device, qs_ctx **out);
+QS_EXPORT void qs_ctx_destroy(qs_ctx *ctx);
+/* cudaStream_t of the context (for event timing by the caller). */
+QS_EXPORT void *qs_ctx_stream(qs_ctx *ctx);
+QS_EXPORT qs_status qs_ctx_sync(qs_ctx *ctx);
+/* Kernels launched on this context since creation (for launch accounting). */
+QS_EXPORT int64_t qs_ctx_launches(const qs_ctx *ctx);
+/* Phase timing (no counterpart in the reference; its WB_CLOCK timers,
+ * Source/wbclock.hh:43-377, play this role on the CPU).  When enabled, each
+ * contraction records CUDA events on the context stream around operand
+ * preparation (digit slicing; empty for the FP64 path) and around the GEMM
+ * kernel; qs_ctx_phase_ms waits for the most recent call and returns both
+ * device times in milliseconds. */
+QS_EXPORT qs_status qs_ctx_set_timing(qs_ctx *ctx, int32_t enable);
+QS_EXPORT qs_status qs_ctx_phase_ms(qs_ctx *ctx, double *prep_ms, double *gemm_ms);
+
+/* ------------------------------------------------------- contractQS (host)
+ * C = contractQS(A, ia, B, ib [,perm]) with host buffers in and out.
+ * Replaces the MEX usage #1 path: contract_plain / CONTRACT_QS
+ * (Source/contractQS.cc:505-632) -> QSpace::contract (Source/QSpace.cc:
+ * 4296-4420) with contract_getIdxSet (:4131-4294) and contractDATA_group
+ * (Source/QSpace_aux.cc:27-355).  Labels and block order are bit-exact;
+ * block data match the reference's dgemm/zgemm results to FP rounding (FP64
+ * path) or to opts->tol (split path).  Abelian symmetries (no CGR) only. */
+QS_EXPORT qs_status qs_contractQS(qs_ctx *ctx,
+                        const qs_qspace_view *A, const char *ia,
+                        const qs_qspace_view *B, const char *ib,
+                        const int32_t *perm, int32_t nperm,
+                        const qs_opts *opts, qs_result **C, qs_stats *stats);
+
+QS_EXPORT qs_status qs_result_info(const qs_result *C, int32_t *rank, int32_t *qdim,
+                         int64_t *nblk, int64_t *nelem, int32_t *is_complex);
+/* Copies labels (nblk*rank*qdim), dims (nblk*rank), offsets (nblk) and data
+ * (nelem, x2 doubles when complex) into caller buffers; any may be NULL. */
+QS_EXPORT qs_status qs_result_copy(const qs_result *C, int32_t *q, int64_t *dims,
+                         int64_t *offs, double *data);
+QS_EXPORT void qs_result_free(qs_result *C);
+
+/* --------------------------------------------------- device-resident API */
+QS_EXPORT qs_status qs_tensor_upload(qs_ctx *ctx, const qs_qspace_view *A, qs_tensor **out);
+QS_EXPORT qs_status qs_tensor_info(const qs_tensor *T, int32_t *rank, int32_t *qdim,
+                         int64_t *nblk, int64_t *nelem, int32_t *is_complex);
+QS_EXPORT qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q,
+                             int64_t *dims, int64_t *offs, double *data);
+/* Device pointer of the block data (for callers that keep data on device). */
+QS_EXPORT const double *qs_tensor_data(const qs_tensor *T);
+QS_EXPORT void qs_tensor_free(qs_tensor *T);
+/* Same contraction as qs_contractQS with device-resident operands and result. */
+QS_EXPORT qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char *ia,
+                          const qs_tensor *B, const char *ib,
+                          const int32_t *perm, int32_t nperm,
+                          const qs_opts *opts, qs_tensor **C, qs_stats *stats);
+
+/* ---------------------------------------------------------- permuteQS
+ * B = permuteQS(A, perm [,'conj']) (Source/permuteQS.cc:198-258;
+ * QSpace::Permute Source/QSpace.hh:2670-2719): legs of labels and of every
+ * block are reordered on the device, block order is unchanged. */
+QS_EXPORT qs_status qs_permuteQS(qs_ctx *ctx, const qs_qspace_view *A,
+                       const int32_t *perm, int32_t nperm, int32_t conj,
+                       qs_result **B);
+QS_EXPORT qs_status qs_permute_dev(qs_ctx *ctx, const qs_tensor *A, const int32_t *perm,
+                         int32_t nperm, int32_t conj, qs_tensor **B);
+
+/* ------------------------------------------------- grouped block products
+ * The per-output-block seam of the reference (the OpenMP loop at
+ * Source/QSpace.cc:4375-4393 calling contractDATA_group, which for each block
+ * pair does Ck += afac * Ai*Bi, Source/QSpace_aux.cc:227-235 and
+ * wbarray::contract Source/wbarray.cc:3389-3500 -> DZGEMM Source/
+ * wbarray_blas.cc:121-213).  Pair p computes
+ *     C[c_blk[p]] (+)= afac[p] * op(A_p) * op(B_p)
+ * with op(A_p) an M x K and op(B_p) a K x N column-major view at the given
+ * element offsets and leading dimensions; trans bit 0 transposes A (A stored
+ * K x M), bit 1 transposes B (B stored N x K), bit 2 conjugates A, bit 3
+ * conjugates B.  Pairs that share c_blk are summed in array order into the
+ * same M x N output block (first pair overwrites).  All pointers are device
+ * pointers; element type double or complex128 (is_complex). */
+typedef struct {
+  int64_t npairs;
+  const int32_t *M, *N, *K;
+  const int64_t *a_off, *b_off, *c_off;
+  const int32_t *lda, *ldb, *ldc;
+  const int32_t *trans;
+  const double *afac;     /* real CG / X-symbol factors                      */
+  const int32_t *c_blk;   /* output block id per pair (pairs of one block are
+                             contiguous)                                     */
+  int32_t is_complex;
+} qs_pair_list;
+
+QS_EXPORT qs_status qs_grouped_gemm(qs_ctx *ctx, const qs_pair_list *pairs,
+                          const double *A, const double *B, double *C,
+                          const qs_opts *opts, qs_stats *stats);
+/* Host-buffer form of the same call: A and B are copied in, C (c_elems
+ * elements) is copied out; elements of C outside every output block come
+ * back as zero.  Every access is checked against the given element counts. */
+QS_EXPORT qs_status qs_grouped_gemm_host(qs_ctx *ctx, const qs_pair_list *pairs,
+                               const double *A, int64_t a_elems,
+                               const double *B, int64_t b_elems,
+                               double *C, int64_t c_elems,
+                               const qs_opts *opts, qs_stats *stats);
+
+/* ------------------------------------------------------- eigQS blocks
+ * Hermitian eigendecomposition of every symmetry block on the device in FP64
+ * (the OpenMP loop of QSpace::EigenSymmetric, Source/QSpace.cc:4789-4811,
+ * calling wbEigenS -> dsyevd/zheevd, Source/wbarray_blas.cc:501-660).
+ * blocks: n[i] x n[i] column-major at offs[i] (device pointer `H`); on return
+ * `E` (device, sum n) holds ascending eigenvalues per block at eoffs[i] and
+ * `U` (device, same layout as H) the eigenvectors. */
+QS_EXPORT qs_status qs_eig_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *n,
+                        const int64_t *offs, const int64_t *eoffs,
+                        const double *H, double *E, double *U,
+                        int32_t is_complex);
+
+/* Global truncation over all blocks' eigenvalues (markSet,
+ * Source/gathered.cc:1822-1990, as used by EigenSymmetric :4814): marks the
+ * Nkeep lowest (weighted by multiplet dimension `qdim_w`, NULL = 1), widened to
+ * keep degenerate multiplets within deps, capped by Etrunc when > 0.  Host
+ * arrays; `keep` receives 0/1 per eigenvalue.  Returns the kept count in
+ * *nkeep_out and the truncation energy in *etrunc_out. */
+QS_EXPORT qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E,
+                       const double *qdim_w, int64_t nkeep, double etrunc,
+                       double deps, uint8_t *keep, int64_t *nkeep_out,
+                       double *etrunc_out);
+
+/* -------------------------------------------------------- svdQS blocks
+ * Thin SVD of every block (SVD_Data::blockSVD, Source/mpsortho.cc:546-613 ->
+ * wbSVD -> dgesdd, Source/wbarray_blas.cc:995-1090).  Block i is m[i] x n[i]
+ * column-major at offs[i]; outputs U (m x k), S (k), Vt (k x n) with
+ * k = min(m, n) at uoffs/soffs/voffs.  Device pointers. */
+QS_EXPORT qs_status qs_svd_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *m,
+                        const int64_t *n, const int64_t *offs,
+                        const int64_t *uoffs, const int64_t *soffs,
+                        const int64_t *voffs, const double *A, double *U,
+                        double *S, double *Vt);
+
+/* ------------------------------------------- Davidson re-orthogonalisation
+ * Double classical Gram-Schmidt of vector v (length n) against the nv
+ * orthonormal columns of V (n x nv, column-major), then normalisation
+ * (RunDavidson, Source/david2SiteQS.cc:440-470; GSProject twice).  Device
+ * pointers, FP64.  *norm_out receives |v| before normalisation. */
+QS_EXPORT qs_status qs_gs_reortho(qs_ctx *ctx, int64_t n, int64_t nv, const double *V,
+                        double *v, double *norm_out);
+
+/* ------------------------------------------------------------ serving loop
+ * A continuous-batching request loop (no counterpart in the reference, whose
+ * MEX calls are one at a time).  Requests are contractions between
+ * device-resident tensors; each runs on its own slot stream once admitted
+ * by HBM footprint; completions are polled. */
+typedef struct qs_server qs_server;
+typedef struct {
+  int32_t nslots;          /* concurrent requests on the device               */
+  int32_t pad_;
+  int64_t hbm_budget;      /* bytes of scratch+output the server may hold      */
+} qs_server_cfg;
+QS_EXPORT qs_status qs_server_create(qs_ctx *ctx, const qs_server_cfg *cfg, qs_server **out);
+QS_EXPORT void qs_server_destroy(qs_server *s);
+/* Enqueue; returns a ticket.  Thread-safe. */
+QS_EXPORT qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const char *ia,
+                           const qs_tensor *B, const char *ib,
+                           const int32_t *perm, int32_t nperm,
+                           const qs_opts *opts, int64_t *ticket);
+/* Non-blocking poll (timeout_ms = 0) or bounded wait.  On completion *done = 1
+ * and *C receives the result tensor (owned by the caller), *latency_ms the
+ * submit-to-completion time. */
+QS_EXPORT qs_status qs_server_poll(qs_server *s, int64_t ticket, int32_t timeout_ms,
+                         int32_t *done, qs_tensor **C, double *latency_ms);
+QS_EXPORT qs_status qs_server_cancel(qs_server *s, int64_t ticket);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSGPU_H */

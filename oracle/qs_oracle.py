@@ -1,0 +1,484 @@
+"""CPU oracle for the contractQS hot path -- TEST INFRASTRUCTURE ONLY.
+
+This module is a plain numpy restatement of QSpace's block-sparse contraction
+(``contractQS`` usage #1) and of the helper steps around it.  Only ``tests/``,
+``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference`` legs
+of ``bench.py`` may import it, and only as the checker or as the timed CPU
+baseline.  The product (``qspace_gb300``) never imports it.
+
+Parity pinning: the restatement is checked against golden fixtures produced by
+the reference's own C++ (``contractQS.cc`` compiled behind a fake MATLAB
+runtime, see ``oracle/refshim``) -- ``tests/golden/*.npz`` with the generating
+script ``tests/golden/make_golden.py``.
+
+A QSpace is represented as a plain dict that mirrors QSpace's MATLAB struct
+(``Source/QSpace.hh:3092`` ``{Q,data,info}``):
+
+* ``Q``    -- list (one per leg) of int arrays of shape (nblk, qdim);
+* ``data`` -- list of nblk numpy arrays, each the dense block (any memory
+  order; values are what matter), shape = the leg dimensions (trailing
+  singleton legs may be dropped, as in MATLAB);
+* ``info`` -- optional dict (``itags`` list of str, ``qtype`` str).
+
+Block order and labels are bit-exact with the reference; block data agree to
+floating-point rounding (the reference uses BLAS dgemm/zgemm).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+__all__ = [
+    "parse_ctr_idx", "contract", "permute", "block_dims", "rank_of",
+    "flops_of_contract", "skip_zero_blocks", "lexsort_rows",
+]
+
+
+# --------------------------------------------------------------------------
+# index strings
+# --------------------------------------------------------------------------
+
+def _str2idx(s: str) -> list[int]:
+    """Restates ``Wb::Str2Idx`` (Source/wbio.c, compact mode 'x').
+
+    A single run of alphanumerics with no separators is read digit by digit
+    ('0'-'9' -> 0..9, 'A'-'Z' -> 10.., 'a'-'z' -> 36..); otherwise the tokens
+    separated by ',', ';' or white space are read as integers; optional
+    surrounding brackets are allowed.
+    """
+    t = s.strip()
+    if t.startswith("[") and t.endswith("]"):
+        t = t[1:-1]
+    toks = [x for x in t.replace(",", " ").replace(";", " ").split() if x]
+    if not toks:
+        return []
+    if len(toks) == 1 and not any(c in s for c in ",; "):
+        out = []
+        for c in toks[0]:
+            if "0" <= c <= "9":
+                out.append(ord(c) - 48)
+            elif "A" <= c <= "Z":
+                out.append(ord(c) - 65 + 10)
+            elif "a" <= c <= "z":
+                out.append(ord(c) - 97 + 36)
+            else:
+                raise ValueError(f"invalid contraction index '{s}'")
+        return out
+    return [int(x, 0) for x in toks]
+
+
+def parse_ctr_idx(spec) -> tuple[list[int], bool]:
+    """Contraction index -> (0-based list, conj flag).
+
+    Restates ``ctrIdx::init`` (Source/wbindex.cc:482-540): a string such as
+    '12*' / '1,2*' with trailing '*' for complex conjugation (an even number of
+    '*' cancels), or a 1-based numeric vector (no conj).
+    """
+    if isinstance(spec, str):
+        s = spec.rstrip()
+        nconj = 0
+        while s.endswith("*"):
+            nconj += 1
+            s = s[:-1].rstrip()
+        if s.endswith(",") or s.endswith(";"):
+            s = s[:-1]
+        idx = _str2idx(s)
+        if not idx:
+            raise ValueError(f"empty contraction index '{spec}'")
+        idx = [i - 1 for i in idx]
+        if min(idx) < 0:
+            raise ValueError(f"contraction index must be 1-based '{spec}'")
+        if len(set(idx)) != len(idx):
+            raise ValueError(f"invalid index set '{spec}'")
+        return idx, bool(nconj % 2)
+    idx = [int(x) for x in np.atleast_1d(spec)]
+    if not idx or min(idx) < 1:
+        raise ValueError("contraction index must be 1-based")
+    if len(set(idx)) != len(idx):
+        raise ValueError("invalid index set")
+    return [i - 1 for i in idx], False
+
+
+# --------------------------------------------------------------------------
+# small helpers
+# --------------------------------------------------------------------------
+
+def rank_of(A: dict) -> int:
+    return len(A["Q"])
+
+
+def nblk_of(A: dict) -> int:
+    return 0 if not A["Q"] else int(np.asarray(A["Q"][0]).shape[0])
+
+
+def block_dims(A: dict, i: int) -> tuple[int, ...]:
+    r = rank_of(A)
+    s = tuple(int(x) for x in np.shape(A["data"][i]))
+    if len(s) > r:
+        if any(x != 1 for x in s[r:]):
+            raise ValueError("block has more non-singleton dims than legs")
+        s = s[:r]
+    return s + (1,) * (r - len(s))
+
+
+def qrows(A: dict, legs) -> np.ndarray:
+    """(nblk, len(legs)*qdim) int64 label rows; restates getQsub
+    (Source/QSpace.hh:2290-2340)."""
+    n = nblk_of(A)
+    if not legs:
+        return np.zeros((n, 0), dtype=np.int64)
+    return np.concatenate([np.asarray(A["Q"][k], dtype=np.int64).reshape(n, -1)
+                           for k in legs], axis=1)
+
+
+def lexsort_rows(R: np.ndarray) -> np.ndarray:
+    """Permutation sorting integer rows lexicographically (first column most
+    significant), as ``Wb::recCompare`` with lex=1 (Source/gathered.hh:538)."""
+    if R.shape[0] == 0:
+        return np.zeros(0, dtype=np.int64)
+    if R.shape[1] == 0:
+        return np.arange(R.shape[0])
+    return np.lexsort(R.T[::-1])
+
+
+def _match_index(QA: np.ndarray, QB: np.ndarray):
+    """All (ia, ib) with identical records; restates ``matchIndex``
+    (Source/wbMatrix.cc:2075) and ``Wb::matchSortedIdx`` (Source/wbsort.cc:
+    154-272): sort both, merge, cross product of equal groups."""
+    if QA.shape[0] == 0 or QB.shape[0] == 0:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
+    pa = lexsort_rows(QA)
+    pb = lexsort_rows(QB)
+    Ia, Ib = [], []
+    ia = ib = 0
+    na, nb = len(pa), len(pb)
+    while ia < na and ib < nb:
+        ra, rb = tuple(QA[pa[ia]]), tuple(QB[pb[ib]])
+        if ra < rb:
+            ia += 1
+            continue
+        if ra > rb:
+            ib += 1
+            continue
+        ja = ia
+        while ja < na and tuple(QA[pa[ja]]) == ra:
+            ja += 1
+        jb = ib
+        while jb < nb and tuple(QB[pb[jb]]) == rb:
+            jb += 1
+        for x in range(ia, ja):
+            for y in range(ib, jb):
+                Ia.append(pa[x])
+                Ib.append(pb[y])
+        ia, ib = ja, jb
+    return np.asarray(Ia, np.int64), np.asarray(Ib, np.int64)
+
+
+def _data_size(A: dict) -> int:
+    return int(sum(np.size(d) for d in A["data"]))
+
+
+# --------------------------------------------------------------------------
+# zero-block rules
+# --------------------------------------------------------------------------
+
+def _is_hconj_rank2(Q: list, data: list, eps: float = 1e-14) -> bool:
+    """Abelian ``isHConj`` for a rank-2 QSpace (Source/QSpace.cc:1719-1775,
+    ``isSym_aux`` 1802-): label set invariant under leg swap, unique, and each
+    block equal to the conjugate transpose of its partner within
+    eps*max(1,norm)."""
+    n = Q[0].shape[0]
+    R = np.concatenate([Q[0], Q[1]], axis=1)
+    R2 = np.concatenate([Q[1], Q[0]], axis=1)
+    p1 = lexsort_rows(R)
+    p2 = lexsort_rows(R2)
+    if not np.array_equal(R[p1], R2[p2]):
+        return False
+    S = R[p1]
+    if n > 1 and np.any(np.all(S[1:] == S[:-1], axis=1)):
+        return False
+    nrm = np.sqrt(sum(float(np.vdot(d, d).real) for d in data))
+    deps = max(nrm, 1.0) * eps
+    ip2 = np.empty(n, np.int64)
+    ip2[p2] = np.arange(n)
+    for i in range(n):
+        j = p1[ip2[i]]
+        if j < i:
+            continue
+        di, dj = np.asarray(data[i]), np.asarray(data[j])
+        di = di.reshape(di.shape + (1,) * (2 - di.ndim))
+        dj = dj.reshape(dj.shape + (1,) * (2 - dj.ndim))
+        if di.shape != dj.shape[::-1]:
+            return False
+        if np.max(np.abs(di - np.conj(dj.T)), initial=0.0) > deps:
+            return False
+    return True
+
+
+def _is_blockdiag_d(Q: list, data: list) -> bool:
+    """``isBlockDiagMatrix('d')`` for rank 2 (Source/QSpace.cc:1604-1642):
+    equal labels on both legs and every block stored as a vector."""
+    if not np.array_equal(Q[0], Q[1]):
+        return False
+    for d in data:
+        s = np.shape(d)
+        s = tuple(s) + (1,) * (2 - len(s))
+        if len(s) != 2 or (s[0] != 1 and s[1] != 1):
+            return False
+    return True
+
+
+def skip_zero_blocks(Q: list, data: list) -> tuple[list, list]:
+    """Restates ``SkipZeroData`` with eps=0 (Source/QSpace.cc:3201-3269):
+    exactly-zero blocks are removed, except for a rank-2 QSpace that is
+    block-diagonal in 'd' storage or hermitian, where they are kept."""
+    r = len(Q)
+    if not data:
+        return Q, data
+    keep_all = False
+    if r == 2:
+        if _is_blockdiag_d(Q, data) or _is_hconj_rank2(Q, data):
+            keep_all = True
+    if keep_all:
+        return Q, data
+    keep = [i for i, d in enumerate(data) if np.any(np.asarray(d) != 0)]
+    if len(keep) == len(data):
+        return Q, data
+    Q2 = [q[keep] for q in Q]
+    return Q2, [data[i] for i in keep]
+
+
+# --------------------------------------------------------------------------
+# contraction
+# --------------------------------------------------------------------------
+
+def _co_sort(A, ica, B, icb):
+    """``if (!ica.isSorted() && !icb.isSorted())`` -> sort by the larger
+    tensor (Source/QSpace.cc:4344-4349); only changes the order of the
+    contracted multi-index, not the result."""
+    if ica == sorted(ica) or icb == sorted(icb):
+        return ica, icb
+    if _data_size(A) > _data_size(B):
+        o = np.argsort(ica, kind="stable")
+    else:
+        o = np.argsort(icb, kind="stable")
+    return [ica[i] for i in o], [icb[i] for i in o]
+
+
+def contract(A: dict, ia, B: dict, ib, perm=None, return_plan: bool = False):
+    """C = contractQS(A, ia, B, ib [,perm]) for abelian QSpaces.
+
+    Follows ``contract_plain`` (Source/contractQS.cc:505-594),
+    ``CONTRACT_QS`` (:596-632), ``QSpace::contract`` (Source/QSpace.cc:
+    4296-4420), ``contract_getIdxSet`` (:4131-4294) and the abelian branch of
+    ``contractDATA_group`` (Source/QSpace_aux.cc:27-355, ``afac=1``).
+    ``perm`` is 1-based over the output legs (string or sequence).
+    """
+    ica, conja = parse_ctr_idx(ia)
+    icb, conjb = parse_ctr_idx(ib)
+    ra, rb = rank_of(A), rank_of(B)
+    if nblk_of(A) == 0 or nblk_of(B) == 0:
+        return _empty_like(0)
+    qdA = np.asarray(A["Q"][0]).reshape(nblk_of(A), -1).shape[1]
+    qdB = np.asarray(B["Q"][0]).reshape(nblk_of(B), -1).shape[1]
+    if qdA != qdB:
+        raise ValueError("incompatible objects (QDIM)")
+    if len(ica) != len(icb):
+        raise ValueError("invalid contraction (length mismatch)")
+    if max(ica) >= ra or max(icb) >= rb:
+        raise ValueError("index out of bounds")
+    ica, icb = _co_sort(A, ica, B, icb)
+    ika = [k for k in range(ra) if k not in ica]
+    ikb = [k for k in range(rb) if k not in icb]
+    rc = len(ika) + len(ikb)
+    P = _parse_perm(perm, rc)
+
+    QAc, QAk = qrows(A, ica), qrows(A, ika)
+    QBc, QBk = qrows(B, icb), qrows(B, ikb)
+    Ia, Ib = _match_index(QAc, QBc)
+    if len(Ia) == 0:
+        return _empty_like(rc)
+    QC = np.concatenate([QAk[Ia], QBk[Ib]], axis=1)
+    if rc:
+        p = lexsort_rows(QC)
+        Ia, Ib, QC = Ia[p], Ib[p], QC[p]
+        newgrp = np.ones(len(QC), bool)
+        newgrp[1:] = np.any(QC[1:] != QC[:-1], axis=1)
+        starts = np.flatnonzero(newgrp)
+    else:
+        starts = np.array([0])
+    ends = np.append(starts[1:], len(Ia))
+
+    out_data = []
+    pairs = []
+    for g, (s, e) in enumerate(zip(starts, ends)):
+        acc = None
+        for t in range(s, e):
+            a = np.asarray(A["data"][Ia[t]]).reshape(block_dims(A, Ia[t]), order="A")
+            b = np.asarray(B["data"][Ib[t]]).reshape(block_dims(B, Ib[t]), order="A")
+            for i, (ka, kb) in enumerate(zip(ica, icb)):
+                if a.shape[ka] != b.shape[kb]:
+                    raise ValueError("contracted dimension mismatch")
+            if conja:
+                a = np.conj(a)
+            if conjb:
+                b = np.conj(b)
+            c = np.tensordot(a, b, axes=(ica, icb))
+            acc = c if acc is None else acc + c
+            pairs.append((g, int(Ia[t]), int(Ib[t])))
+        out_data.append(np.asarray(acc))
+    qdim = qdA
+    Qout = [QC[starts, k * qdim:(k + 1) * qdim].astype(np.int32) for k in range(rc)]
+
+    # SkipZeroData inside QSpace::contract, then Permute, then again.
+    Qout, out_data = skip_zero_blocks(Qout, out_data)
+    if P is not None and rc:
+        Qout = [Qout[P[k]] for k in range(rc)]
+        out_data = [np.transpose(d.reshape(d.shape + (1,) * (rc - d.ndim)), P)
+                    for d in out_data]
+    Qout, out_data = skip_zero_blocks(Qout, out_data)
+    info = {}
+    it_a = (A.get("info") or {}).get("itags")
+    it_b = (B.get("info") or {}).get("itags")
+    if it_a and it_b:
+        def cj(t, c):
+            if not c:
+                return t
+            return t[:-1] if t.endswith("*") else t + "*"
+        tags = [cj(it_a[k], conja) for k in ika] + [cj(it_b[k], conjb) for k in ikb]
+        if P is not None:
+            tags = [tags[P[k]] for k in range(rc)]
+        info["itags"] = tags
+    C = {"Q": Qout, "data": out_data, "info": info}
+    if return_plan:
+        return C, {"ica": ica, "icb": icb, "pairs": pairs}
+    return C
+
+
+def _empty_like(rc: int) -> dict:
+    return {"Q": [], "data": [], "info": {}}
+
+
+def _parse_perm(perm, rc):
+    if perm is None or (isinstance(perm, str) and not perm.strip()):
+        return None
+    if isinstance(perm, str):
+        p = _str2idx(perm)
+    else:
+        p = [int(x) for x in np.atleast_1d(perm)]
+    if not p:
+        return None
+    p = [x - 1 for x in p]
+    if sorted(p) != list(range(len(p))) or len(p) > rc:
+        raise ValueError(f"invalid permutation {perm}")
+    if len(p) < rc:
+        p = p + list(range(len(p), rc))
+    return p
+
+
+def permute(A: dict, perm, conj: bool = False) -> dict:
+    """permuteQS(A, perm [,'conj']) for abelian QSpaces (Source/permuteQS.cc:
+    198-258; ``QSpace::Permute`` Source/QSpace.hh:2670-2719): the legs of the
+    labels and of every block are reordered, block order is unchanged."""
+    r = rank_of(A)
+    P = _parse_perm(perm, r)
+    Q = [np.asarray(q) for q in A["Q"]]
+    data = [np.asarray(d).reshape(block_dims(A, i)) for i, d in enumerate(A["data"])]
+    if P is not None:
+        Q = [Q[P[k]] for k in range(r)]
+        data = [np.transpose(d, P) for d in data]
+    if conj:
+        data = [np.conj(d) for d in data]
+    return {"Q": Q, "data": data, "info": dict(A.get("info") or {})}
+
+
+def flops_of_contract(A: dict, ia, B: dict, ib) -> int:
+    """FP64-equivalent flops of one contraction: 2*M*N*K per real pair,
+    8*M*N*K per complex pair, summed over all block pairs."""
+    _, plan = contract(A, ia, B, ib, return_plan=True)
+    ica, icb = plan["ica"], plan["icb"]
+    tot = 0
+    cplx = any(np.iscomplexobj(d) for d in A["data"]) or any(np.iscomplexobj(d) for d in B["data"])
+    for (_, a, b) in plan["pairs"]:
+        da, db = block_dims(A, a), block_dims(B, b)
+        K = int(np.prod([da[k] for k in ica]))
+        M = int(np.prod(da)) // max(K, 1)
+        N = int(np.prod(db)) // max(K, 1)
+        tot += (8 if cplx else 2) * M * N * K
+    return tot
+
+
+# --------------------------------------------------------------------------
+# truncation (markSet) and the Gram-Schmidt step
+# --------------------------------------------------------------------------
+
+def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0):
+    """Kept-eigenvalue mask per block; restates markSet for ascending order
+    (Source/gathered.cc:1822-2040) with eigQS's option handling
+    (Source/eigQS.cc:55-100): deps > 0 averages near-degenerate levels and
+    moves the cut to the largest weighted gap near Nkeep (b=-1, dmax=-1).
+    Returns (list of bool arrays, Nkeep)."""
+    sizes = [len(e) for e in E_blocks]
+    E = np.concatenate([np.asarray(e, float) for e in E_blocks]) if E_blocks else np.zeros(0)
+    N = len(E)
+    keep = np.zeros(N, bool)
+    out = lambda: ([keep[s:s + n] for s, n in zip(np.cumsum([0] + sizes[:-1]), sizes)], int(keep.sum()))
+    if N == 0:
+        return out()
+    P = np.argsort(E, kind="stable")
+    s = E[P].copy()
+    b = -1.0 if deps > 0 else 0.0
+    if deps > 0:
+        eps = deps * abs(s[-1] - s[0])
+        i0 = 0
+        for i in range(1, N + 1):
+            if i == N or abs(s[i] - s[i - 1]) > eps:
+                if i - i0 > 1:
+                    s[i0:i] = np.mean(s[i0:i])
+                i0 = i
+    Nk = N if (nkeep < 0 or nkeep > N) else nkeep
+    if Nk == 0:
+        return out()
+    if Nk >= N and etrunc <= 0:
+        keep[:] = True
+        return out()
+    if etrunc > 0:
+        x = etrunc + s[0]
+        l = 1
+        while l < N and not (s[l] >= x and l > 0):
+            l += 1
+        l = min(l, Nk)
+    else:
+        l = Nk
+    if 0 < l < N and b < 0:
+        nx = max(16, l // 5)
+        q = 10.0 / (-b * nx)
+        NX = int(5.0 / q)
+        i = max(1, l - NX)
+        i2 = min(N, l + NX)
+        imax, xmax = l, 0.0
+        while i < i2:
+            t = q * (i - l)
+            x = np.exp(-t * t) * abs(s[i] - s[i - 1])
+            if x > xmax:
+                xmax, imax = x, i
+            i += 1
+        if i == N:
+            t = q * (i - l)
+            x = 0.1 * np.exp(-t * t) * abs(s[N - 1] - s[0])
+            if x > xmax:
+                xmax, imax = x, i
+        l = imax
+    keep[P[:min(l, N)]] = True
+    return out()
+
+
+def gs_reortho(V: np.ndarray, v: np.ndarray):
+    """Double classical Gram-Schmidt of v against the orthonormal columns of
+    V, then normalisation (Source/david2SiteQS.cc:440-470).  Returns
+    (v_new, |v| before normalisation)."""
+    v = np.array(v, dtype=float)
+    for _ in range(2):
+        if V.shape[1]:
+            v = v - V @ (V.T @ v)
+    n = float(np.linalg.norm(v))
+    return (v / n if n > 0 else v * 0.0), n

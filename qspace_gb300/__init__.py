@@ -1,0 +1,13 @@
+"""qspace_gb300 -- GB300-native block-sparse symmetric tensor contraction.
+
+A drop-in for QSpace's contractQS / permuteQS numerical core (block-sparse
+contraction with exact label bookkeeping) with a plain FP64 path and a
+split-precision BF16 tensor-core path; block eig/SVD and a serving loop.
+The numerical work runs in libqsgpu.so (CUDA for sm_103a) behind the C-ABI
+of include/qsgpu.h.
+"""
+from .qspace import (QSpace, Tensor, Context, contractQS, permuteQS, default_context, upload,
+                     contract_dev, permute_dev)
+
+__all__ = ["QSpace", "Tensor", "Context", "contractQS", "permuteQS", "default_context", "upload",
+           "contract_dev", "permute_dev"]

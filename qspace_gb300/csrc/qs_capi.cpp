@@ -1,0 +1,538 @@
+// C-ABI entry points of libqsgpu (include/qsgpu.h): context, device tensors,
+// contractQS / permuteQS drivers and the grouped block-product seam.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <numeric>
+
+#include "qs_internal.h"
+#include "qs_objects.h"
+#include "qs_plan.h"
+#include "qs_split.h"
+
+namespace qs {
+const std::string &last_error();
+}  // namespace qs
+
+using namespace qs;
+
+namespace qs {
+
+void dev_free(Ctx *ctx, void *p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+void *Ctx::ensure_scratch(size_t bytes) {
+  if (bytes <= scratch_bytes) return scratch;
+  if (scratch) QS_CUDA(cudaFreeAsync(scratch, stream));
+  size_t nb = std::max(bytes, scratch_bytes * 3 / 2);
+  scratch = nullptr;
+  cudaError_t e = cudaMallocAsync(&scratch, nb, stream);
+  if (e != cudaSuccess) {
+    scratch_bytes = 0;
+    fail(e == cudaErrorMemoryAllocation ? QS_ERR_OOM : QS_ERR_CUDA, "scratch allocation of %zu bytes: %s", nb,
+         cudaGetErrorString(e));
+  }
+  scratch_bytes = nb;
+  return scratch;
+}
+
+// Chunk tables for the permute kernel.
+static void run_permute(Ctx *ctx, const std::vector<PermDesc> &descs, const double *in, double *out,
+                        bool cplx) {
+  if (descs.empty()) return;
+  const int CH = 4096;
+  std::vector<int64_t> cb, cs;
+  for (size_t i = 0; i < descs.size(); ++i)
+    for (int64_t s = 0; s < descs[i].n; s += CH) {
+      cb.push_back((int64_t)i);
+      cs.push_back(s);
+    }
+  if (cb.empty()) return;
+  PermDesc *dd = dev_upload(ctx, descs);
+  int64_t *dcb = dev_upload(ctx, cb), *dcs = dev_upload(ctx, cs);
+  launch_permute(ctx, dd, dcb, dcs, (int64_t)cb.size(), in, out, cplx ? 1 : 0, CH);
+  dev_free(ctx, dd);
+  dev_free(ctx, dcb);
+  dev_free(ctx, dcs);
+}
+
+// Rank-2 exemption of SkipZeroData (Source/QSpace.cc:3225-3229): zero blocks
+// of a rank-2 QSpace are kept when it is block diagonal in vector storage or
+// hermitian (isHConj, Source/QSpace.cc:1719-1775 -> isSym_aux :1802-).
+static bool rank2_keeps_zero_blocks(const QMeta &m, const std::vector<double> &h) {
+  const int qd = m.qdim;
+  // 'd' storage: labels equal on both legs, every block a vector
+  bool dstore = true;
+  for (int64_t i = 0; i < m.nblk && dstore; ++i) {
+    if (rec_compare(m.qrow(i), m.qrow(i) + qd, qd) != 0) dstore = false;
+    const int64_t *d = m.drow(i);
+    if (d[0] != 1 && d[1] != 1) dstore = false;
+  }
+  if (dstore) return true;
+  // hermitian: the label set is invariant under leg swap, labels unique,
+  // and data(i) == data(j)^H within 1e-14 * max(1, |A|)
+  const int64_t n = m.nblk;
+  const int w = 2 * qd;
+  std::vector<int32_t> R(n * w), R2(n * w);
+  for (int64_t i = 0; i < n; ++i) {
+    std::memcpy(&R[i * w], m.qrow(i), w * 4);
+    std::memcpy(&R2[i * w], m.qrow(i) + qd, qd * 4);
+    std::memcpy(&R2[i * w + qd], m.qrow(i), qd * 4);
+  }
+  auto sp = [&](const std::vector<int32_t> &X) {
+    std::vector<int64_t> p(n);
+    std::iota(p.begin(), p.end(), 0);
+    std::stable_sort(p.begin(), p.end(), [&](int64_t a, int64_t b) { return rec_compare(&X[a * w], &X[b * w], w) < 0; });
+    return p;
+  };
+  std::vector<int64_t> p1 = sp(R), p2 = sp(R2);
+  for (int64_t i = 0; i < n; ++i)
+    if (rec_compare(&R[p1[i] * w], &R2[p2[i] * w], w) != 0) return false;
+  for (int64_t i = 1; i < n; ++i)
+    if (rec_compare(&R[p1[i] * w], &R[p1[i - 1] * w], w) == 0) return false;
+  const int es = m.cplx ? 2 : 1;
+  double nrm2 = 0;
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = 0; e < m.bsize(i) * es; ++e) nrm2 += h[m.offs[i] * es + e] * h[m.offs[i] * es + e];
+  const double deps = std::max(std::sqrt(nrm2), 1.0) * 1e-14;
+  std::vector<int64_t> ip2(n);
+  for (int64_t i = 0; i < n; ++i) ip2[p2[i]] = i;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t j = p1[ip2[i]];
+    if (j < i) continue;
+    const int64_t *di = m.drow(i), *dj = m.drow(j);
+    if (di[0] != dj[1] || di[1] != dj[0]) return false;
+    for (int64_t r = 0; r < di[0]; ++r)
+      for (int64_t c = 0; c < di[1]; ++c) {
+        const int64_t a = m.offs[i] + r + c * di[0], b = m.offs[j] + c + r * dj[0];
+        const double re = h[a * es] - h[b * es];
+        const double im = m.cplx ? h[a * es + 1] + h[b * es + 1] : 0.0;
+        if (std::fabs(re) > deps || std::fabs(im) > deps) return false;
+      }
+  }
+  return true;
+}
+
+static std::unique_ptr<qs_tensor> empty_tensor(Ctx *ctx, int rank, int qdim, bool cplx) {
+  auto T = std::make_unique<qs_tensor>();
+  T->ctx = ctx;
+  T->meta.rank = rank;
+  T->meta.qdim = qdim;
+  T->meta.cplx = cplx;
+  return T;
+}
+
+// The device contraction driver shared by the host and device entry points.
+std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double *dA,
+                                                const QMeta &Bm, const double *dB, const char *ia,
+                                                const char *ib, const int32_t *perm, int32_t nperm,
+                                                const qs_opts *opts, qs_stats *stats) {
+  const int64_t launches0 = ctx->launches;
+  ContractPlan pl = plan_contract(Am, ia, Bm, ib, perm, nperm);
+  const bool cplx = pl.C.cplx;
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->flops = pl.flops;
+    stats->bytes = pl.bytes;
+    stats->npairs = (int64_t)pl.pairs.size();
+  }
+  if (pl.C.nblk == 0) return empty_tensor(ctx, 0, Am.qdim, cplx);
+  const int es = cplx ? 2 : 1;
+
+  // Operands in the element type of the result, in the layout the plan wants.
+  std::vector<void *> tmp;
+  auto prep = [&](const QMeta &m, const double *d, const OperandLayout &lay) -> const double * {
+    const double *cur = d;
+    if (cplx && !m.cplx) {
+      double *w = dev_alloc<double>(ctx, (size_t)m.nelem * 2);
+      tmp.push_back(w);
+      launch_widen(ctx, d, w, m.nelem);
+      cur = w;
+    }
+    if (lay.permute) {
+      double *o = dev_alloc<double>(ctx, (size_t)m.nelem * es);
+      tmp.push_back(o);
+      std::vector<PermDesc> pd = make_perm_descs(m, lay.perm, false, m.offs);
+      run_permute(ctx, pd, cur, o, cplx);
+      cur = o;
+    }
+    return cur;
+  };
+  const double *a2 = prep(Am, dA, pl.la);
+  const double *b2 = prep(Bm, dB, pl.lb);
+
+  double *dC = dev_alloc<double>(ctx, (size_t)pl.C.nelem * es);
+  const int prec = opts ? opts->prec : QS_PREC_FP64;
+  std::vector<int64_t> c_off = pl.C.offs;
+  if (prec == QS_PREC_SPLIT) {
+    SplitResult sr = run_split(ctx, pl.pairs, pl.grp, pl.blk_M, pl.blk_N, c_off, a2, b2, dC, cplx,
+                               opts ? opts->nslices : 0, opts && opts->tol > 0 ? opts->tol : 1e-12);
+    if (stats) {
+      stats->nslices = sr.nslices;
+      stats->digit_bits = sr.bits;
+      stats->err_bound = sr.err_bound;
+    }
+  } else if (prec == QS_PREC_FP64) {
+    std::vector<TileDesc> tiles =
+        make_tiles(pl.grp, pl.blk_M, pl.blk_N, c_off, gemm_f64_tile_m(), gemm_f64_tile_n());
+    PairDesc *dp = dev_upload(ctx, pl.pairs);
+    TileDesc *dt = dev_upload(ctx, tiles);
+    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), a2, b2, dC, cplx ? 1 : 0);
+    dev_free(ctx, dp);
+    dev_free(ctx, dt);
+  } else {
+    fail(QS_ERR_ARG, "unknown precision mode %d", prec);
+  }
+  for (void *p : tmp) dev_free(ctx, p);
+
+  // SkipZeroData: drop exactly-zero output blocks (with the rank-2 rule).
+  const int64_t nb = pl.C.nblk;
+  std::vector<int64_t> sizes(nb);
+  for (int64_t i = 0; i < nb; ++i) sizes[i] = pl.C.bsize(i);
+  int64_t *doff = dev_upload(ctx, pl.C.offs), *dsz = dev_upload(ctx, sizes);
+  int *dflag = dev_alloc<int>(ctx, nb);
+  launch_block_nonzero(ctx, doff, dsz, nb, dC, cplx ? 1 : 0, dflag);
+  std::vector<int> flags(nb);
+  int kerr = 0;
+  QS_CUDA(cudaMemcpyAsync(flags.data(), dflag, nb * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaMemcpyAsync(&kerr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (kerr) {
+    QS_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    fail(QS_ERR_TIMEOUT, "a bounded device wait ran out (code %d)", kerr);
+  }
+  dev_free(ctx, doff);
+  dev_free(ctx, dsz);
+  dev_free(ctx, dflag);
+  std::vector<int64_t> keep;
+  for (int64_t i = 0; i < nb; ++i)
+    if (flags[i]) keep.push_back(i);
+  if ((int64_t)keep.size() < nb && pl.rc == 2) {
+    std::vector<double> h((size_t)pl.C.nelem * es);
+    QS_CUDA(cudaMemcpyAsync(h.data(), dC, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QS_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (rank2_keeps_zero_blocks(pl.C, h)) {
+      keep.resize(nb);
+      std::iota(keep.begin(), keep.end(), 0);
+    }
+  }
+
+  auto T = std::make_unique<qs_tensor>();
+  T->ctx = ctx;
+  QMeta &M = T->meta;
+  M.rank = pl.rc;
+  M.qdim = pl.C.qdim;
+  M.cplx = cplx;
+  M.nblk = (int64_t)keep.size();
+  const int r = pl.rc, qd = pl.C.qdim;
+  if (keep.empty()) {
+    dev_free(ctx, dC);
+    M.rank = 0;
+    if (stats) stats->launches = (int32_t)(ctx->launches - launches0);
+    return T;
+  }
+  if (pl.P.empty()) {
+    for (int64_t i : keep) {
+      M.q.insert(M.q.end(), pl.C.qrow(i), pl.C.qrow(i) + r * qd);
+      M.dims.insert(M.dims.end(), pl.C.drow(i), pl.C.drow(i) + r);
+      M.offs.push_back(pl.C.offs[i]);
+    }
+    M.nelem = pl.C.nelem;
+    T->d = dC;
+  } else {
+    // Permute(P) of labels and data (Source/QSpace.hh:2670-2719); the block
+    // order is not changed.
+    std::vector<int64_t> noffs;
+    int64_t ne = 0;
+    for (int64_t i : keep) {
+      for (int k = 0; k < r; ++k) {
+        const int32_t *src = pl.C.qrow(i) + pl.P[k] * qd;
+        M.q.insert(M.q.end(), src, src + qd);
+        M.dims.push_back(pl.C.drow(i)[pl.P[k]]);
+      }
+      noffs.push_back(ne);
+      ne += pl.C.bsize(i);
+    }
+    M.offs = noffs;
+    M.nelem = ne;
+    double *dP = dev_alloc<double>(ctx, (size_t)ne * es);
+    std::vector<PermDesc> pd = make_perm_descs(pl.C, pl.P, false, noffs, &keep);
+    run_permute(ctx, pd, dC, dP, cplx);
+    dev_free(ctx, dC);
+    T->d = dP;
+  }
+  if (stats) {
+    stats->nblk_out = M.nblk;
+    stats->launches = (int32_t)(ctx->launches - launches0);
+  }
+  return T;
+}
+
+int64_t contract_footprint(const QMeta &Am, const QMeta &Bm, const char *ia, const char *ib,
+                           const qs_opts *opts) {
+  ContractPlan pl = plan_contract(Am, ia, Bm, ib, nullptr, 0);
+  const int64_t es = pl.C.cplx ? 16 : 8;
+  int64_t fp = pl.C.nelem * es * 2;  // result, and its permuted copy
+  if (pl.la.permute || (pl.C.cplx && !Am.cplx)) fp += Am.nelem * es * 2;
+  if (pl.lb.permute || (pl.C.cplx && !Bm.cplx)) fp += Bm.nelem * es * 2;
+  if (opts && opts->prec == QS_PREC_SPLIT) {
+    // at most 8 BF16 digits of every pair operand, padded to 128x32 / 64x32
+    const int64_t cm = pl.C.cplx ? 2 : 1;
+    for (const PairDesc &d : pl.pairs) {
+      const int64_t Mr = d.M * cm, Kr = std::max<int64_t>(d.K * cm, 1);
+      const int64_t rows = (Mr + 127) / 128 * 128 + (d.N + 63) / 64 * 64;
+      fp += rows * ((Kr + 31) / 32 * 32) * 2 * 8;
+    }
+  }
+  return fp;
+}
+
+static std::unique_ptr<qs_tensor> upload(Ctx *ctx, const qs_qspace_view *v) {
+  QMeta m = meta_from_view(v);
+  auto T = std::make_unique<qs_tensor>();
+  T->ctx = ctx;
+  T->meta = m;
+  const size_t n = (size_t)m.nelem * (m.cplx ? 2 : 1);
+  T->d = dev_alloc<double>(ctx, n);
+  if (n) QS_CUDA(cudaMemcpyAsync(T->d, v->data, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  return T;
+}
+
+static qs_result *download(Ctx *ctx, const qs_tensor *T) {
+  auto R = std::make_unique<qs_result>();
+  const QMeta &m = T->meta;
+  R->meta = m;
+  const int es = m.cplx ? 2 : 1;
+  std::vector<double> h((size_t)m.nelem * es);
+  if (!h.empty()) {
+    QS_CUDA(cudaMemcpyAsync(h.data(), T->d, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  int64_t ne = 0;
+  for (int64_t i = 0; i < m.nblk; ++i) ne += m.bsize(i);
+  R->data.resize((size_t)ne * es);
+  R->meta.nelem = ne;
+  int64_t o = 0;
+  for (int64_t i = 0; i < m.nblk; ++i) {
+    const int64_t s = m.bsize(i);
+    if (s) std::memcpy(&R->data[o * es], &h[m.offs[i] * es], s * es * 8);
+    R->meta.offs[i] = o;
+    o += s;
+  }
+  return R.release();
+}
+
+}  // namespace qs
+
+// ======================================================================= C-ABI
+extern "C" {
+
+const char *qs_last_error(void) { return qs::last_error().c_str(); }
+const char *qs_version(void) { return "qsgpu 0.1 (sm_103a)"; }
+
+qs_status qs_ctx_create(int device, qs_ctx **out) {
+  QS_API_BEGIN
+  if (!out) fail(QS_ERR_ARG, "null out");
+  auto c = std::make_unique<qs_ctx>();
+  c->c.device = device;
+  QS_CUDA(cudaSetDevice(device));
+  QS_CUDA(cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking));
+  QS_CUDA(cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+  // keep freed stream-ordered memory cached in the pool between calls
+  cudaMemPool_t pool;
+  QS_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t thr = UINT64_MAX;
+  QS_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  QS_CUDA(cudaMalloc(&c->c.d_err, 64));
+  QS_CUDA(cudaMemset(c->c.d_err, 0, 64));
+  *out = c.release();
+  QS_API_END
+}
+
+void qs_ctx_destroy(qs_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c.device);
+  if (ctx->c.scratch) cudaFreeAsync(ctx->c.scratch, ctx->c.stream);
+  destroy_solver(&ctx->c);
+  cudaStreamSynchronize(ctx->c.stream);
+  if (ctx->c.d_err) cudaFree(ctx->c.d_err);
+  for (auto &e : ctx->c.ev)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+}
+
+void *qs_ctx_stream(qs_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+qs_status qs_ctx_sync(qs_ctx *ctx) {
+  QS_API_BEGIN
+  if (!ctx) fail(QS_ERR_ARG, "null ctx");
+  QS_CUDA(cudaStreamSynchronize(ctx->c.stream));
+  QS_API_END
+}
+
+int64_t qs_ctx_launches(const qs_ctx *ctx) { return ctx ? ctx->c.launches : 0; }
+
+qs_status qs_ctx_set_timing(qs_ctx *ctx, int32_t enable) {
+  QS_API_BEGIN
+  if (!ctx) fail(QS_ERR_ARG, "null ctx");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  for (auto &e : ctx->c.ev)
+    if (!e) QS_CUDA(cudaEventCreate(&e));
+  ctx->c.timing = enable != 0;
+  ctx->c.ev_used = false;
+  QS_API_END
+}
+
+qs_status qs_ctx_phase_ms(qs_ctx *ctx, double *prep_ms, double *gemm_ms) {
+  QS_API_BEGIN
+  if (!ctx) fail(QS_ERR_ARG, "null ctx");
+  if (!ctx->c.ev_used) fail(QS_ERR_ARG, "no timed call on this context");
+  QS_CUDA(cudaEventSynchronize(ctx->c.ev[2]));
+  float a = 0, b = 0;
+  QS_CUDA(cudaEventElapsedTime(&a, ctx->c.ev[0], ctx->c.ev[1]));
+  QS_CUDA(cudaEventElapsedTime(&b, ctx->c.ev[1], ctx->c.ev[2]));
+  if (prep_ms) *prep_ms = a;
+  if (gemm_ms) *gemm_ms = b;
+  QS_API_END
+}
+
+qs_status qs_contractQS(qs_ctx *ctx, const qs_qspace_view *A, const char *ia,
+                        const qs_qspace_view *B, const char *ib, const int32_t *perm,
+                        int32_t nperm, const qs_opts *opts, qs_result **C, qs_stats *stats) {
+  QS_API_BEGIN
+  if (!ctx || !C) fail(QS_ERR_ARG, "null argument");
+  *C = nullptr;
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  auto tA = upload(&ctx->c, A);
+  auto tB = upload(&ctx->c, B);
+  auto tC = contract_core(&ctx->c, tA->meta, tA->d, tB->meta, tB->d, ia, ib, perm, nperm, opts, stats);
+  *C = download(&ctx->c, tC.get());
+  QS_API_END
+}
+
+qs_status qs_result_info(const qs_result *C, int32_t *rank, int32_t *qdim, int64_t *nblk,
+                         int64_t *nelem, int32_t *is_complex) {
+  QS_API_BEGIN
+  if (!C) fail(QS_ERR_ARG, "null result");
+  if (rank) *rank = C->meta.rank;
+  if (qdim) *qdim = C->meta.qdim;
+  if (nblk) *nblk = C->meta.nblk;
+  if (nelem) *nelem = C->meta.nelem;
+  if (is_complex) *is_complex = C->meta.cplx ? 1 : 0;
+  QS_API_END
+}
+
+qs_status qs_result_copy(const qs_result *C, int32_t *q, int64_t *dims, int64_t *offs, double *data) {
+  QS_API_BEGIN
+  if (!C) fail(QS_ERR_ARG, "null result");
+  const QMeta &m = C->meta;
+  if (q && !m.q.empty()) std::memcpy(q, m.q.data(), m.q.size() * 4);
+  if (dims && !m.dims.empty()) std::memcpy(dims, m.dims.data(), m.dims.size() * 8);
+  if (offs && !m.offs.empty()) std::memcpy(offs, m.offs.data(), m.offs.size() * 8);
+  if (data && !C->data.empty()) std::memcpy(data, C->data.data(), C->data.size() * 8);
+  QS_API_END
+}
+
+void qs_result_free(qs_result *C) { delete C; }
+
+qs_status qs_tensor_upload(qs_ctx *ctx, const qs_qspace_view *A, qs_tensor **out) {
+  QS_API_BEGIN
+  if (!ctx || !out) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  *out = upload(&ctx->c, A).release();
+  QS_API_END
+}
+
+qs_status qs_tensor_info(const qs_tensor *T, int32_t *rank, int32_t *qdim, int64_t *nblk,
+                         int64_t *nelem, int32_t *is_complex) {
+  QS_API_BEGIN
+  if (!T) fail(QS_ERR_ARG, "null tensor");
+  int64_t ne = 0;
+  for (int64_t i = 0; i < T->meta.nblk; ++i) ne += T->meta.bsize(i);
+  if (rank) *rank = T->meta.rank;
+  if (qdim) *qdim = T->meta.qdim;
+  if (nblk) *nblk = T->meta.nblk;
+  if (nelem) *nelem = ne;
+  if (is_complex) *is_complex = T->meta.cplx ? 1 : 0;
+  QS_API_END
+}
+
+qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q, int64_t *dims,
+                             int64_t *offs, double *data) {
+  QS_API_BEGIN
+  if (!ctx || !T) fail(QS_ERR_ARG, "null argument");
+  std::unique_ptr<qs_result> R(download(&ctx->c, T));
+  return qs_result_copy(R.get(), q, dims, offs, data);
+  QS_API_END
+}
+
+const double *qs_tensor_data(const qs_tensor *T) { return T ? T->d : nullptr; }
+
+void qs_tensor_free(qs_tensor *T) { delete T; }
+
+qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char *ia, const qs_tensor *B,
+                          const char *ib, const int32_t *perm, int32_t nperm, const qs_opts *opts,
+                          qs_tensor **C, qs_stats *stats) {
+  QS_API_BEGIN
+  if (!ctx || !A || !B || !C) fail(QS_ERR_ARG, "null argument");
+  *C = nullptr;
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  *C = contract_core(&ctx->c, A->meta, A->d, B->meta, B->d, ia, ib, perm, nperm, opts, stats).release();
+  QS_API_END
+}
+
+static std::unique_ptr<qs_tensor> permute_core(Ctx *ctx, const QMeta &m, const double *d,
+                                               const int32_t *perm, int32_t nperm, int32_t conj) {
+  std::vector<int> P = parse_perm(perm, nperm, m.rank);
+  auto T = std::make_unique<qs_tensor>();
+  T->ctx = ctx;
+  QMeta &M = T->meta;
+  M.rank = m.rank;
+  M.qdim = m.qdim;
+  M.nblk = m.nblk;
+  M.cplx = m.cplx;
+  const int r = m.rank, qd = m.qdim;
+  int64_t ne = 0;
+  for (int64_t i = 0; i < m.nblk; ++i) {
+    for (int k = 0; k < r; ++k) {
+      const int src = P.empty() ? k : P[k];
+      M.q.insert(M.q.end(), m.qrow(i) + src * qd, m.qrow(i) + (src + 1) * qd);
+      M.dims.push_back(m.drow(i)[src]);
+    }
+    M.offs.push_back(ne);
+    ne += m.bsize(i);
+  }
+  M.nelem = ne;
+  const int es = m.cplx ? 2 : 1;
+  T->d = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(ne, 1) * es);
+  std::vector<PermDesc> pd = make_perm_descs(m, P, conj && m.cplx, M.offs);
+  run_permute(ctx, pd, d, T->d, m.cplx);
+  return T;
+}
+
+qs_status qs_permuteQS(qs_ctx *ctx, const qs_qspace_view *A, const int32_t *perm, int32_t nperm,
+                       int32_t conj, qs_result **B) {
+  QS_API_BEGIN
+  if (!ctx || !B) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  auto tA = upload(&ctx->c, A);
+  auto tB = permute_core(&ctx->c, tA->meta, tA->d, perm, nperm, conj);
+  *B = download(&ctx->c, tB.get());
+  QS_API_END
+}
+
+qs_status qs_permute_dev(qs_ctx *ctx, const qs_tensor *A, const int32_t *perm, int32_t nperm,
+                         int32_t conj, qs_tensor **B) {
+  QS_API_BEGIN
+  if (!ctx || !A || !B) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  *B = permute_core(&ctx->c, A->meta, A->d, perm, nperm, conj).release();
+  QS_API_END
+}
+
+}  // extern "C"

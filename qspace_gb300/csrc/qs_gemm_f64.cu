@@ -1,0 +1,149 @@
+// Plain FP64 grouped block GEMM: the drop-in numerical path.
+//
+// Replaces the per-pair dgemm/zgemm of contractDATA_group (Source/
+// QSpace_aux.cc:27-355 -> wbarray::contract Source/wbarray.cc:3389-3500 ->
+// DZGEMM Source/wbarray_blas.cc:121-213).  One CTA owns one 64x64 tile of one
+// output block and sums all block pairs of that block in plan order, so the
+// result is deterministic and needs no atomics.  The K loop stages 64xKC
+// panels of op(A) and KCx64 panels of op(B) in shared memory (coalesced
+// loads in either storage order); each thread accumulates a 4x4 sub-tile in
+// registers with FP64 FMAs (GB300's FP64 rate, not memory, bounds this path).
+#include <type_traits>
+
+#include "qs_internal.h"
+
+namespace qs {
+
+namespace {
+constexpr int TM = 64, TN = 64;
+
+__device__ __forceinline__ double cmul_re(double2 a, double2 b) { return a.x * b.x - a.y * b.y; }
+
+template <bool CPLX>
+struct Elem;
+template <>
+struct Elem<false> {
+  using T = double;
+  static constexpr int KC = 16;
+  __device__ static T zero() { return 0.0; }
+  __device__ static T load(const double *p, int64_t i, bool /*conj*/, double f) { return p[i] * f; }
+  __device__ static void fma(T &c, T a, T b) { c = ::fma(a, b, c); }
+  __device__ static void store(double *p, int64_t i, T v) { p[i] = v; }
+};
+template <>
+struct Elem<true> {
+  using T = double2;
+  static constexpr int KC = 8;
+  __device__ static T zero() { return make_double2(0.0, 0.0); }
+  __device__ static T load(const double *p, int64_t i, bool conj, double f) {
+    double2 v = reinterpret_cast<const double2 *>(p)[i];
+    return make_double2(v.x * f, (conj ? -v.y : v.y) * f);
+  }
+  __device__ static void fma(T &c, T a, T b) {
+    c.x = ::fma(a.x, b.x, c.x);
+    c.x = ::fma(-a.y, b.y, c.x);
+    c.y = ::fma(a.x, b.y, c.y);
+    c.y = ::fma(a.y, b.x, c.y);
+  }
+  __device__ static void store(double *p, int64_t i, T v) { reinterpret_cast<double2 *>(p)[i] = v; }
+};
+
+template <bool CPLX>
+__global__ void __launch_bounds__(256)
+gemm_f64_kernel(const PairDesc *__restrict__ pairs, const TileDesc *__restrict__ tiles,
+                const double *__restrict__ A, const double *__restrict__ B, double *__restrict__ C) {
+  using E = Elem<CPLX>;
+  using T = typename E::T;
+  constexpr int KC = E::KC;
+  __shared__ T As[KC][TM + 1];
+  __shared__ T Bs[KC][TN + 1];
+
+  const TileDesc t = tiles[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = E::zero();
+
+  for (int p = t.p0; p < t.p1; ++p) {
+    const PairDesc pd = pairs[p];
+    const bool ta = pd.trans & 1, tb = pd.trans & 2;
+    const bool ca = pd.trans & 4, cb = pd.trans & 8;
+    for (int k0 = 0; k0 < pd.K; k0 += KC) {
+      // op(A)(m,k): stored M x K (m fastest) or K x M (k fastest)
+#pragma unroll
+      for (int e = tid; e < TM * KC; e += 256) {
+        int mm, kk;
+        if (ta) { kk = e % KC; mm = e / KC; }
+        else    { mm = e % TM; kk = e / TM; }
+        const int m = t.m0 + mm, k = k0 + kk;
+        T v = E::zero();
+        if (m < pd.M && k < pd.K)
+          v = E::load(A, pd.a_off + (ta ? (int64_t)k + (int64_t)m * pd.lda
+                                        : (int64_t)m + (int64_t)k * pd.lda), ca, pd.afac);
+        As[kk][mm] = v;
+      }
+      // op(B)(k,n): stored K x N (k fastest) or N x K (n fastest)
+#pragma unroll
+      for (int e = tid; e < TN * KC; e += 256) {
+        int nn, kk;
+        if (tb) { nn = e % TN; kk = e / TN; }
+        else    { kk = e % KC; nn = e / KC; }
+        const int n = t.n0 + nn, k = k0 + kk;
+        T v = E::zero();
+        if (n < pd.N && k < pd.K)
+          v = E::load(B, pd.b_off + (tb ? (int64_t)n + (int64_t)k * pd.ldb
+                                        : (int64_t)k + (int64_t)n * pd.ldb), cb, 1.0);
+        Bs[kk][nn] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < KC; ++kk) {
+        T a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) E::fma(acc[i][j], a[i], b[j]);
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int n = t.n0 + ty + 16 * j;
+    if (n >= t.N) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = t.m0 + tx + 16 * i;
+      if (m < t.M) E::store(C, t.c_off + (int64_t)m + (int64_t)n * t.ldc, acc[i][j]);
+    }
+  }
+}
+}  // namespace
+
+int gemm_f64_tile_m() { return TM; }
+int gemm_f64_tile_n() { return TN; }
+
+void launch_gemm_f64(Ctx *ctx, const PairDesc *d_pairs, const TileDesc *d_tiles,
+                     int64_t ntiles, const double *A, const double *B, double *C,
+                     int is_complex) {
+  if (ntiles <= 0) return;
+  if (ntiles > 0x7fffffff) fail(QS_ERR_SHAPE, "gemm_f64: too many tiles");
+  ctx->mark(0);
+  ctx->mark(1);
+  if (is_complex)
+    gemm_f64_kernel<true><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(d_pairs, d_tiles, A, B, C);
+  else
+    gemm_f64_kernel<false><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(d_pairs, d_tiles, A, B, C);
+  QS_LAUNCHED(ctx);
+  ctx->mark(2);
+}
+
+}  // namespace qs

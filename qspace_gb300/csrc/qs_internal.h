@@ -1,0 +1,173 @@
+// Internal declarations of libqsgpu: error handling, device work descriptors
+// and the kernel launchers shared between the host planner (qs_plan.cpp,
+// qs_capi.cpp) and the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/qsgpu.h"
+
+namespace qs {
+
+// ------------------------------------------------------------------ errors
+struct Error : std::runtime_error {
+  qs_status code;
+  Error(qs_status c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(qs_status code, const char *fmt, ...);
+void set_last_error(const std::string &msg);
+
+#define QS_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      ::qs::fail(QS_ERR_CUDA, "%s:%d %s -> %s", __FILE__, __LINE__, #call,   \
+                 cudaGetErrorString(e_));                                    \
+  } while (0)
+
+// Check the most recent launch.
+#define QS_LAUNCHED(ctx)                                                     \
+  do {                                                                       \
+    cudaError_t e_ = cudaGetLastError();                                     \
+    if (e_ != cudaSuccess)                                                   \
+      ::qs::fail(QS_ERR_CUDA, "%s:%d kernel launch -> %s", __FILE__,         \
+                 __LINE__, cudaGetErrorString(e_));                          \
+    (ctx)->launches++;                                                       \
+  } while (0)
+
+// ------------------------------------------------------------------ context
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int64_t launches = 0;
+  // device error word for bounded waits inside kernels (0 = ok)
+  int *d_err = nullptr;
+  // pooled scratch (grown on demand, stream ordered)
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+  void *ensure_scratch(size_t bytes);
+  // cuSOLVER handle (created on first use)
+  void *solver = nullptr;
+  // phase timing: events around operand preparation and the GEMM kernel
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  bool ev_used = false;
+  void mark(int i) {
+    if (timing && ev[i]) {
+      cudaEventRecord(ev[i], stream);
+      if (i == 2) ev_used = true;
+    }
+  }
+};
+
+// --------------------------------------------- device work descriptors
+// One block product C[c] (+)= afac * op(A) * op(B), element offsets in units
+// of the element type (double or complex).
+struct PairDesc {
+  int64_t a_off, b_off;
+  int32_t M, N, K;
+  int32_t lda, ldb;
+  int32_t trans;   // bit0 transA, bit1 transB, bit2 conjA, bit3 conjB
+  double afac;
+};
+static_assert(sizeof(PairDesc) == 48, "PairDesc layout");
+
+// One output tile of one output block: the pairs [p0, p1) all write block c.
+struct TileDesc {
+  int64_t c_off;
+  int32_t p0, p1;
+  int32_t m0, n0;
+  int32_t M, N;
+  int32_t ldc;
+  int32_t cblk;
+};
+static_assert(sizeof(TileDesc) == 40, "TileDesc layout");
+
+// Generalised transpose of one block: out(j0..jr) = in(P-permuted index).
+struct PermDesc {
+  int64_t in_off, out_off;
+  int64_t n;            // elements
+  int32_t rank;
+  int32_t conj;
+  int64_t out_dims[8];
+  int64_t in_stride[8]; // stride in the input of output leg k
+};
+
+// ------------------------------------------------------- kernel launchers
+// qs_permute.cu
+void launch_permute(Ctx *ctx, const PermDesc *d_desc, const int64_t *d_chunk_blk,
+                    const int64_t *d_chunk_start, int64_t nchunks, const double *in,
+                    double *out, int is_complex, int chunk_elems);
+
+// qs_gemm_f64.cu -- plain FP64 grouped GEMM (deterministic: one CTA owns an
+// output tile, pairs summed in order)
+void launch_gemm_f64(Ctx *ctx, const PairDesc *d_pairs, const TileDesc *d_tiles,
+                     int64_t ntiles, const double *A, const double *B, double *C,
+                     int is_complex);
+int gemm_f64_tile_m();
+int gemm_f64_tile_n();
+
+// qs_permute.cu -- per-block "all zero" test for SkipZeroData, and the
+// real -> complex widening of an operand arena
+void launch_block_nonzero(Ctx *ctx, const int64_t *d_offs, const int64_t *d_sizes,
+                          int64_t nblk, const double *data, int is_complex,
+                          int *d_flags);
+void launch_widen(Ctx *ctx, const double *in, double *out, int64_t n);
+
+// qs_linalg.cu
+void destroy_solver(Ctx *ctx);
+
+// ------------------------------------------------------ small utilities
+template <class T>
+T *dev_alloc(Ctx *ctx, size_t n) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMallocAsync(&p, n * sizeof(T), ctx->stream);
+  if (e != cudaSuccess)
+    fail(e == cudaErrorMemoryAllocation ? QS_ERR_OOM : QS_ERR_CUDA,
+         "cudaMallocAsync(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
+  return static_cast<T *>(p);
+}
+void dev_free(Ctx *ctx, void *p);
+
+template <class T>
+T *dev_upload(Ctx *ctx, const std::vector<T> &v) {
+  T *p = dev_alloc<T>(ctx, v.size());
+  if (!v.empty())
+    QS_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T),
+                            cudaMemcpyHostToDevice, ctx->stream));
+  return p;
+}
+
+}  // namespace qs
+
+// C-ABI context object: one device, one stream, one memory pool.
+struct qs_ctx {
+  qs::Ctx c;
+};
+
+// Exception-to-status translation at every C-ABI entry point.
+#define QS_API_BEGIN try {
+#define QS_API_END                                \
+  }                                               \
+  catch (const qs::Error &e) {                    \
+    qs::set_last_error(e.what());                 \
+    return e.code;                                \
+  }                                               \
+  catch (const std::bad_alloc &) {                \
+    qs::set_last_error("host allocation failed"); \
+    return QS_ERR_OOM;                            \
+  }                                               \
+  catch (const std::exception &e) {               \
+    qs::set_last_error(e.what());                 \
+    return QS_ERR_INTERNAL;                       \
+  }                                               \
+  return QS_OK;

@@ -1,0 +1,456 @@
+// FP64 block linear algebra: Hermitian eigendecomposition and SVD of every
+// symmetry block, global truncation (markSet) and the Davidson double
+// Gram-Schmidt re-orthogonalisation.
+//
+//  * qs_eig_blocks  -- the OpenMP loop of QSpace::EigenSymmetric
+//    (Source/QSpace.cc:4789-4811) calling wbEigenS -> dsyevd / zheevd
+//    (Source/wbarray_blas.cc:501-660).  Blocks up to 32 rows go through one
+//    batched Jacobi call per distinct size (syevjBatched); larger blocks use
+//    the divide-and-conquer solver (syevd) on the context stream.
+//  * qs_svd_blocks  -- SVD_Data::blockSVD (Source/mpsortho.cc:546-613) ->
+//    wbSVD -> dgesdd (Source/wbarray_blas.cc:995-1090); Jacobi SVD (gesvdj).
+//  * qs_mark_keep   -- markSet (Source/gathered.cc:1822-1990) on the host.
+//  * qs_gs_reortho  -- RunDavidson's double classical Gram-Schmidt
+//    (Source/david2SiteQS.cc:440-470): two passes of v -= V (V^T v), then
+//    v /= |v|; FP64 dot/axpy kernels (memory bound).
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "qs_internal.h"
+
+namespace qs {
+
+#define QS_SOLVER(call)                                                                   \
+  do {                                                                                    \
+    cusolverStatus_t s_ = (call);                                                         \
+    if (s_ != CUSOLVER_STATUS_SUCCESS)                                                    \
+      ::qs::fail(QS_ERR_CUDA, "%s:%d %s -> cusolver status %d", __FILE__, __LINE__, #call, \
+                 (int)s_);                                                                \
+  } while (0)
+
+cusolverDnHandle_t solver_of(Ctx *ctx) {
+  if (!ctx->solver) {
+    cusolverDnHandle_t h;
+    QS_SOLVER(cusolverDnCreate(&h));
+    ctx->solver = h;
+  }
+  cusolverDnHandle_t h = static_cast<cusolverDnHandle_t>(ctx->solver);
+  QS_SOLVER(cusolverDnSetStream(h, ctx->stream));
+  return h;
+}
+
+void destroy_solver(Ctx *ctx) {
+  if (ctx->solver) cusolverDnDestroy(static_cast<cusolverDnHandle_t>(ctx->solver));
+  ctx->solver = nullptr;
+}
+
+namespace {
+
+// dst[i] (+)= ..., block-strided gather/scatter helpers
+__global__ void copy_blocks_kernel(const double *__restrict__ src, double *__restrict__ dst,
+                                   const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
+                                   const int64_t *__restrict__ size, int es) {
+  const int64_t b = blockIdx.y;
+  const int64_t n = size[b] * es;
+  const double *s = src + soff[b] * es;
+  double *d = dst + doff[b] * es;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+
+// V^T for an n x k column-major V (complex: conjugate transpose).
+__global__ void transpose_kernel(const double *__restrict__ in, double *__restrict__ out, int64_t n,
+                                 int64_t k, int cplx) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * k; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i % n, c = i / n;  // in(r, c)
+    if (cplx) {
+      const double2 v = reinterpret_cast<const double2 *>(in)[i];
+      reinterpret_cast<double2 *>(out)[c + r * k] = make_double2(v.x, -v.y);
+    } else {
+      out[c + r * k] = in[i];
+    }
+  }
+}
+
+// c[j] = V(:,j)^T v, one CTA per (chunk, j) accumulated with atomics into
+// FP64 partial sums per chunk (deterministic: chunks are reduced in order
+// by the second kernel).
+constexpr int GS_CHUNK = 8192;
+__global__ void gs_dot_kernel(const double *__restrict__ V, const double *__restrict__ v, int64_t n,
+                              double *__restrict__ part) {
+  const int64_t c = blockIdx.x, j = blockIdx.y;
+  const int64_t i0 = c * GS_CHUNK, i1 = min(n, i0 + GS_CHUNK);
+  double s = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(V[j * n + i], v[i], s);
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[j * gridDim.x + c] = red[0];
+}
+
+__global__ void gs_reduce_kernel(const double *__restrict__ part, int64_t nchunk, int64_t nv,
+                                 double *__restrict__ coef) {
+  const int64_t j = blockIdx.x;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int64_t c = 0; c < nchunk; ++c) s += part[j * nchunk + c];
+    coef[j] = s;
+  }
+}
+
+__global__ void gs_axpy_kernel(const double *__restrict__ V, double *__restrict__ v, int64_t n, int64_t nv,
+                               const double *__restrict__ coef) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double x = v[i];
+    for (int64_t j = 0; j < nv; ++j) x = fma(-coef[j], V[j * n + i], x);
+    v[i] = x;
+  }
+}
+
+__global__ void scale_kernel(double *__restrict__ v, int64_t n, const double *__restrict__ nrm) {
+  const double s = nrm[0] > 0 ? 1.0 / sqrt(nrm[0]) : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] *= s;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- markSet
+// Sorted global selection of the kept eigenvalues, restating markSet for the
+// ascending direction (Source/gathered.cc:1822-2040) with eigQS's option
+// handling (Source/eigQS.cc:55-100): deps > 0 averages near-degenerate
+// levels (relative to the spectral width) and moves the cut to the largest
+// weighted gap near Nkeep (b = -1, dmax = -1); otherwise the Nkeep lowest
+// levels are kept, or those below E_min + Etrunc when Etrunc > 0.
+void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nkeep_in, double etrunc,
+                    double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
+  int64_t N = 0;
+  for (int64_t i = 0; i < nblk; ++i) N += n[i];
+  std::fill(keep, keep + N, 0);
+  if (nkeep_out) *nkeep_out = 0;
+  if (etrunc_out) *etrunc_out = etrunc;
+  if (N == 0) return;
+  std::vector<double> e(E, E + N);
+  std::vector<int64_t> P(N);
+  std::iota(P.begin(), P.end(), 0);
+  std::stable_sort(P.begin(), P.end(), [&](int64_t a, int64_t b) { return e[a] < e[b]; });
+  std::vector<double> s(N);
+  for (int64_t i = 0; i < N; ++i) s[i] = e[P[i]];
+  const double b = deps > 0 ? -1.0 : 0.0;
+  if (deps > 0) {
+    const double eps = deps * std::fabs(s[N - 1] - s[0]);
+    int64_t i0 = 0;
+    for (int64_t i = 1; i <= N; ++i) {
+      if (i == N || std::fabs(s[i] - s[i - 1]) > eps) {
+        const int64_t d = i - i0;
+        if (d > 1) {
+          double avg = 0;
+          for (int64_t j = i0; j < i; ++j) avg += s[j];
+          avg /= (double)d;
+          for (int64_t j = i0; j < i; ++j) s[j] = avg;
+        }
+        i0 = i;
+      }
+    }
+  }
+  int64_t Nkeep = (nkeep_in < 0 || nkeep_in > N) ? N : nkeep_in;
+  if (Nkeep == 0) return;
+  if (Nkeep >= N && etrunc <= 0) {
+    std::fill(keep, keep + N, 1);
+    if (nkeep_out) *nkeep_out = N;
+    return;
+  }
+  int64_t l;
+  const int64_t Nkmin = 0;
+  if (etrunc > 0) {
+    const double x = etrunc + s[0];
+    for (l = 1; l < N; ++l)
+      if (s[l] >= x && l > Nkmin) break;
+    if (l > Nkeep) l = Nkeep;
+  } else {
+    l = Nkeep;
+  }
+  if (l < N && l > 0 && b < 0) {
+    const int64_t nx = std::max<int64_t>(16, l / 5);
+    const double q = 10.0 / (-b * (double)nx);
+    const int64_t NX = (int64_t)(5.0 / q);
+    int64_t i = std::max<int64_t>(1, l - NX);
+    const int64_t i2 = std::min<int64_t>(N, l + NX);
+    int64_t imax = l;
+    double xmax = 0;
+    for (; i < i2; ++i) {
+      const double t = q * (double)(i - l);
+      const double x = std::exp(-t * t) * std::fabs(s[i] - s[i - 1]);
+      if (x > xmax) { xmax = x; imax = i; }
+    }
+    if (i == N) {
+      const double t = q * (double)(i - l);
+      const double x = 0.1 * std::exp(-t * t) * std::fabs(s[N - 1] - s[0]);
+      if (x > xmax) { xmax = x; imax = i; }
+    }
+    l = imax;
+  }
+  if (l >= N) l = N;
+  for (int64_t i = 0; i < l; ++i) keep[P[i]] = 1;
+  if (nkeep_out) *nkeep_out = l;
+  if (etrunc_out) *etrunc_out = (l < N) ? s[l] - s[0] : 0.0;
+}
+
+// -------------------------------------------------------------- eig blocks
+void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, const int64_t *eoffs,
+                const double *H, double *E, double *U, bool cplx) {
+  if (nblk <= 0) return;
+  cusolverDnHandle_t h = solver_of(ctx);
+  const int es = cplx ? 2 : 1;
+  for (int64_t i = 0; i < nblk; ++i)
+    if (n[i] < 0 || n[i] > INT32_MAX) fail(QS_ERR_SHAPE, "eig: block %lld has size %lld", (long long)i, (long long)n[i]);
+  // U <- H (the solvers overwrite their input with the eigenvectors)
+  {
+    std::vector<int64_t> sz(nblk);
+    int64_t mx = 1;
+    for (int64_t i = 0; i < nblk; ++i) { sz[i] = n[i] * n[i]; mx = std::max(mx, sz[i]); }
+    std::vector<int64_t> so(offs, offs + nblk);
+    int64_t *d_so = dev_upload(ctx, so), *d_sz = dev_upload(ctx, sz);
+    dim3 g((unsigned)std::min<int64_t>((mx * es + 255) / 256, 1024), (unsigned)nblk);
+    if (nblk > 65535) fail(QS_ERR_SHAPE, "eig: too many blocks in one call");
+    copy_blocks_kernel<<<g, 256, 0, ctx->stream>>>(H, U, d_so, d_so, d_sz, es);
+    QS_LAUNCHED(ctx);
+    dev_free(ctx, d_so);
+    dev_free(ctx, d_sz);
+  }
+  // group small blocks by size for batched Jacobi; others one by one
+  std::map<int64_t, std::vector<int64_t>> small;
+  std::vector<int64_t> large;
+  for (int64_t i = 0; i < nblk; ++i) {
+    if (n[i] == 0) continue;
+    if (n[i] <= 32) small[n[i]].push_back(i);
+    else large.push_back(i);
+  }
+  int *d_info = dev_alloc<int>(ctx, (size_t)std::max<int64_t>(nblk, 1));
+  QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * std::max<int64_t>(nblk, 1), ctx->stream));
+  // large blocks: syevd
+  int64_t nmax = 0;
+  for (int64_t i : large) nmax = std::max(nmax, n[i]);
+  if (nmax > 0) {
+    int lwork = 0;
+    const int nm = (int)nmax;
+    if (cplx)
+      QS_SOLVER(cusolverDnZheevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm,
+                                            reinterpret_cast<cuDoubleComplex *>(U), nm, E, &lwork));
+    else
+      QS_SOLVER(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm, U, nm, E, &lwork));
+    // the workspace for the largest size bounds the smaller ones
+    double *work = dev_alloc<double>(ctx, (size_t)std::max(lwork, 1) * es);
+    for (int64_t i : large) {
+      const int ni = (int)n[i];
+      if (cplx)
+        QS_SOLVER(cusolverDnZheevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
+                                   reinterpret_cast<cuDoubleComplex *>(U) + offs[i], ni, E + eoffs[i],
+                                   reinterpret_cast<cuDoubleComplex *>(work), lwork, d_info + i));
+      else
+        QS_SOLVER(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni, U + offs[i] * es, ni,
+                                   E + eoffs[i], work, lwork, d_info + i));
+      ctx->launches++;
+    }
+    dev_free(ctx, work);
+  }
+  // small blocks: batched Jacobi on contiguous copies
+  if (!small.empty()) {
+    syevjInfo_t params;
+    QS_SOLVER(cusolverDnCreateSyevjInfo(&params));
+    QS_SOLVER(cusolverDnXsyevjSetTolerance(params, 1e-15));
+    QS_SOLVER(cusolverDnXsyevjSetMaxSweeps(params, 100));
+    for (auto &kv : small) {
+      const int ni = (int)kv.first;
+      const int nb = (int)kv.second.size();
+      const int64_t bs = (int64_t)ni * ni;
+      double *Ab = dev_alloc<double>(ctx, (size_t)bs * nb * es);
+      double *Wb = dev_alloc<double>(ctx, (size_t)ni * nb);
+      int *ib = dev_alloc<int>(ctx, nb);
+      std::vector<int64_t> so, dof, sz, eo, ed, es1;
+      for (int j = 0; j < nb; ++j) {
+        so.push_back(offs[kv.second[j]]);
+        dof.push_back(bs * j);
+        sz.push_back(bs);
+        eo.push_back((int64_t)ni * j);
+        ed.push_back(eoffs[kv.second[j]]);
+        es1.push_back(ni);
+      }
+      int64_t *d_so = dev_upload(ctx, so), *d_do = dev_upload(ctx, dof), *d_sz = dev_upload(ctx, sz);
+      dim3 g((unsigned)std::min<int64_t>((bs * es + 255) / 256, 64), (unsigned)nb);
+      copy_blocks_kernel<<<g, 256, 0, ctx->stream>>>(U, Ab, d_so, d_do, d_sz, es);
+      QS_LAUNCHED(ctx);
+      int lwork = 0;
+      if (cplx)
+        QS_SOLVER(cusolverDnZheevjBatched_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
+                                                     reinterpret_cast<cuDoubleComplex *>(Ab), ni, Wb, &lwork,
+                                                     params, nb));
+      else
+        QS_SOLVER(cusolverDnDsyevjBatched_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni, Ab,
+                                                     ni, Wb, &lwork, params, nb));
+      double *work = dev_alloc<double>(ctx, (size_t)std::max(lwork, 1) * es);
+      if (cplx)
+        QS_SOLVER(cusolverDnZheevjBatched(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
+                                          reinterpret_cast<cuDoubleComplex *>(Ab), ni, Wb,
+                                          reinterpret_cast<cuDoubleComplex *>(work), lwork, ib, params, nb));
+      else
+        QS_SOLVER(cusolverDnDsyevjBatched(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni, Ab, ni, Wb, work,
+                                          lwork, ib, params, nb));
+      ctx->launches++;
+      // scatter vectors and values back
+      copy_blocks_kernel<<<g, 256, 0, ctx->stream>>>(Ab, U, d_do, d_so, d_sz, es);
+      QS_LAUNCHED(ctx);
+      int64_t *d_eo = dev_upload(ctx, eo), *d_ed = dev_upload(ctx, ed), *d_es = dev_upload(ctx, es1);
+      dim3 g2(1, (unsigned)nb);
+      copy_blocks_kernel<<<g2, 64, 0, ctx->stream>>>(Wb, E, d_eo, d_ed, d_es, 1);
+      QS_LAUNCHED(ctx);
+      std::vector<int> hinfo(nb);
+      QS_CUDA(cudaMemcpyAsync(hinfo.data(), ib, nb * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      QS_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int j = 0; j < nb; ++j)
+        if (hinfo[j] < 0) fail(QS_ERR_NUMERIC, "syevjBatched: argument error %d", hinfo[j]);
+      for (void *p : {(void *)Ab, (void *)Wb, (void *)ib, (void *)work, (void *)d_so, (void *)d_do, (void *)d_sz,
+                      (void *)d_eo, (void *)d_ed, (void *)d_es})
+        dev_free(ctx, p);
+    }
+    cusolverDnDestroySyevjInfo(params);
+  }
+  std::vector<int> info(std::max<int64_t>(nblk, 1));
+  QS_CUDA(cudaMemcpyAsync(info.data(), d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, d_info);
+  for (int64_t i = 0; i < nblk; ++i)
+    if (info[i] != 0) fail(QS_ERR_NUMERIC, "eig: block %lld did not converge (info %d)", (long long)i, info[i]);
+}
+
+// -------------------------------------------------------------- svd blocks
+void svd_blocks(Ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
+                const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, const double *A, double *U,
+                double *S, double *Vt) {
+  if (nblk <= 0) return;
+  cusolverDnHandle_t h = solver_of(ctx);
+  gesvdjInfo_t params;
+  QS_SOLVER(cusolverDnCreateGesvdjInfo(&params));
+  QS_SOLVER(cusolverDnXgesvdjSetTolerance(params, 1e-15));
+  QS_SOLVER(cusolverDnXgesvdjSetMaxSweeps(params, 100));
+  int *d_info = dev_alloc<int>(ctx, (size_t)nblk);
+  QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * nblk, ctx->stream));
+  for (int64_t i = 0; i < nblk; ++i) {
+    const int64_t mi = m[i], ni = n[i];
+    if (mi < 0 || ni < 0 || mi > INT32_MAX || ni > INT32_MAX) fail(QS_ERR_SHAPE, "svd: bad block size");
+    if (mi == 0 || ni == 0) continue;
+    const int64_t k = std::min(mi, ni);
+    double *a = dev_alloc<double>(ctx, (size_t)(mi * ni));
+    double *v = dev_alloc<double>(ctx, (size_t)(ni * k));
+    QS_CUDA(cudaMemcpyAsync(a, A + offs[i], (size_t)(mi * ni) * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    int lwork = 0;
+    QS_SOLVER(cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)mi, (int)ni, a, (int)mi, S + soffs[i],
+                                           U + uoffs[i], (int)mi, v, (int)ni, &lwork, params));
+    double *work = dev_alloc<double>(ctx, (size_t)std::max(lwork, 1));
+    QS_SOLVER(cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)mi, (int)ni, a, (int)mi, S + soffs[i],
+                                U + uoffs[i], (int)mi, v, (int)ni, work, lwork, d_info + i, params));
+    ctx->launches++;
+    const int64_t tot = ni * k;
+    transpose_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 1024), 256, 0, ctx->stream>>>(
+        v, Vt + voffs[i], ni, k, 0);
+    QS_LAUNCHED(ctx);
+    dev_free(ctx, a);
+    dev_free(ctx, v);
+    dev_free(ctx, work);
+  }
+  std::vector<int> info(nblk);
+  QS_CUDA(cudaMemcpyAsync(info.data(), d_info, nblk * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, d_info);
+  cusolverDnDestroyGesvdjInfo(params);
+  for (int64_t i = 0; i < nblk; ++i)
+    if (info[i] < 0) fail(QS_ERR_NUMERIC, "svd: block %lld argument error %d", (long long)i, info[i]);
+}
+
+// ------------------------------------------------------------ Gram-Schmidt
+void gs_reortho(Ctx *ctx, int64_t n, int64_t nv, const double *V, double *v, double *norm_out) {
+  if (n <= 0) fail(QS_ERR_ARG, "gs_reortho: empty vector");
+  if (nv < 0 || nv > 65535) fail(QS_ERR_ARG, "gs_reortho: bad basis size");
+  const int64_t nch = (n + GS_CHUNK - 1) / GS_CHUNK;
+  if (nch > 0x7fffffff) fail(QS_ERR_SHAPE, "gs_reortho: vector too long");
+  double *part = dev_alloc<double>(ctx, (size_t)(nch * std::max<int64_t>(nv, 1)));
+  double *coef = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(nv, 1));
+  const unsigned gax = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 16);
+  for (int pass = 0; pass < 2 && nv > 0; ++pass) {
+    gs_dot_kernel<<<dim3((unsigned)nch, (unsigned)nv), 256, 0, ctx->stream>>>(V, v, n, part);
+    QS_LAUNCHED(ctx);
+    gs_reduce_kernel<<<(unsigned)nv, 32, 0, ctx->stream>>>(part, nch, nv, coef);
+    QS_LAUNCHED(ctx);
+    gs_axpy_kernel<<<gax, 256, 0, ctx->stream>>>(V, v, n, nv, coef);
+    QS_LAUNCHED(ctx);
+  }
+  // |v|^2 with the same chunked reduction (v against itself)
+  gs_dot_kernel<<<dim3((unsigned)nch, 1), 256, 0, ctx->stream>>>(v, v, n, part);
+  QS_LAUNCHED(ctx);
+  gs_reduce_kernel<<<1, 32, 0, ctx->stream>>>(part, nch, 1, coef);
+  QS_LAUNCHED(ctx);
+  scale_kernel<<<gax, 256, 0, ctx->stream>>>(v, n, coef);
+  QS_LAUNCHED(ctx);
+  double nrm2 = 0;
+  QS_CUDA(cudaMemcpyAsync(&nrm2, coef, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (norm_out) *norm_out = std::sqrt(nrm2);
+  dev_free(ctx, part);
+  dev_free(ctx, coef);
+}
+
+}  // namespace qs
+
+using namespace qs;
+
+extern "C" {
+
+qs_status qs_eig_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, const int64_t *eoffs,
+                        const double *H, double *E, double *U, int32_t is_complex) {
+  QS_API_BEGIN
+  if (!ctx || (nblk > 0 && (!n || !offs || !eoffs || !H || !E || !U))) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  eig_blocks(&ctx->c, nblk, n, offs, eoffs, H, E, U, is_complex != 0);
+  QS_API_END
+}
+
+qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E, const double *qdim_w, int64_t nkeep,
+                       double etrunc, double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
+  QS_API_BEGIN
+  if (nblk < 0 || (nblk > 0 && (!n || !E || !keep))) fail(QS_ERR_ARG, "null argument");
+  if (qdim_w) fail(QS_ERR_UNSUPPORTED, "multiplet weights: markSet counts every multiplet once; pass NULL");
+  mark_keep_host(nblk, n, E, nkeep, etrunc, deps, keep, nkeep_out, etrunc_out);
+  QS_API_END
+}
+
+qs_status qs_svd_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
+                        const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, const double *A, double *U,
+                        double *S, double *Vt) {
+  QS_API_BEGIN
+  if (!ctx || (nblk > 0 && (!m || !n || !offs || !uoffs || !soffs || !voffs || !A || !U || !S || !Vt)))
+    fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  svd_blocks(&ctx->c, nblk, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt);
+  QS_API_END
+}
+
+qs_status qs_gs_reortho(qs_ctx *ctx, int64_t n, int64_t nv, const double *V, double *v, double *norm_out) {
+  QS_API_BEGIN
+  if (!ctx || !v || (nv > 0 && !V)) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  gs_reortho(&ctx->c, n, nv, V, v, norm_out);
+  QS_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// C-ABI object definitions shared by the contraction driver (qs_capi.cpp)
+// and the serving loop (qs_serve.cpp).
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "qs_internal.h"
+#include "qs_plan.h"
+
+struct qs_tensor {
+  qs::QMeta meta;
+  double *d = nullptr;   // owned arena (stream-ordered allocation)
+  qs::Ctx *ctx = nullptr;  // context whose stream frees the arena
+  ~qs_tensor() {
+    if (d && ctx) cudaFreeAsync(d, ctx->stream);
+  }
+};
+
+struct qs_result {
+  qs::QMeta meta;              // contiguous offsets
+  std::vector<double> data;    // nelem (x2 when complex)
+};
+
+namespace qs {
+// The device contraction driver: plan on the host, kernels on ctx->stream.
+// Synchronises ctx->stream once (the data-dependent zero-block test).
+std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double *dA, const QMeta &Bm,
+                                         const double *dB, const char *ia, const char *ib,
+                                         const int32_t *perm, int32_t nperm, const qs_opts *opts,
+                                         qs_stats *stats);
+// Device bytes a contraction will hold while it runs (output, operand
+// copies, digit arena): the admission footprint of the serving loop.
+int64_t contract_footprint(const QMeta &Am, const QMeta &Bm, const char *ia, const char *ib,
+                           const qs_opts *opts);
+}  // namespace qs

@@ -1,0 +1,252 @@
+// Serving loop: continuous batching of contractions between device-resident
+// tensors for many concurrent NRG / DMRG instances.  (The reference has no
+// counterpart: its MEX calls run one at a time from MATLAB.)
+//
+//  * qs_server_submit enqueues a request (FIFO) and records an event on the
+//    submitting context's stream, so the request sees every earlier write to
+//    its operands.
+//  * nslots worker threads each own a stream, a scratch arena and an error
+//    word (a qs::Ctx).  A worker takes the head of the queue as soon as the
+//    request's device footprint fits into the HBM budget next to the
+//    requests already running, so requests that arrive while others are on
+//    the GPU are admitted as slots and memory free up, and their kernels
+//    overlap on the device.  A request larger than the whole budget is
+//    refused at submit time (QS_ERR_OOM).
+//  * Results are identical alone and in the mix: every kernel is
+//    deterministic (fixed reduction order) and requests share no buffers.
+//  * qs_server_poll waits a bounded time; qs_server_cancel removes a
+//    request that has not started.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+
+#include "qs_objects.h"
+
+using namespace qs;
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+struct Request {
+  int64_t ticket = 0;
+  const qs_tensor *A = nullptr, *B = nullptr;
+  std::string ia, ib;
+  std::vector<int32_t> perm;
+  qs_opts opts{};
+  bool has_opts = false;
+  cudaEvent_t ready = nullptr;
+  int64_t footprint = 0;
+  clk::time_point t_submit;
+  enum State { QUEUED, RUNNING, DONE, FAILED, CANCELLED } state = QUEUED;
+  qs_status status = QS_OK;
+  std::string err;
+  qs_tensor *C = nullptr;
+  double latency_ms = 0;
+};
+
+}  // namespace
+
+struct qs_server {
+  qs_ctx *parent = nullptr;
+  std::vector<std::unique_ptr<Ctx>> slots;
+  std::vector<std::thread> workers;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::shared_ptr<Request>> queue;
+  std::unordered_map<int64_t, std::shared_ptr<Request>> reqs;
+  int64_t next_ticket = 1;
+  int64_t budget = 0, in_use = 0;
+  bool stop = false;
+
+  void worker(Ctx *slot) {
+    cudaSetDevice(slot->device);
+    for (;;) {
+      std::shared_ptr<Request> r;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_work.wait(lk, [&] {
+          return stop || (!queue.empty() && in_use + queue.front()->footprint <= budget);
+        });
+        if (stop) return;
+        r = queue.front();
+        queue.pop_front();
+        in_use += r->footprint;
+        r->state = Request::RUNNING;
+      }
+      qs_status st = QS_OK;
+      std::string msg;
+      qs_tensor *C = nullptr;
+      try {
+        if (r->ready) QS_CUDA(cudaStreamWaitEvent(slot->stream, r->ready, 0));
+        auto T = contract_core(slot, r->A->meta, r->A->d, r->B->meta, r->B->d, r->ia.c_str(), r->ib.c_str(),
+                               r->perm.empty() ? nullptr : r->perm.data(), (int32_t)r->perm.size(),
+                               r->has_opts ? &r->opts : nullptr, nullptr);
+        QS_CUDA(cudaStreamSynchronize(slot->stream));
+        // the caller frees the result on the parent context's stream
+        T->ctx = &parent->c;
+        C = T.release();
+      } catch (const Error &e) {
+        st = e.code;
+        msg = e.what();
+      } catch (const std::exception &e) {
+        st = QS_ERR_INTERNAL;
+        msg = e.what();
+      }
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        in_use -= r->footprint;
+        r->latency_ms = std::chrono::duration<double, std::milli>(clk::now() - r->t_submit).count();
+        r->status = st;
+        r->err = msg;
+        r->C = C;
+        r->state = st == QS_OK ? Request::DONE : Request::FAILED;
+        if (r->ready) {
+          cudaEventDestroy(r->ready);
+          r->ready = nullptr;
+        }
+      }
+      cv_done.notify_all();
+      cv_work.notify_all();
+    }
+  }
+};
+
+extern "C" {
+
+qs_status qs_server_create(qs_ctx *ctx, const qs_server_cfg *cfg, qs_server **out) {
+  QS_API_BEGIN
+  if (!ctx || !cfg || !out) fail(QS_ERR_ARG, "null argument");
+  if (cfg->nslots < 1 || cfg->nslots > 256) fail(QS_ERR_ARG, "nslots must be in 1..256");
+  if (cfg->hbm_budget <= 0) fail(QS_ERR_ARG, "hbm_budget must be positive");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  auto s = std::make_unique<qs_server>();
+  s->parent = ctx;
+  s->budget = cfg->hbm_budget;
+  for (int i = 0; i < cfg->nslots; ++i) {
+    auto c = std::make_unique<Ctx>();
+    c->device = ctx->c.device;
+    c->num_sms = ctx->c.num_sms;
+    QS_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    QS_CUDA(cudaMalloc(&c->d_err, 64));
+    QS_CUDA(cudaMemset(c->d_err, 0, 64));
+    s->slots.push_back(std::move(c));
+  }
+  for (auto &c : s->slots) s->workers.emplace_back(&qs_server::worker, s.get(), c.get());
+  *out = s.release();
+  QS_API_END
+}
+
+void qs_server_destroy(qs_server *s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (auto &t : s->workers) t.join();
+  for (auto &kv : s->reqs) {
+    if (kv.second->ready) cudaEventDestroy(kv.second->ready);
+    delete kv.second->C;  // results nobody collected
+  }
+  for (auto &c : s->slots) {
+    if (c->scratch) cudaFreeAsync(c->scratch, c->stream);
+    cudaStreamSynchronize(c->stream);
+    destroy_solver(c.get());
+    cudaFree(c->d_err);
+    cudaStreamDestroy(c->stream);
+  }
+  delete s;
+}
+
+qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const char *ia, const qs_tensor *B, const char *ib,
+                           const int32_t *perm, int32_t nperm, const qs_opts *opts, int64_t *ticket) {
+  QS_API_BEGIN
+  if (!s || !A || !B || !ia || !ib || !ticket) fail(QS_ERR_ARG, "null argument");
+  // validate the request on the host now: a malformed request fails here,
+  // not in a worker
+  (void)parse_ctr_idx(ia);
+  (void)parse_ctr_idx(ib);
+  const int64_t fp = contract_footprint(A->meta, B->meta, ia, ib, opts);
+  if (fp > s->budget)
+    fail(QS_ERR_OOM, "admission refused: request needs %lld bytes, budget is %lld", (long long)fp,
+         (long long)s->budget);
+  auto r = std::make_shared<Request>();
+  r->A = A;
+  r->B = B;
+  r->ia = ia;
+  r->ib = ib;
+  if (perm && nperm > 0) r->perm.assign(perm, perm + nperm);
+  if (opts) {
+    r->opts = *opts;
+    r->has_opts = true;
+  }
+  r->footprint = fp;
+  QS_CUDA(cudaSetDevice(s->parent->c.device));
+  QS_CUDA(cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming));
+  QS_CUDA(cudaEventRecord(r->ready, s->parent->c.stream));
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->ticket = s->next_ticket++;
+    r->t_submit = clk::now();
+    s->reqs[r->ticket] = r;
+    s->queue.push_back(r);
+    *ticket = r->ticket;
+  }
+  s->cv_work.notify_one();
+  QS_API_END
+}
+
+qs_status qs_server_poll(qs_server *s, int64_t ticket, int32_t timeout_ms, int32_t *done, qs_tensor **C,
+                         double *latency_ms) {
+  QS_API_BEGIN
+  if (!s || !done) fail(QS_ERR_ARG, "null argument");
+  *done = 0;
+  if (C) *C = nullptr;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) fail(QS_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  std::shared_ptr<Request> r = it->second;
+  auto finished = [&] { return r->state == Request::DONE || r->state == Request::FAILED || r->state == Request::CANCELLED; };
+  if (!finished() && timeout_ms > 0) s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished);
+  if (!finished()) return QS_OK;
+  *done = 1;
+  if (latency_ms) *latency_ms = r->latency_ms;
+  s->reqs.erase(it);
+  if (r->state == Request::CANCELLED) fail(QS_ERR_CANCELLED, "request %lld was cancelled", (long long)ticket);
+  if (r->state == Request::FAILED) fail(r->status, "%s", r->err.c_str());
+  if (C) *C = r->C;
+  else delete r->C;
+  r->C = nullptr;
+  QS_API_END
+}
+
+qs_status qs_server_cancel(qs_server *s, int64_t ticket) {
+  QS_API_BEGIN
+  if (!s) fail(QS_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) fail(QS_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  std::shared_ptr<Request> r = it->second;
+  if (r->state != Request::QUEUED) fail(QS_ERR_ARG, "request %lld already started", (long long)ticket);
+  for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+    if ((*q)->ticket == ticket) {
+      s->queue.erase(q);
+      break;
+    }
+  r->state = Request::CANCELLED;
+  if (r->ready) {
+    cudaEventDestroy(r->ready);
+    r->ready = nullptr;
+  }
+  s->cv_done.notify_all();
+  QS_API_END
+}
+
+}  // extern "C"

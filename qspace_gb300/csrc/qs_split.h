@@ -1,0 +1,36 @@
+// Split-precision grouped block GEMM (FP64 emulated with BF16 digits on the
+// 5th-generation tensor cores).  See qs_gemm_split.cu for the method.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "qs_internal.h"
+
+namespace qs {
+
+struct SplitResult {
+  int nslices = 0;
+  int bits = 0;
+  double err_bound = 0;
+  int64_t slice_bytes = 0;
+  int64_t ntiles = 0;
+};
+
+// Digit plan for a maximal accumulated depth `kreal` (real terms summed into
+// one output element) and a target relative error.
+struct DigitPlan {
+  int bits;    // bits per digit (the leading digit carries bits+1)
+  int nslices; // digits per operand
+  double err_bound;
+};
+DigitPlan choose_digits(int64_t kreal, double tol, int forced_slices);
+
+SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs,
+                      const std::vector<int64_t> &grp, const std::vector<int32_t> &blk_M,
+                      const std::vector<int32_t> &blk_N, const std::vector<int64_t> &c_off,
+                      const double *A, const double *B, double *C, bool cplx,
+                      int forced_slices, double tol,
+                      const std::vector<int32_t> *blk_ldc = nullptr);
+
+}  // namespace qs

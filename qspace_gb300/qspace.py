@@ -1,0 +1,402 @@
+"""Host-side mirror of QSpace's MEX interface on top of libqsgpu.
+
+``QSpace`` mirrors the MATLAB struct ``{Q, data, info}`` (Source/QSpace.hh:
+3092): ``Q`` is a list with one (nblk x qdim) int array per leg, ``data`` a
+list of dense blocks, ``info`` a dict (``itags``).  The functions keep the
+reference's names, argument meaning and error behaviour:
+
+* ``contractQS(A, ia, B, ib[, perm])`` -- Source/contractQS.cc:505-632;
+* ``permuteQS(A, perm[, 'conj'])``     -- Source/permuteQS.cc:198-258.
+
+All numerical work runs on the GPU through the C-ABI; only label bookkeeping
+of itags happens here.  ``Tensor`` is a device-resident QSpace.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+from ._capi import QSpaceView, Opts, Stats, check
+
+__all__ = ["QSpace", "Tensor", "Context", "contractQS", "permuteQS", "default_context",
+           "upload", "contract_dev", "permute_dev"]
+
+
+# --------------------------------------------------------------------- QSpace
+@dataclass
+class QSpace:
+    Q: list                      # per leg: (nblk, qdim) int32
+    data: list                   # per block: ndarray with the leg dims
+    info: dict = field(default_factory=dict)
+
+    @property
+    def rank(self) -> int:
+        return len(self.Q)
+
+    @property
+    def nblk(self) -> int:
+        return len(self.data)
+
+    @property
+    def qdim(self) -> int:
+        if not self.Q or self.nblk == 0:
+            return 1
+        return int(np.asarray(self.Q[0]).reshape(self.nblk, -1).shape[1])
+
+    @property
+    def is_complex(self) -> bool:
+        return any(np.iscomplexobj(d) for d in self.data)
+
+    def block_dims(self, i: int) -> tuple:
+        r = self.rank
+        s = tuple(int(x) for x in np.shape(self.data[i]))
+        if len(s) > r:
+            if any(x != 1 for x in s[r:]):
+                raise ValueError("block has more non-singleton dims than legs")
+            s = s[:r]
+        return s + (1,) * (r - len(s))
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "QSpace":
+        return cls([np.asarray(q, dtype=np.int32).reshape(len(q), -1) if np.ndim(q) else q
+                    for q in d["Q"]], list(d["data"]), dict(d.get("info") or {}))
+
+    def to_dict(self) -> dict:
+        return {"Q": [np.asarray(q) for q in self.Q], "data": list(self.data), "info": dict(self.info)}
+
+    # -- packing into the C-ABI layout
+    def pack(self):
+        """(view, keepalive): labels block-major int32, dims int64, blocks
+        column-major back to back (complex interleaved)."""
+        n, r = self.nblk, self.rank
+        qd = self.qdim
+        cplx = self.is_complex
+        if n:
+            q = np.stack([np.asarray(x, dtype=np.int32).reshape(n, qd) for x in self.Q], axis=1)
+            q = np.ascontiguousarray(q.reshape(n, r * qd), dtype=np.int32)
+        else:
+            q = np.zeros((0,), np.int32)
+        dims = np.array([self.block_dims(i) for i in range(n)], dtype=np.int64).reshape(n, r)
+        sizes = np.prod(dims, axis=1) if r else np.ones(n, np.int64)
+        offs = np.zeros(n, np.int64)
+        if n > 1:
+            offs[1:] = np.cumsum(sizes)[:-1]
+        total = int(sizes.sum()) if n else 0
+        buf = np.empty(total, dtype=np.complex128 if cplx else np.float64)
+        for i, d in enumerate(self.data):
+            a = np.asarray(d, dtype=buf.dtype)
+            buf[offs[i]:offs[i] + sizes[i]] = a.reshape(-1, order="F") if a.ndim > 1 else a.reshape(-1)
+        dims = np.ascontiguousarray(dims)
+        v = QSpaceView()
+        v.rank, v.qdim, v.nblk = r, qd, n
+        v.q = q.ctypes.data_as(_capi.c_int32_p)
+        v.dims = dims.ctypes.data_as(_capi.c_int64_p)
+        v.offs = offs.ctypes.data_as(_capi.c_int64_p)
+        v.data = buf.ctypes.data_as(_capi.c_double_p)
+        v.is_complex = 1 if cplx else 0
+        return v, (q, dims, offs, buf)
+
+    @classmethod
+    def unpack(cls, rank, qdim, q, dims, offs, data, cplx, info=None) -> "QSpace":
+        n = len(offs)
+        if n == 0:
+            return cls([], [], dict(info or {}))
+        q = np.asarray(q, np.int32).reshape(n, rank, qdim)
+        dims = np.asarray(dims, np.int64).reshape(n, rank)
+        arr = np.asarray(data)
+        if cplx:
+            arr = arr.view(np.complex128)
+        blocks = []
+        for i in range(n):
+            s = int(np.prod(dims[i])) if rank else 1
+            blk = arr[offs[i]:offs[i] + s]
+            blocks.append(blk.reshape(tuple(dims[i]), order="F") if rank else blk.reshape(()))
+        Q = [np.ascontiguousarray(q[:, k, :]) for k in range(rank)]
+        return cls(Q, blocks, dict(info or {}))
+
+
+# -------------------------------------------------------------------- context
+class Context:
+    """One CUDA device + stream + memory pool (qs_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _capi.load()
+        h = C.c_void_p()
+        check(self.lib.qs_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    @property
+    def stream_ptr(self) -> int:
+        return int(self.lib.qs_ctx_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.qs_ctx_launches(self.h))
+
+    def sync(self):
+        check(self.lib.qs_ctx_sync(self.h))
+
+    def set_timing(self, on: bool = True):
+        check(self.lib.qs_ctx_set_timing(self.h, 1 if on else 0))
+
+    def phase_ms(self) -> tuple[float, float]:
+        """(operand preparation ms, GEMM kernel ms) of the most recent call."""
+        a, b = C.c_double(), C.c_double()
+        check(self.lib.qs_ctx_phase_ms(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qs_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_ctx_lock = threading.Lock()
+_contexts: dict[int, Context] = {}
+
+
+def default_context(device: int = 0) -> Context:
+    with _ctx_lock:
+        c = _contexts.get(device)
+        if c is None:
+            c = _contexts[device] = Context(device)
+        return c
+
+
+def make_opts(prec: str = "fp64", nslices: int = 0, tol: float = 1e-12, flags: int = 0) -> Opts:
+    o = Opts()
+    p = prec.lower()
+    if p in ("fp64", "plain", "double"):
+        o.prec = _capi.QS_PREC_FP64
+    elif p in ("split", "bf16", "ozaki"):
+        o.prec = _capi.QS_PREC_SPLIT
+    else:
+        raise ValueError(f"unknown precision mode '{prec}'")
+    o.nslices, o.tol, o.flags = int(nslices), float(tol), int(flags)
+    return o
+
+
+def _perm_arg(perm):
+    if perm is None:
+        return None, 0
+    if isinstance(perm, str):
+        s = perm.strip()
+        if not s:
+            return None, 0
+        if any(c in s for c in ",; "):
+            p = [int(x) for x in s.replace(",", " ").replace(";", " ").split()]
+        else:
+            p = [int(c) for c in s]
+    else:
+        p = [int(x) for x in np.atleast_1d(perm)]
+    if not p:
+        return None, 0
+    arr = (C.c_int32 * len(p))(*p)
+    return arr, len(p)
+
+
+def _idx_str(ix) -> bytes:
+    if isinstance(ix, str):
+        return ix.encode()
+    v = [int(x) for x in np.atleast_1d(ix)]
+    # numeric (1-based) indices: bracketed and blank separated so that a
+    # single multi-digit leg is not read in compact form
+    return ("[" + " ".join(str(x) for x in v) + " ]").encode()
+
+
+def _conj_flag(ix) -> bool:
+    if not isinstance(ix, str):
+        return False
+    s = ix.rstrip()
+    n = 0
+    while s.endswith("*"):
+        n += 1
+        s = s[:-1].rstrip()
+    return bool(n % 2)
+
+
+def _legs(ix) -> list[int]:
+    if isinstance(ix, str):
+        s = ix.rstrip().rstrip("*").strip().strip("[]")
+        if any(c in s for c in ",; "):
+            return [int(x) - 1 for x in s.replace(",", " ").replace(";", " ").split()]
+        out = []
+        for c in s:
+            out.append(int(c) - 1 if c.isdigit() else
+                       (ord(c) - 65 + 10 - 1 if c.isupper() else ord(c) - 97 + 36 - 1))
+        return out
+    return [int(x) - 1 for x in np.atleast_1d(ix)]
+
+
+def _out_itags(A: QSpace, ia, B: QSpace, ib, perm) -> list | None:
+    ta, tb = A.info.get("itags"), B.info.get("itags")
+    if not ta or not tb:
+        return None
+    la, lb = _legs(ia), _legs(ib)
+    ka = [k for k in range(A.rank) if k not in la]
+    kb = [k for k in range(B.rank) if k not in lb]
+
+    def cj(t, c):
+        if not c:
+            return t
+        return t[:-1] if t.endswith("*") else t + "*"
+
+    tags = [cj(ta[k], _conj_flag(ia)) for k in ka] + [cj(tb[k], _conj_flag(ib)) for k in kb]
+    p, n = _perm_arg(perm)
+    if p is not None:
+        pl = [p[i] - 1 for i in range(n)] + list(range(n, len(tags)))
+        tags = [tags[pl[i]] for i in range(len(tags))]
+    return tags
+
+
+def _check_itags(A: QSpace, ia, B: QSpace, ib):
+    """itag consistency of contracted legs (contract_getIdxSet,
+    Source/QSpace.cc:4230-4271): names must match up to the conjugation
+    mark."""
+    ta, tb = A.info.get("itags"), B.info.get("itags")
+    if not ta or not tb:
+        return
+    for a, b in zip(_legs(ia), _legs(ib)):
+        if a < len(ta) and b < len(tb) and ta[a].rstrip("*") != tb[b].rstrip("*"):
+            raise _capi.QSError(3, f"contract() itag mismatch {ta[a]} <> {tb[b]}")
+
+
+# ---------------------------------------------------------------- host calls
+def _result_to_qspace(lib, res, info=None) -> QSpace:
+    r, qd, nb, ne, cx = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64(), C.c_int32()
+    check(lib.qs_result_info(res, C.byref(r), C.byref(qd), C.byref(nb), C.byref(ne), C.byref(cx)))
+    n, rank, qdim = nb.value, r.value, qd.value
+    q = np.empty(max(n * rank * qdim, 1), np.int32)
+    dims = np.empty(max(n * rank, 1), np.int64)
+    offs = np.empty(max(n, 1), np.int64)
+    data = np.empty(max(ne.value * (2 if cx.value else 1), 1), np.float64)
+    check(lib.qs_result_copy(res, q.ctypes.data_as(_capi.c_int32_p), dims.ctypes.data_as(_capi.c_int64_p),
+                             offs.ctypes.data_as(_capi.c_int64_p), data.ctypes.data_as(_capi.c_double_p)))
+    lib.qs_result_free(res)
+    return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, bool(cx.value), info)
+
+
+def contractQS(A: QSpace, ia, B: QSpace, ib, perm=None, *, prec: str = "fp64", nslices: int = 0,
+               tol: float = 1e-12, ctx: Context | None = None, stats: dict | None = None) -> QSpace:
+    """C = contractQS(A, ia, B, ib [,perm]) on the GPU (host buffers in/out).
+
+    ``ia``/``ib``: '12*' style strings or 1-based sequences; ``perm`` 1-based.
+    ``prec``: 'fp64' (plain drop-in) or 'split' (BF16 digits on tcgen05).
+    """
+    ctx = ctx or default_context()
+    _check_itags(A, ia, B, ib)
+    va, ka = A.pack()
+    vb, kb = B.pack()
+    p, n = _perm_arg(perm)
+    o = make_opts(prec, nslices, tol)
+    st = Stats()
+    res = C.c_void_p()
+    check(ctx.lib.qs_contractQS(ctx.h, C.byref(va), _idx_str(ia), C.byref(vb), _idx_str(ib), p, n,
+                                C.byref(o), C.byref(res), C.byref(st)))
+    tags = _out_itags(A, ia, B, ib, perm)
+    out = _result_to_qspace(ctx.lib, res, {"itags": tags} if tags else None)
+    if stats is not None:
+        stats.update(st.as_dict())
+    del ka, kb
+    return out
+
+
+def permuteQS(A: QSpace, perm, conj=False, *, ctx: Context | None = None) -> QSpace:
+    """permuteQS(A, perm [,'conj']) on the GPU; block order unchanged."""
+    ctx = ctx or default_context()
+    if isinstance(conj, str):
+        conj = conj.lower() == "conj"
+    va, ka = A.pack()
+    p, n = _perm_arg(perm)
+    res = C.c_void_p()
+    check(ctx.lib.qs_permuteQS(ctx.h, C.byref(va), p, n, 1 if conj else 0, C.byref(res)))
+    info = dict(A.info)
+    if A.info.get("itags") and p is not None:
+        t = A.info["itags"]
+        pl = [p[i] - 1 for i in range(n)] + list(range(n, len(t)))
+        info["itags"] = [t[pl[i]] for i in range(len(t))]
+    return _result_to_qspace(ctx.lib, res, info)
+
+
+# ------------------------------------------------------------ device tensors
+class Tensor:
+    """A device-resident QSpace (qs_tensor)."""
+
+    def __init__(self, ctx: Context, handle: C.c_void_p, info: dict | None = None):
+        self.ctx, self.h, self.info = ctx, handle, dict(info or {})
+
+    def meta(self):
+        r, qd, nb, ne, cx = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64(), C.c_int32()
+        check(self.ctx.lib.qs_tensor_info(self.h, C.byref(r), C.byref(qd), C.byref(nb), C.byref(ne),
+                                          C.byref(cx)))
+        return r.value, qd.value, nb.value, ne.value, bool(cx.value)
+
+    @property
+    def data_ptr(self) -> int:
+        return int(self.ctx.lib.qs_tensor_data(self.h) or 0)
+
+    def download(self) -> QSpace:
+        rank, qdim, n, ne, cx = self.meta()
+        q = np.empty(max(n * rank * qdim, 1), np.int32)
+        dims = np.empty(max(n * rank, 1), np.int64)
+        offs = np.empty(max(n, 1), np.int64)
+        data = np.empty(max(ne * (2 if cx else 1), 1), np.float64)
+        check(self.ctx.lib.qs_tensor_download(self.ctx.h, self.h, q.ctypes.data_as(_capi.c_int32_p),
+                                              dims.ctypes.data_as(_capi.c_int64_p),
+                                              offs.ctypes.data_as(_capi.c_int64_p),
+                                              data.ctypes.data_as(_capi.c_double_p)))
+        return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, cx, self.info)
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.qs_tensor_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def upload(A: QSpace, ctx: Context | None = None) -> Tensor:
+    ctx = ctx or default_context()
+    v, keep = A.pack()
+    h = C.c_void_p()
+    check(ctx.lib.qs_tensor_upload(ctx.h, C.byref(v), C.byref(h)))
+    ctx.sync()
+    del keep
+    return Tensor(ctx, h, A.info)
+
+
+def contract_dev(A: Tensor, ia, B: Tensor, ib, perm=None, *, prec: str = "fp64", nslices: int = 0,
+                 tol: float = 1e-12, stats: dict | None = None) -> Tensor:
+    ctx = A.ctx
+    p, n = _perm_arg(perm)
+    o = make_opts(prec, nslices, tol)
+    st = Stats()
+    h = C.c_void_p()
+    check(ctx.lib.qs_contract_dev(ctx.h, A.h, _idx_str(ia), B.h, _idx_str(ib), p, n, C.byref(o),
+                                  C.byref(h), C.byref(st)))
+    if stats is not None:
+        stats.update(st.as_dict())
+    return Tensor(ctx, h)
+
+
+def permute_dev(A: Tensor, perm, conj=False) -> Tensor:
+    ctx = A.ctx
+    p, n = _perm_arg(perm)
+    h = C.c_void_p()
+    check(ctx.lib.qs_permute_dev(ctx.h, A.h, p, n, 1 if conj else 0, C.byref(h)))
+    return Tensor(ctx, h)

@@ -1,0 +1,117 @@
+"""Seeded synthetic inputs with the shapes of the benchmark workloads.
+
+The reference ships no benchmark data; these generators build block-sparse
+tensors with the stated sector structure and N(0,1) entries from
+``numpy.random.default_rng(seed)``.
+
+* ``mps_site_tensor`` -- abelian U(1)xU(1) (charge, 2Sz) MPS site tensor
+  A(L, s, R) with 41 charge sectors q in [-20, 20] per bond (one 2Sz sector
+  per charge, drawn from {-1, 0, 1}), sector dims round(512 exp(-q^2/50)/Z);
+  rule for the rounding: sectors that round to 0 are dropped and the
+  remainder goes to q = 0 so that every bond has D = 512.  The local site is
+  d = 4 with (charge, 2Sz) in {(-1,0), (0,+1), (0,-1), (+1,0)}.  A block
+  exists for every (L, s) whose fused (q_L + q_s, Sz_L + Sz_s) is a sector of
+  R.  The reduced density matrix is contractQS(A, '12*', A, '12').
+* ``grouped_pairs`` -- 2000 independent block pairs with M, N, K =
+  round(exp(U(ln 8, ln 1024))), complex128 N(0,1) entries and a CG factor
+  U(-1, 1) per pair; output = one block per pair.
+* ``random_abelian`` -- small random abelian QSpaces for parity tests.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .qspace import QSpace
+
+LOCAL_FERMION_SITE = [(-1, 0), (0, 1), (0, -1), (1, 0)]
+
+
+def bond_sectors(rng: np.random.Generator, D: int = 512, qmax: int = 20, width: float = 50.0):
+    q = np.arange(-qmax, qmax + 1)
+    w = np.exp(-q.astype(float) ** 2 / width)
+    d = np.rint(D * w / w.sum()).astype(np.int64)
+    sz = rng.integers(-1, 2, size=q.size)
+    keep = d > 0
+    q, d, sz = q[keep], d[keep], sz[keep]
+    d[np.flatnonzero(q == 0)[0]] += D - int(d.sum())
+    return [(int(a), int(b), int(c)) for a, b, c in zip(q, sz, d)]  # (charge, 2Sz, dim)
+
+
+def mps_site_tensor(seed: int = 0, D: int = 512, complex_data: bool = False) -> QSpace:
+    rng = np.random.default_rng(seed)
+    L = bond_sectors(rng, D)
+    R = bond_sectors(rng, D)
+    rmap = {(q, s): d for q, s, d in R}
+    QL, QS, QR, data = [], [], [], []
+    for (ql, sl, dl) in L:
+        for (qs, ss) in LOCAL_FERMION_SITE:
+            key = (ql + qs, sl + ss)
+            if key not in rmap:
+                continue
+            dr = rmap[key]
+            QL.append((ql, sl))
+            QS.append((qs, ss))
+            QR.append(key)
+            blk = rng.standard_normal((dl, 1, dr))
+            if complex_data:
+                blk = blk + 1j * rng.standard_normal((dl, 1, dr))
+            data.append(blk)
+    Q = [np.asarray(QL, np.int32), np.asarray(QS, np.int32), np.asarray(QR, np.int32)]
+    return QSpace(Q, data, {"itags": ["L", "s", "R*"]})
+
+
+def grouped_pairs(seed: int = 0, npairs: int = 2000, lo: int = 8, hi: int = 1024,
+                  complex_data: bool = True):
+    """Returns dict with M, N, K, afac arrays and lists of A (MxK), B (KxN)."""
+    rng = np.random.default_rng(seed)
+    dims = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), size=(npairs, 3)))).astype(np.int64)
+    afac = rng.uniform(-1.0, 1.0, size=npairs)
+    A, B = [], []
+    for p in range(npairs):
+        M, N, K = (int(x) for x in dims[p])
+        if complex_data:
+            a = rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))
+            b = rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))
+        else:
+            a = rng.standard_normal((M, K))
+            b = rng.standard_normal((K, N))
+        A.append(np.asfortranarray(a))
+        B.append(np.asfortranarray(b))
+    return {"M": dims[:, 0], "N": dims[:, 1], "K": dims[:, 2], "afac": afac, "A": A, "B": B,
+            "complex": complex_data}
+
+
+def random_abelian(rng: np.random.Generator, legs: list, nblk_max: int = 40,
+                   complex_data: bool = False, density: float = 0.6) -> QSpace:
+    """Random abelian QSpace over the given leg sector tables.
+
+    ``legs``: one list per leg of (label tuple, dim).  Blocks are a random
+    subset of the label combinations (no conservation law is imposed; the
+    contraction semantics do not need one)."""
+    combos = [[]]
+    for lg in legs:
+        combos = [c + [i] for c in combos for i in range(len(lg))]
+    rng.shuffle(combos)
+    n = min(nblk_max, max(1, int(len(combos) * density)))
+    combos = combos[:n]
+    qdim = len(legs[0][0][0])
+    Q = [np.zeros((n, qdim), np.int32) for _ in legs]
+    data = []
+    for b, c in enumerate(combos):
+        shape = []
+        for k, i in enumerate(c):
+            lab, d = legs[k][i]
+            Q[k][b] = lab
+            shape.append(d)
+        x = rng.standard_normal(shape)
+        if complex_data:
+            x = x + 1j * rng.standard_normal(shape)
+        data.append(x)
+    return QSpace(Q, data, {})
+
+
+def random_leg(rng: np.random.Generator, nsec: int = 4, dmax: int = 5, qdim: int = 1, qmax: int = 3):
+    labs = set()
+    while len(labs) < nsec:
+        labs.add(tuple(int(x) for x in rng.integers(-qmax, qmax + 1, size=qdim)))
+    return [(lab, int(rng.integers(1, dmax + 1))) for lab in sorted(labs)]
