@@ -20,24 +20,29 @@
 //    chosen so that |acc_g| < 2^24 for every partial sum: all tensor-core
 //    accumulations in FP32 are then exact integer arithmetic.  When the summed
 //    depth of a block exceeds that bound, the K loop is cut into chunks whose
-//    accumulators are drained and added in FP64.
+//    accumulators are drained and added exactly (int64).
 //  * The S digit tiles of B are laid side by side along N, so one
 //    tcgen05.mma with A-digit t and N = (S-t)*64 produces all products
 //    d_t * d'_u (u = 0..S-1-t) at once and drops each into the TMEM columns of
 //    accumulator group g = t+u (column offset 64*g).  S(S+1)/2 digit
 //    products therefore take about S + S/2 wide MMA instructions per K step.
-//  * The epilogue reads the S accumulators from TMEM, combines them with a
-//    double-FP32 Horner sum (exact until the final rounding to FP64), scales
-//    by 2^(E_i+F_j-2b) and the CG factor, and writes (or, for later chunks,
-//    adds) the FP64 result.  One CTA owns one 128x64 output tile and sums the
-//    block pairs in plan order: deterministic, no atomics.
+//  * The CG factor of each pair is folded into A's digits with an exact
+//    integer product (53 x 53 bits) before rounding, so pairs with different
+//    factors share the accumulators.
+//  * The epilogue reads the S accumulators from TMEM, combines them in int64
+//    fixed point, and assembles the FP64 result with integer bit operations
+//    (scale 2^(E_i+F_j-2b), round to nearest even): no FP64 instruction, as
+//    the FP64 pipe of GB300 is narrow.  Partial sums of later accumulator
+//    chunks are added exactly as int64 in the output slot.  One CTA owns one
+//    128x64 output tile and sums the block pairs in plan order:
+//    deterministic, no atomics.
 //
 // Data movement: a slicing kernel writes the digits of every pair operand once
 // into an HBM arena, pre-tiled in the tcgen05 K-major, no-swizzle core-matrix
 // layout (8 rows x 16 bytes per core matrix); the GEMM kernel then moves
 // whole digit tiles with 1-D TMA bulk copies (cp.async.bulk + mbarrier
 // transaction counts) into a multi-stage shared-memory ring.  Warp roles:
-// warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2..5 =
+// warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2..9 =
 // epilogue (one TMEM lane quarter each).  Every mbarrier wait is bounded; on
 // timeout the kernel records an error code, stops issuing work, waits a
 // bounded time for what is in flight, frees its TMEM and returns.
@@ -71,8 +76,9 @@ struct SplitPair {
   int32_t Mr, Kr;          // real rows of op(A~) and real depth
   int32_t MT, NT, KB;      // tile counts
   int32_t eoff, foff;      // exponent array offsets of the output block
-  int32_t e_afac;          // exponent added by a folded CG factor
-  double afac_fold;        // factor folded into A's digits (1: epilogue)
+  int32_t e_afac;          // exponent added by the CG factor (|afac| < 2^e)
+  int32_t fe, fneg;        // CG factor folded into A's digits: fm 2^fe, sign
+  uint64_t fm;             // (fm = 0: factor 1)
 };
 
 struct SplitTile {
@@ -82,7 +88,7 @@ struct SplitTile {
   int32_t Mr, N, ldc;
   int32_t eoff, foff;
   int32_t nchunk;          // drains of the accumulators
-  double afac;             // epilogue factor
+  int32_t rshift;          // bits dropped below the lowest group (int64 headroom)
 };
 
 // ------------------------------------------------------------ bit helpers
@@ -92,20 +98,55 @@ __device__ __forceinline__ int exp_key(double x) {
   return ((b << 1) != 0) ? max(be, 1) : 0;
 }
 
-// Balanced digits of N = round(x * 2^(b*S - E)); |x| < 2^E is guaranteed by
-// construction of E.  Integer operations only.
+// A factor f (CG coefficient) as an exact integer mantissa and exponent,
+// f = fm * 2^fe; fm = 0 means "no factor" (f = 1); fe = -100000 means f = 0.
+struct Factor {
+  unsigned long long fm;
+  int fe;
+  bool neg;
+};
+
+__host__ __device__ inline Factor make_factor(double f) {
+  Factor r{0ull, 0, false};
+  if (f == 1.0) return r;
+  unsigned long long bits;
+  memcpy(&bits, &f, 8);
+  int be = (int)((bits >> 52) & 0x7ff);
+  unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+  if (be == 0) be = 1; else m |= (1ull << 52);
+  r.fm = m ? m : 0ull;
+  r.fe = be - 1075;
+  r.neg = (bits >> 63) != 0;
+  if (!m) { r.fm = 0; r.fe = 0; r.neg = false; r.fe = -100000; }  // f == 0
+  return r;
+}
+
+// Balanced digits of N = round(x f 2^(b*S - E)); |x f| < 2^E is guaranteed
+// by construction of E.  Integer operations only.
 template <int S>
-__device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S]) {
+__device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S], const Factor &F) {
   const long long bits = __double_as_longlong(x);
   int be = (int)((bits >> 52) & 0x7ff);
-  long long mant = bits & 0xFFFFFFFFFFFFFLL;
-  if (be == 0) be = 1; else mant |= (1LL << 52);
+  unsigned long long mant = bits & 0xFFFFFFFFFFFFFull;
+  if (be == 0) be = 1; else mant |= (1ull << 52);
   long long N = 0;
-  if (mant != 0) {
-    const int shift = be - 1075 + b * S - E;
-    if (shift >= 0) N = mant << min(shift, 62);
-    else if (shift > -62) N = (mant + (1LL << (-shift - 1))) >> (-shift);
-    if (bits < 0) N = -N;
+  bool neg = bits < 0;
+  if (mant != 0 && F.fe > -100000) {
+    if (F.fm == 0) {
+      // N = round(mant * 2^shift)
+      const int shift = be - 1075 + b * S - E;
+      if (shift >= 0) N = (long long)(mant << min(shift, 62));
+      else if (shift > -62) N = (long long)((mant + (1ull << (-shift - 1))) >> (-shift));
+    } else {
+      // exact 106-bit product with the factor's mantissa, then the same
+      // rounding shift (|x f| < 2^E holds by construction of E)
+      const unsigned __int128 P = (unsigned __int128)mant * F.fm;
+      const int shift = be - 1075 + F.fe + b * S - E;
+      if (shift >= 0) N = (long long)(P << min(shift, 62));
+      else if (shift > -127) N = (long long)((P + ((unsigned __int128)1 << (-shift - 1))) >> (-shift));
+      neg ^= F.neg;
+    }
+    if (neg) N = -N;
   }
   const long long half = 1LL << (b - 1), mask = (1LL << b) - 1;
 #pragma unroll
@@ -194,7 +235,47 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
   const SplitPair P = pairs[tk.x];
   const int mt = tk.y, kb = tk.z;
   const bool ta = P.trans & 1, ca = P.trans & 4;
+  const Factor Fa{P.fm, P.fe, P.fneg != 0};
   uint8_t *tile = arena + P.as_off + ((int64_t)(mt * P.KB + kb) * S) * A_DIGIT_BYTES;
+  if constexpr (CPLX) {
+    // one task = one complex row m (real rows 2m, 2m+1 of A~) x 4 complex k:
+    // the digits of re and im are cut once and placed as
+    //   row 2m:   ( re, -im )    row 2m+1: ( im, re )
+    for (int w = threadIdx.x; w < (TMS / 2) * (TKS / 8); w += blockDim.x) {
+      const int ml = w % (TMS / 2), q = w / (TMS / 2);
+      const int m = mt * (TMS / 2) + ml;
+      const bool rv = m < P.M;
+      const int Ei = rv ? E[P.eoff + 2 * m] : 0;
+      uint32_t p0[S][4], p1[S][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = (kb * TKS + q * 8) / 2 + j;
+        double re = 0.0, im = 0.0;
+        if (rv && k < P.K) {
+          const double2 a = reinterpret_cast<const double2 *>(A)[
+              P.a_off + (ta ? (int64_t)k + (int64_t)m * P.lda : (int64_t)m + (int64_t)k * P.lda)];
+          re = a.x;
+          im = ca ? -a.y : a.y;
+        }
+        int dr[S], di[S];
+        make_digits<S>(re, Ei, b, dr, Fa);
+        make_digits<S>(im, Ei, b, di, Fa);
+#pragma unroll
+        for (int t = 0; t < S; ++t) {
+          p0[t][j] = pack_bf16(dr[t], -di[t]);
+          p1[t][j] = pack_bf16(di[t], dr[t]);
+        }
+      }
+      const int r0 = 2 * ml, r1 = r0 + 1;
+      uint8_t *d0 = tile + ((r0 >> 3) * 4 + q) * 128 + (r0 & 7) * 16;
+      uint8_t *d1 = tile + ((r1 >> 3) * 4 + q) * 128 + (r1 & 7) * 16;
+#pragma unroll
+      for (int t = 0; t < S; ++t) {
+        *reinterpret_cast<uint4 *>(d0 + t * A_DIGIT_BYTES) = make_uint4(p0[t][0], p0[t][1], p0[t][2], p0[t][3]);
+        *reinterpret_cast<uint4 *>(d1 + t * A_DIGIT_BYTES) = make_uint4(p1[t][0], p1[t][1], p1[t][2], p1[t][3]);
+      }
+    }
+  } else {
   for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
     const int r = w % TMS, q = w / TMS;
     const int rr = mt * TMS + r;
@@ -208,19 +289,9 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
       for (int h = 0; h < 2; ++h) {
         const int kk = kb * TKS + q * 8 + e + h;
         double v = 0.0;
-        if (rv && kk < P.Kr) {
-          if (CPLX) {
-            const int m = rr >> 1, rho = rr & 1, k = kk >> 1, kap = kk & 1;
-            const double2 a = reinterpret_cast<const double2 *>(A)[
-                P.a_off + (ta ? (int64_t)k + (int64_t)m * P.lda : (int64_t)m + (int64_t)k * P.lda)];
-            const double ai = ca ? -a.y : a.y;
-            v = rho == 0 ? (kap == 0 ? a.x : -ai) : (kap == 0 ? ai : a.x);
-          } else {
-            v = A[P.a_off + (ta ? (int64_t)kk + (int64_t)rr * P.lda : (int64_t)rr + (int64_t)kk * P.lda)];
-          }
-          if (P.afac_fold != 1.0) v *= P.afac_fold;
-        }
-        make_digits<S>(v, Ei, b, dd[h]);
+        if (rv && kk < P.Kr)
+          v = A[P.a_off + (ta ? (int64_t)kk + (int64_t)rr * P.lda : (int64_t)rr + (int64_t)kk * P.lda)];
+        make_digits<S>(v, Ei, b, dd[h], Fa);
       }
 #pragma unroll
       for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack_bf16(dd[0][t], dd[1][t]);
@@ -229,6 +300,7 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
 #pragma unroll
     for (int t = 0; t < S; ++t)
       *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+  }
   }
 }
 
@@ -267,7 +339,7 @@ slice_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
             v = B[P.b_off + (tb ? (int64_t)n + (int64_t)kk * P.ldb : (int64_t)kk + (int64_t)n * P.ldb)];
           }
         }
-        make_digits<S>(v, Fj, b, dd[h]);
+        make_digits<S>(v, Fj, b, dd[h], Factor{0ull, 0, false});
       }
 #pragma unroll
       for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack_bf16(dd[0][t], dd[1][t]);
@@ -369,11 +441,42 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Exact double-FP32 helpers for the recombination.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
+// Recombination without the FP64 pipe.  The S accumulators hold exact
+// integers (|acc_g| <= 2^24); their weighted sum
+//   V = sum_g acc_g 2^(b(S-1-g) - r)
+// is formed in int64 (r low bits of the smallest group are rounded away so
+// that V and the sum over accumulator chunks keep headroom), then turned into
+// an FP64 value V * 2^scale by integer bit assembly (round to nearest even).
+template <int S>
+__device__ __forceinline__ long long combine_groups(const float (&acc)[S][8], int cc, int b, int r) {
+  long long V = 0;
+#pragma unroll
+  for (int g = 0; g < S; ++g) {
+    const long long a = (long long)__float2int_rn(acc[g][cc]);
+    const int sh = b * (S - 1 - g) - r;
+    if (sh >= 0) V += a << sh;
+    else V += (a + (1LL << (-sh - 1))) >> (-sh);
+  }
+  return V;
+}
+
+__device__ __forceinline__ double fixed_to_double(long long V, int scale) {
+  if (V == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)V & 0x8000000000000000ull;
+  const unsigned long long a = V < 0 ? (unsigned long long)(-V) : (unsigned long long)V;
+  const int lz = __clzll(a);
+  const unsigned long long m = a << lz;  // leading one at bit 63
+  unsigned long long mant = m >> 11;
+  const unsigned long long rem = m & 0x7FFull;
+  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  int e = 63 - lz + scale;  // value = 1.f * 2^e
+  if (mant >> 53) {
+    mant >>= 1;
+    ++e;
+  }
+  const int be = e + 1023;
+  if (be <= 0 || be >= 2047) return ldexp((double)V, scale);  // subnormal / overflow: rare path
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 // Chunking rule shared by the host and the MMA issuer: a new chunk starts
@@ -383,7 +486,7 @@ __device__ __forceinline__ int kblock_depth(int Kr, int kb) { return min(TKS, Kr
 
 // ------------------------------------------------------------ GEMM kernel
 template <int S>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(320, 1)
 gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restrict__ pairs,
                   const uint8_t *__restrict__ arena, const int *__restrict__ E,
                   const int *__restrict__ F, double *__restrict__ C, int b, int nstages,
@@ -409,7 +512,7 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restri
       mbar_init(&empty[s], 1);
     }
     mbar_init(acc_full, 1);
-    mbar_init(acc_empty, 4);  // one arrive per epilogue warp
+    mbar_init(acc_empty, 8);  // one arrive per epilogue warp
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -511,14 +614,18 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restri
       }
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..5)
+    // ------------------------------------------- epilogue (warps 2..9)
+    // warp w reads TMEM lane quarter w % 4; warps 2..5 take columns 0..31,
+    // warps 6..9 columns 32..63.
     const int q = warp & 3;
+    const int cbase = warp < 6 ? 0 : TNS / 2;
     const int row = q * 32 + lane;
     const int i_glob = T.mt * TMS + row;
     const bool rv = i_glob < T.Mr;
     const int Ei = rv ? E[T.eoff + i_glob] : 0;
-    const float sb = ldexpf(1.0f, -b);
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    // value = V * 2^(E_i + F_j + scale0), V the fixed-point group sum
+    const int scale0 = T.rshift - b * (S + 1);
     for (int ch = 0; ch < T.nchunk; ++ch) {
       // one lane polls; the warp proceeds together (tcgen05.ld is .aligned)
       int ok = 1;
@@ -526,8 +633,9 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restri
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       tc_fence_after();
+      const bool last = ch + 1 == T.nchunk;
 #pragma unroll 1
-      for (int c0 = 0; c0 < TNS; c0 += 8) {
+      for (int c0 = cbase; c0 < cbase + TNS / 2; c0 += 8) {
         float acc[S][8];
 #pragma unroll
         for (int g = 0; g < S; ++g) tmem_ld8(lane_base + (uint32_t)(g * TNS + c0), acc[g]);
@@ -536,25 +644,13 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restri
         for (int cc = 0; cc < 8; ++cc) {
           const int j = T.nt * TNS + c0 + cc;
           if (!rv || j >= T.N) continue;
-          // Horner sum of 2^(-b g) acc_g in double-FP32 (hi, lo)
-          float hi = acc[S - 1][cc], lo = 0.0f;
-#pragma unroll
-          for (int g = S - 2; g >= 0; --g) {
-            hi *= sb;
-            lo *= sb;
-            float s, e;
-            two_sum(hi, acc[g][cc], s, e);
-            lo += e;
-            const float h2 = s + lo;
-            lo = lo - (h2 - s);
-            hi = h2;
-          }
-          double v = (double)hi + (double)lo;
-          const int ex = Ei + F[T.foff + j] - 2 * b;
-          v = ldexp(v, ex) * T.afac;
+          long long V = combine_groups<S>(acc, cc, b, T.rshift);
           double *dst = C + T.c_off + (int64_t)i_glob + (int64_t)j * T.ldc;
-          if (ch == 0) *dst = v;
-          else *dst += v;
+          // earlier chunks of this tile left their exact partial sums as
+          // int64 in the output slot
+          if (ch > 0) V += *reinterpret_cast<const long long *>(dst);
+          if (last) *dst = fixed_to_double(V, Ei + F[T.foff + j] + scale0);
+          else *reinterpret_cast<long long *>(dst) = V;
         }
       }
       tc_fence_before();
@@ -610,7 +706,7 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
   const size_t sm = smem_bytes<S>(nst);
   QS_CUDA(cudaFuncSetAttribute(gemm_split_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   ctx->mark(1);
-  gemm_split_kernel<S><<<ntiles, 192, sm, st>>>(d_tiles, d_pairs, arena, dE, dF, C, b, nst, kchunk, ctx->d_err);
+  gemm_split_kernel<S><<<ntiles, 320, sm, st>>>(d_tiles, d_pairs, arena, dE, dF, C, b, nst, kchunk, ctx->d_err);
   QS_LAUNCHED(ctx);
   ctx->mark(2);
 }
@@ -618,24 +714,62 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
 }  // namespace
 
 // ---------------------------------------------------------------- host side
-DigitPlan choose_digits(int64_t kreal, double tol, int forced_slices) {
-  (void)kreal;
+// Largest summed (real) depth that keeps every accumulator group exact:
+// |sum_{t+u=g} d_t d'_u| <= 2^(2b) (1 + max(0, g-1)/4) per term.
+static int kchunk_of(int b, int S) {
+  const double grow = std::max(1.0, 1.0 + (S - 2) / 4.0);
+  const double kc = std::floor(16777216.0 / (std::ldexp(1.0, 2 * b) * grow));
+  return (int)std::min(kc, 1.0e9);
+}
+
+// Accumulator drains of one output block: a new chunk starts when the next K
+// block would push the chunk's summed depth above kchunk (the MMA issuer
+// applies the same rule).
+static int chunks_of(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1, int cm, int kchunk) {
+  int nchunk = 1, depth = 0;
+  bool fresh = true;
+  for (int64_t p = p0; p < p1; ++p) {
+    const int Kr = pairs[p].K * cm;
+    const int KB = std::max(1, (Kr + TKS - 1) / TKS);
+    for (int kb = 0; kb < KB; ++kb) {
+      const int dk = std::max(std::min(TKS, Kr - kb * TKS), 0);
+      if (!fresh && depth + dk > kchunk) { ++nchunk; depth = 0; fresh = true; }
+      depth += dk;
+      fresh = false;
+    }
+  }
+  return nchunk;
+}
+
+// Digit plan: the (bits, digits) pair that reaches the wanted precision at
+// the lowest modelled cost over the actual tiles -- tensor work grows as
+// S(S+1)/2 per K block, and each accumulator drain costs about as much as
+// DRAIN_UNITS single-digit K blocks.
+constexpr double DRAIN_UNITS = 50.0;
+
+DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                            const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
+                            double tol, int forced_slices) {
   if (!(tol > 0)) tol = 1e-12;
   // bits of precision wanted: the tolerance plus a margin for the growth of
   // the error with the summed depth relative to |C|.
   const int need = (int)std::ceil(-std::log2(tol)) + 8;
   DigitPlan best{0, 0, 0};
   double best_cost = 1e300;
+  const int64_t nb = (int64_t)blk_M.size();
   for (int b = 8; b >= 5; --b) {
     int S = forced_slices > 0 ? forced_slices : (need - 1 + b - 1) / b;
     S = std::max(S, 2);
     if (S > 8) continue;
-    // largest summed depth that keeps every accumulator exact
-    const double grow = std::max(1.0, 1.0 + (S - 2) / 4.0);
-    const double kchunk = std::floor(16777216.0 / (std::ldexp(1.0, 2 * b) * grow));
+    const int kchunk = kchunk_of(b, S);
     if (kchunk < TKS) continue;
-    // cost model: digit products per K step, plus a drain per chunk
-    const double cost = S * (S + 1) / 2.0 * (1.0 + 24.0 / kchunk);
+    double cost = 0;
+    for (int64_t g = 0; g < nb; ++g) {
+      const double tiles = double((blk_M[g] * cm + TMS - 1) / TMS) * double((blk_N[g] + TNS - 1) / TNS);
+      double kbs = 0;
+      for (int64_t p = grp[g]; p < grp[g + 1]; ++p) kbs += std::max(1, (pairs[p].K * cm + TKS - 1) / TKS);
+      cost += tiles * (S * (S + 1) / 2.0 * kbs + DRAIN_UNITS * chunks_of(pairs, grp[g], grp[g + 1], cm, kchunk));
+    }
     if (cost < best_cost) {
       best_cost = cost;
       best.bits = b;
@@ -647,10 +781,12 @@ DigitPlan choose_digits(int64_t kreal, double tol, int forced_slices) {
   return best;
 }
 
-static int kchunk_of(int b, int S) {
-  const double grow = std::max(1.0, 1.0 + (S - 2) / 4.0);
-  const double kc = std::floor(16777216.0 / (std::ldexp(1.0, 2 * b) * grow));
-  return (int)std::min(kc, 1.0e9);
+DigitPlan choose_digits(int64_t kreal, double tol, int forced_slices) {
+  std::vector<PairDesc> one(1);
+  one[0].M = TMS;
+  one[0].N = TNS;
+  one[0].K = (int32_t)std::max<int64_t>(kreal, 1);
+  return choose_digits_for(one, {0, 1}, {TMS}, {TNS}, 1, tol, forced_slices);
 }
 
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
@@ -660,13 +796,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   SplitResult res;
   const int64_t nb = (int64_t)blk_M.size();
   const int cm = cplx ? 2 : 1;
-  int64_t kmax = 0;
-  for (int64_t g = 0; g < nb; ++g) {
-    int64_t ks = 0;
-    for (int64_t p = grp[g]; p < grp[g + 1]; ++p) ks += (int64_t)pairs[p].K * cm;
-    kmax = std::max(kmax, ks);
-  }
-  DigitPlan dp = choose_digits(kmax, tol, forced_slices);
+  DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices);
   const int S = dp.nslices, b = dp.bits;
   const int kchunk = kchunk_of(b, S);
   res.nslices = S;
@@ -689,11 +819,8 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   std::vector<int4> at, bt;
   std::vector<SplitTile> tiles;
   for (int64_t g = 0; g < nb; ++g) {
-    // one CG factor for the whole block goes into the epilogue; otherwise
-    // each pair's factor is folded into its A digits
-    bool same = true;
-    for (int64_t p = grp[g]; p < grp[g + 1]; ++p) same &= (pairs[p].afac == pairs[grp[g]].afac);
-    int64_t depth_blk = 0;
+    // every pair's CG factor is folded into its A digits (exact integer
+    // product), so the pairs of a block share the accumulators
     for (int64_t p = grp[g]; p < grp[g + 1]; ++p) {
       const PairDesc &d = pairs[p];
       SplitPair &s = sp[p];
@@ -712,15 +839,13 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
       s.KB = std::max(1, (s.Kr + TKS - 1) / TKS);
       s.eoff = (int32_t)eoff[g];
       s.foff = (int32_t)foff[g];
-      if (same) {
-        s.afac_fold = 1.0;
-        s.e_afac = 0;
-      } else {
-        s.afac_fold = d.afac;
-        int e = 0;
-        std::frexp(d.afac, &e);
-        s.e_afac = d.afac != 0.0 ? e : 0;
-      }
+      const Factor f = make_factor(d.afac);
+      s.fm = f.fm;
+      s.fe = f.fe;
+      s.fneg = f.neg ? 1 : 0;
+      int e = 0;
+      if (d.afac != 1.0 && d.afac != 0.0) std::frexp(d.afac, &e);
+      s.e_afac = e;
       s.as_off = arena;
       arena += (int64_t)s.MT * s.KB * S * A_DIGIT_BYTES;
       s.bs_off = arena;
@@ -731,19 +856,13 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
         for (int kb = 0; kb < s.KB; ++kb) at.push_back(make_int4((int)p, mt, kb, 0));
       for (int nt = 0; nt < s.NT; ++nt)
         for (int kb = 0; kb < s.KB; ++kb) bt.push_back(make_int4((int)p, nt, kb, 0));
-      depth_blk += s.Kr;
     }
-    // number of accumulator drains of this block's tiles (same rule as the
-    // MMA issuer: per K block of depth min(32, Kr - 32 kb))
-    int nchunk = 1, depth = 0;
-    bool fresh = true;
-    for (int64_t p = grp[g]; p < grp[g + 1]; ++p)
-      for (int kb = 0; kb < sp[p].KB; ++kb) {
-        const int dk = std::max(std::min(TKS, sp[p].Kr - kb * TKS), 0);
-        if (!fresh && depth + dk > kchunk) { ++nchunk; depth = 0; fresh = true; }
-        depth += dk;
-        fresh = false;
-      }
+    const int nchunk = chunks_of(pairs, grp[g], grp[g + 1], cm, kchunk);
+    // int64 headroom of the fixed-point sum over all chunks:
+    // nchunk * 2^(24.2 + b(S-1) - r) < 2^63
+    int lg = 0;
+    while ((1 << lg) < nchunk) ++lg;
+    const int rshift = std::max(0, 25 + b * (S - 1) + lg - 63);
     const int MT = (blk_M[g] * cm + TMS - 1) / TMS, NT = (blk_N[g] + TNS - 1) / TNS;
     for (int nt = 0; nt < NT; ++nt)
       for (int mt = 0; mt < MT; ++mt) {
@@ -759,7 +878,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
         t.eoff = (int32_t)eoff[g];
         t.foff = (int32_t)foff[g];
         t.nchunk = nchunk;
-        t.afac = same ? pairs[grp[g]].afac : 1.0;
+        t.rshift = rshift;
         tiles.push_back(t);
       }
   }
