@@ -50,6 +50,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "qs_internal.h"
 #include "qs_split.h"
@@ -59,10 +60,10 @@ namespace qs {
 namespace {
 
 constexpr int TMS = 128;          // output tile rows (MMA M)
-constexpr int TNS = 64;           // output tile cols (per digit group)
+constexpr int TNS = 32;           // output tile cols (per digit group)
 constexpr int TKS = 32;           // K block per pipeline stage
 constexpr int A_DIGIT_BYTES = TMS * TKS * 2;  // 8 KB
-constexpr int B_DIGIT_BYTES = TNS * TKS * 2;  // 4 KB
+constexpr int B_DIGIT_BYTES = TNS * TKS * 2;  // 2 KB
 constexpr int EMPTY_EXP = -30000;
 constexpr int SMEM_HDR = 1024;
 constexpr int SMEM_LIMIT = 227 * 1024;
@@ -138,12 +139,14 @@ __device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S],
       if (shift >= 0) N = (long long)(mant << min(shift, 62));
       else if (shift > -62) N = (long long)((mant + (1ull << (-shift - 1))) >> (-shift));
     } else {
-      // exact 106-bit product with the factor's mantissa, then the same
-      // rounding shift (|x f| < 2^E holds by construction of E)
-      const unsigned __int128 P = (unsigned __int128)mant * F.fm;
-      const int shift = be - 1075 + F.fe + b * S - E;
+      // product with the factor's mantissa: the upper 64 bits of
+      // (mant 2^11) (fm 2^11), i.e. mant fm 2^-42 truncated (relative error
+      // < 2^-63, far below the 2^-(bS) of the digits), then the rounding shift
+      // (|x f| < 2^E holds by construction of E)
+      const unsigned long long P = __umul64hi(mant << 11, F.fm << 11);
+      const int shift = be - 1075 + F.fe + 42 + b * S - E;
       if (shift >= 0) N = (long long)(P << min(shift, 62));
-      else if (shift > -127) N = (long long)((P + ((unsigned __int128)1 << (-shift - 1))) >> (-shift));
+      else if (shift > -64) N = (long long)((P >> (-shift - 1)) + 1 >> 1);
       neg ^= F.neg;
     }
     if (neg) N = -N;
@@ -158,9 +161,16 @@ __device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S],
   d[0] = (int)N;
 }
 
+// BF16 bits of a small integer |d| <= 2^22 (digits are |d| <= 256, nine
+// significant bits at most, so the BF16 value is exact): the FP32 value is
+// formed with the 1.5*2^23 offset (one integer add, one FP32 add), its upper
+// half is the BF16 pattern.  Avoids the int-to-float conversion unit.
+__device__ __forceinline__ uint32_t bf16_bits(int d) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+  return __float_as_uint(f) >> 16;
+}
 __device__ __forceinline__ uint32_t pack_bf16(int lo, int hi) {
-  __nv_bfloat162 h = __floats2bfloat162_rn((float)lo, (float)hi);
-  return *reinterpret_cast<uint32_t *>(&h);
+  return (bf16_bits(hi) << 16) | bf16_bits(lo);
 }
 
 // --------------------------------------------------------- exponent passes
@@ -174,14 +184,28 @@ exp_rows_kernel(const SplitPair *__restrict__ pairs, const int2 *__restrict__ ta
   const int m = tk.y + threadIdx.x;
   if (m >= P.M) return;
   const bool ta = P.trans & 1;
+  const int64_t sk = ta ? 1 : P.lda, base = P.a_off + (ta ? (int64_t)m * P.lda : (int64_t)m);
   int key = 0;
-  for (int k = 0; k < P.K; ++k) {
-    const int64_t idx = ta ? (int64_t)k + (int64_t)m * P.lda : (int64_t)m + (int64_t)k * P.lda;
+  int k = 0;
+  // four independent loads in flight per thread
+  for (; k + 4 <= P.K; k += 4) {
     if (CPLX) {
-      const double2 v = reinterpret_cast<const double2 *>(A)[P.a_off + idx];
+      const double2 *a = reinterpret_cast<const double2 *>(A) + base;
+      const double2 v0 = a[(k + 0) * sk], v1 = a[(k + 1) * sk], v2 = a[(k + 2) * sk], v3 = a[(k + 3) * sk];
+      key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
+                         max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
+    } else {
+      const double *a = A + base;
+      key = max(key, max(max(exp_key(a[(k + 0) * sk]), exp_key(a[(k + 1) * sk])),
+                         max(exp_key(a[(k + 2) * sk]), exp_key(a[(k + 3) * sk]))));
+    }
+  }
+  for (; k < P.K; ++k) {
+    if (CPLX) {
+      const double2 v = reinterpret_cast<const double2 *>(A)[base + k * sk];
       key = max(key, max(exp_key(v.x), exp_key(v.y)));
     } else {
-      key = max(key, exp_key(A[P.a_off + idx]));
+      key = max(key, exp_key(A[base + k * sk]));
     }
   }
   if (!key) return;
@@ -215,6 +239,47 @@ exp_cols_kernel(const SplitPair *__restrict__ pairs, const int2 *__restrict__ ta
     }
   }
   if (key) atomicMax(&F[P.foff + n], key - 1022);
+}
+
+// Same maxima for lines stored contiguously along k (rows of a transposed
+// op(A), columns of a plain op(B)): one warp per line, lanes stride over k
+// (coalesced), warp max reduction.  Task = (pair, first line, role 0 = A
+// rows / 1 = B columns); 8 lines per CTA.
+template <bool CPLX>
+__global__ void __launch_bounds__(256)
+exp_contig_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
+                  const double *__restrict__ A, const double *__restrict__ B, int *__restrict__ E,
+                  int *__restrict__ F) {
+  const int4 tk = tasks[blockIdx.x];
+  const SplitPair P = pairs[tk.x];
+  const int lane = threadIdx.x & 31;
+  const int line = tk.y + (threadIdx.x >> 5);
+  const bool rowsA = tk.z == 0;
+  if (line >= (rowsA ? P.M : P.N)) return;
+  const double *base = rowsA ? A : B;
+  const int64_t off = rowsA ? P.a_off + (int64_t)line * P.lda : P.b_off + (int64_t)line * P.ldb;
+  int key = 0;
+  for (int k = lane; k < P.K; k += 32) {
+    if (CPLX) {
+      const double2 v = reinterpret_cast<const double2 *>(base)[off + k];
+      key = max(key, max(exp_key(v.x), exp_key(v.y)));
+    } else {
+      key = max(key, exp_key(base[off + k]));
+    }
+  }
+  key = __reduce_max_sync(0xffffffffu, key);
+  if (lane != 0 || !key) return;
+  if (rowsA) {
+    const int e = key - 1022 + P.e_afac;
+    if (CPLX) {
+      atomicMax(&E[P.eoff + 2 * line], e);
+      atomicMax(&E[P.eoff + 2 * line + 1], e);
+    } else {
+      atomicMax(&E[P.eoff + line], e);
+    }
+  } else {
+    atomicMax(&F[P.foff + line], key - 1022);
+  }
 }
 
 __global__ void fill_int_kernel(int *p, int64_t n, int v) {
@@ -262,8 +327,9 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
         make_digits<S>(im, Ei, b, di, Fa);
 #pragma unroll
         for (int t = 0; t < S; ++t) {
-          p0[t][j] = pack_bf16(dr[t], -di[t]);
-          p1[t][j] = pack_bf16(di[t], dr[t]);
+          const uint32_t hr = bf16_bits(dr[t]), hi = bf16_bits(di[t]);
+          p0[t][j] = ((hi ^ 0x8000u) << 16) | hr;  // ( re, -im )
+          p1[t][j] = (hr << 16) | hi;              // ( im,  re )
         }
       }
       const int r0 = 2 * ml, r1 = r0 + 1;
@@ -430,14 +496,13 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
                    smem_u32(bar))
                : "memory");
 }
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-  uint32_t r[8];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-      : "r"(taddr));
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -447,8 +512,8 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // is formed in int64 (r low bits of the smallest group are rounded away so
 // that V and the sum over accumulator chunks keep headroom), then turned into
 // an FP64 value V * 2^scale by integer bit assembly (round to nearest even).
-template <int S>
-__device__ __forceinline__ long long combine_groups(const float (&acc)[S][8], int cc, int b, int r) {
+template <int S, int W>
+__device__ __forceinline__ long long combine_groups(const float (&acc)[S][W], int cc, int b, int r) {
   long long V = 0;
 #pragma unroll
   for (int g = 0; g < S; ++g) {
@@ -485,34 +550,45 @@ __device__ __forceinline__ double fixed_to_double(long long V, int scale) {
 __device__ __forceinline__ int kblock_depth(int Kr, int kb) { return min(TKS, Kr - kb * TKS); }
 
 // ------------------------------------------------------------ GEMM kernel
+// Persistent: one CTA per SM walks tiles r*G + c (snake order over the
+// depth-sorted tile list so every CTA gets a similar mix).  The three roles
+// step through the same sequence; the TMA ring and the accumulator hand-off
+// run continuously across tile boundaries.  TMEM holds two accumulator sets
+// (S groups x 32 columns each): the epilogue drains one while the MMA issuer
+// fills the other.
+__device__ __forceinline__ int tile_of(int r, int c, int G) { return r * G + ((r & 1) ? (G - 1 - c) : c); }
+
 template <int S>
 __global__ void __launch_bounds__(320, 1)
-gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restrict__ pairs,
+gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPair *__restrict__ pairs,
                   const uint8_t *__restrict__ arena, const int *__restrict__ E,
                   const int *__restrict__ F, double *__restrict__ C, int b, int nstages,
                   int kchunk, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);       // [8]
   uint64_t *empty = full + 8;                                 // [8]
-  uint64_t *acc_full = full + 16;
-  uint64_t *acc_empty = full + 17;
+  uint64_t *acc_full = full + 16;                             // [2]
+  uint64_t *acc_empty = full + 18;                            // [2]
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 512);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 516);
   uint8_t *stages = smem + SMEM_HDR;
   constexpr uint32_t A_BYTES = S * A_DIGIT_BYTES, B_BYTES = S * B_DIGIT_BYTES;
   constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-  constexpr uint32_t NCOLS = (S * TNS <= 256) ? 256 : 512;
+  constexpr uint32_t SET_COLS = S * TNS;  // columns of one accumulator set
+  constexpr uint32_t NCOLS = (2 * SET_COLS <= 256) ? 256 : 512;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const SplitTile T = tiles[blockIdx.x];
+  const int G = gridDim.x, cta = blockIdx.x;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < nstages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(acc_full, 1);
-    mbar_init(acc_empty, 8);  // one arrive per epilogue warp
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&acc_full[s], 1);
+      mbar_init(&acc_empty[s], 8);  // one arrive per epilogue warp
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -532,19 +608,24 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restri
       // ------------------------------------------------ TMA producer
       int it = 0;
       bool ok = true;
-      for (int p = T.p0; p < T.p1 && ok; ++p) {
-        const SplitPair &P = pairs[p];
-        const int KB = P.KB;
-        const uint8_t *a_src = arena + P.as_off + (int64_t)T.mt * KB * A_BYTES;
-        const uint8_t *b_src = arena + P.bs_off + (int64_t)T.nt * KB * B_BYTES;
-        for (int kb = 0; kb < KB; ++kb, ++it) {
-          const int st = it % nstages;
-          const uint32_t ph = (uint32_t)((it / nstages) & 1);
-          if (!mbar_wait(&empty[st], ph ^ 1u, abort_flag, err, 1)) { ok = false; break; }
-          uint8_t *sa = stages + (size_t)st * STAGE_BYTES;
-          mbar_expect_tx(&full[st], STAGE_BYTES);
-          bulk_g2s(sa, a_src + (int64_t)kb * A_BYTES, A_BYTES, &full[st]);
-          bulk_g2s(sa + A_BYTES, b_src + (int64_t)kb * B_BYTES, B_BYTES, &full[st]);
+      for (int r = 0; ok; ++r) {
+        const int ti = tile_of(r, cta, G);
+        if (ti >= ntiles) break;
+        const SplitTile &T = tiles[ti];
+        for (int p = T.p0; p < T.p1 && ok; ++p) {
+          const SplitPair &P = pairs[p];
+          const int KB = P.KB;
+          const uint8_t *a_src = arena + P.as_off + (int64_t)T.mt * KB * A_BYTES;
+          const uint8_t *b_src = arena + P.bs_off + (int64_t)T.nt * KB * B_BYTES;
+          for (int kb = 0; kb < KB; ++kb, ++it) {
+            const int st = it % nstages;
+            const uint32_t ph = (uint32_t)((it / nstages) & 1);
+            if (!mbar_wait(&empty[st], ph ^ 1u, abort_flag, err, 1)) { ok = false; break; }
+            uint8_t *sa = stages + (size_t)st * STAGE_BYTES;
+            mbar_expect_tx(&full[st], STAGE_BYTES);
+            bulk_g2s(sa, a_src + (int64_t)kb * A_BYTES, A_BYTES, &full[st]);
+            bulk_g2s(sa + A_BYTES, b_src + (int64_t)kb * B_BYTES, B_BYTES, &full[st]);
+          }
         }
       }
       // Wait (bounded) until every stage issued has landed, so that no bulk
@@ -560,102 +641,128 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, const SplitPair *__restri
   } else if (warp == 1) {
     if (lane == 0) {
       // ------------------------------------------------ MMA issuer
-      uint32_t idesc[4];
+      // one instruction per A digit t: N = (S - t) * 32 columns of B digits
+      uint32_t idesc[S];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) idesc[j] = make_idesc(TNS * (j + 1));
-      int it = 0, chunk = 0, depth = 0;
-      bool fresh = true, ok = true;
-      for (int p = T.p0; p < T.p1 && ok; ++p) {
-        const int KB = pairs[p].KB, Kr = pairs[p].Kr;
-        for (int kb = 0; kb < KB; ++kb, ++it) {
-          const int dk = max(kblock_depth(Kr, kb), 0);
-          if (!fresh && depth + dk > kchunk) {
-            // drain: hand the accumulators to the epilogue, wait until read
-            umma_commit(acc_full);
-            if (!mbar_wait(acc_empty, (uint32_t)(chunk & 1), abort_flag, err, 2)) { ok = false; break; }
-            tc_fence_after();
-            ++chunk;
-            fresh = true;
-            depth = 0;
-          }
-          depth += dk;
-          const int st = it % nstages;
-          const uint32_t ph = (uint32_t)((it / nstages) & 1);
-          if (!mbar_wait(&full[st], ph, abort_flag, err, 3)) { ok = false; break; }
+      for (int j = 0; j < S; ++j) idesc[j] = make_idesc(TNS * (j + 1));
+      int it = 0, u = 0;  // u: accumulator uses (chunks) handed to the epilogue
+      bool ok = true;
+      // before filling set u & 1 for use u >= 2, wait until use u - 2 is read
+      auto acquire = [&](int uu) -> bool {
+        if (uu >= 2) {
+          if (!mbar_wait(&acc_empty[uu & 1], (uint32_t)(((uu >> 1) - 1) & 1), abort_flag, err, 2)) return false;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(stages + (size_t)st * STAGE_BYTES);
-          const uint32_t b0 = a0 + A_BYTES;
+        }
+        return true;
+      };
+      for (int r = 0; ok; ++r) {
+        const int ti = tile_of(r, cta, G);
+        if (ti >= ntiles) break;
+        const SplitTile &T = tiles[ti];
+        int depth = 0;
+        bool fresh = true;
+        if (!acquire(u)) { ok = false; break; }
+        for (int p = T.p0; p < T.p1 && ok; ++p) {
+          const int KB = pairs[p].KB, Kr = pairs[p].Kr;
+          for (int kb = 0; kb < KB; ++kb, ++it) {
+            const int dk = max(kblock_depth(Kr, kb), 0);
+            if (!fresh && depth + dk > kchunk) {
+              // this chunk is done: hand the set to the epilogue, go on in
+              // the other set
+              umma_commit(&acc_full[u & 1]);
+              ++u;
+              if (!acquire(u)) { ok = false; break; }
+              fresh = true;
+              depth = 0;
+            }
+            depth += dk;
+            const int st = it % nstages;
+            const uint32_t ph = (uint32_t)((it / nstages) & 1);
+            if (!mbar_wait(&full[st], ph, abort_flag, err, 3)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(stages + (size_t)st * STAGE_BYTES);
+            const uint32_t b0 = a0 + A_BYTES;
+            const uint32_t dset = tmem + (uint32_t)((u & 1) * SET_COLS);
 #pragma unroll
-          for (int ks = 0; ks < TKS / 16; ++ks) {
+            for (int ks = 0; ks < TKS / 16; ++ks) {
 #pragma unroll
-            for (int t = 0; t < S; ++t) {
-#pragma unroll
-              for (int u0 = 0; u0 < S - t; u0 += 4) {
-                const int nu = min(4, S - t - u0);
+              for (int t = 0; t < S; ++t) {
                 const uint64_t ad = make_desc(a0 + t * A_DIGIT_BYTES + ks * 256, 128, 512);
-                const uint64_t bd = make_desc(b0 + u0 * B_DIGIT_BYTES + ks * 256, 128, 512);
+                const uint64_t bd = make_desc(b0 + ks * 256, 128, 512);
                 const uint32_t acc = (fresh && ks == 0 && t == 0) ? 0u : 1u;
-                umma_bf16(tmem + (uint32_t)((t + u0) * TNS), ad, bd, idesc[nu - 1], acc);
+                umma_bf16(dset + (uint32_t)(t * TNS), ad, bd, idesc[S - 1 - t], acc);
               }
             }
+            fresh = false;
+            umma_commit(&empty[st]);
           }
-          fresh = false;
-          umma_commit(&empty[st]);
         }
+        if (!ok) break;
+        umma_commit(&acc_full[u & 1]);
+        ++u;
       }
-      umma_commit(acc_full);
-      // make sure every MMA issued has completed before TMEM is released
+      // every MMA must have completed before TMEM is released: wait until the
+      // epilogue has read the last two uses
       if (ok) {
-        // the epilogue's final acc_empty arrive follows its last TMEM read
-        mbar_wait(acc_empty, (uint32_t)(chunk & 1), abort_flag, err, 4);
+        for (int uu = max(0, u - 2); uu < u; ++uu)
+          mbar_wait(&acc_empty[uu & 1], (uint32_t)((uu >> 1) & 1), abort_flag, err, 4);
       } else {
-        for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(acc_full, (uint32_t)(chunk & 1)); ++i) {
+        umma_commit(&acc_full[u & 1]);
+        for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&acc_full[u & 1], (uint32_t)((u >> 1) & 1)); ++i) {
         }
       }
     }
   } else {
     // ------------------------------------------- epilogue (warps 2..9)
-    // warp w reads TMEM lane quarter w % 4; warps 2..5 take columns 0..31,
-    // warps 6..9 columns 32..63.
+    // warp w reads TMEM lane quarter w % 4; warps 2..5 take columns 0..15,
+    // warps 6..9 columns 16..31 of each tile.
     const int q = warp & 3;
-    const int cbase = warp < 6 ? 0 : TNS / 2;
-    const int row = q * 32 + lane;
-    const int i_glob = T.mt * TMS + row;
-    const bool rv = i_glob < T.Mr;
-    const int Ei = rv ? E[T.eoff + i_glob] : 0;
+    constexpr int CW = TNS / 2;
+    const int cbase = warp < 6 ? 0 : CW;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-    // value = V * 2^(E_i + F_j + scale0), V the fixed-point group sum
-    const int scale0 = T.rshift - b * (S + 1);
-    for (int ch = 0; ch < T.nchunk; ++ch) {
-      // one lane polls; the warp proceeds together (tcgen05.ld is .aligned)
-      int ok = 1;
-      if (lane == 0) ok = mbar_wait(acc_full, (uint32_t)(ch & 1), abort_flag, err, 5) ? 1 : 0;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
+    const int scale_b = -b * (S + 1);
+    int u = 0;
+    bool ok = true;
+    for (int r = 0; ok; ++r) {
+      const int ti = tile_of(r, cta, G);
+      if (ti >= ntiles) break;
+      const SplitTile T = tiles[ti];
+      const int i_glob = T.mt * TMS + q * 32 + lane;
+      const bool rv = i_glob < T.Mr;
+      long long V[CW];
+#pragma unroll
+      for (int jj = 0; jj < CW; ++jj) V[jj] = 0;
+      for (int ch = 0; ch < T.nchunk; ++ch, ++u) {
+        // one lane polls; the warp proceeds together (tcgen05.ld is .aligned)
+        int w = 1;
+        if (lane == 0) w = mbar_wait(&acc_full[u & 1], (uint32_t)((u >> 1) & 1), abort_flag, err, 5) ? 1 : 0;
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (!w) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t set_base = lane_base + (uint32_t)((u & 1) * SET_COLS);
+#pragma unroll
+        for (int c4 = 0; c4 < CW; c4 += 4) {
+          float acc[S][4];
+#pragma unroll
+          for (int g = 0; g < S; ++g) tmem_ld4(set_base + (uint32_t)(g * TNS + cbase + c4), acc[g]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) V[c4 + cc] += combine_groups<S, 4>(acc, cc, b, T.rshift);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[u & 1]);
+      }
       if (!ok) break;
-      tc_fence_after();
-      const bool last = ch + 1 == T.nchunk;
-#pragma unroll 1
-      for (int c0 = cbase; c0 < cbase + TNS / 2; c0 += 8) {
-        float acc[S][8];
+      if (rv) {
+        const int Ei = E[T.eoff + i_glob];
+        double *crow = C + T.c_off + (int64_t)i_glob;
 #pragma unroll
-        for (int g = 0; g < S; ++g) tmem_ld8(lane_base + (uint32_t)(g * TNS + c0), acc[g]);
-        tmem_wait_ld();
-#pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-          const int j = T.nt * TNS + c0 + cc;
-          if (!rv || j >= T.N) continue;
-          long long V = combine_groups<S>(acc, cc, b, T.rshift);
-          double *dst = C + T.c_off + (int64_t)i_glob + (int64_t)j * T.ldc;
-          // earlier chunks of this tile left their exact partial sums as
-          // int64 in the output slot
-          if (ch > 0) V += *reinterpret_cast<const long long *>(dst);
-          if (last) *dst = fixed_to_double(V, Ei + F[T.foff + j] + scale0);
-          else *reinterpret_cast<long long *>(dst) = V;
+        for (int jj = 0; jj < CW; ++jj) {
+          const int j = T.nt * TNS + cbase + jj;
+          if (j < T.N) crow[(int64_t)j * T.ldc] = fixed_to_double(V[jj], Ei + F[T.foff + j] + T.rshift + scale_b);
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty);
     }
   }
 
@@ -681,7 +788,8 @@ int pick_stages() {
 
 template <int S>
 void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d_rt, int nrt,
-                    const int2 *d_ct, int nct, const int4 *d_at, int nat, const int4 *d_bt, int nbt,
+                    const int2 *d_ct, int nct, const int4 *d_xt, int nxt, const int4 *d_at, int nat,
+                    const int4 *d_bt, int nbt,
                     const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
                     int *dE, int64_t nE, int *dF, int64_t nF, uint8_t *arena, int b, int kchunk) {
   cudaStream_t st = ctx->stream;
@@ -694,19 +802,23 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
   if (cplx) {
     if (nrt) { exp_rows_kernel<true><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, dE); QS_LAUNCHED(ctx); }
     if (nct) { exp_cols_kernel<true><<<nct, 256, 0, st>>>(d_pairs, d_ct, B, dF); QS_LAUNCHED(ctx); }
+    if (nxt) { exp_contig_kernel<true><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
     if (nat) { slice_a_kernel<true, S><<<nat, 256, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<true, S><<<nbt, 256, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nbt) { slice_b_kernel<true, S><<<nbt, 128, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
   } else {
     if (nrt) { exp_rows_kernel<false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, dE); QS_LAUNCHED(ctx); }
     if (nct) { exp_cols_kernel<false><<<nct, 256, 0, st>>>(d_pairs, d_ct, B, dF); QS_LAUNCHED(ctx); }
+    if (nxt) { exp_contig_kernel<false><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
     if (nat) { slice_a_kernel<false, S><<<nat, 256, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<false, S><<<nbt, 256, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nbt) { slice_b_kernel<false, S><<<nbt, 128, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
   }
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);
   QS_CUDA(cudaFuncSetAttribute(gemm_split_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   ctx->mark(1);
-  gemm_split_kernel<S><<<ntiles, 320, sm, st>>>(d_tiles, d_pairs, arena, dE, dF, C, b, nst, kchunk, ctx->d_err);
+  const int grid = std::min(ntiles, std::max(ctx->num_sms, 1));
+  gemm_split_kernel<S><<<grid, 320, sm, st>>>(d_tiles, ntiles, d_pairs, arena, dE, dF, C, b, nst, kchunk,
+                                              ctx->d_err);
   QS_LAUNCHED(ctx);
   ctx->mark(2);
 }
@@ -744,8 +856,13 @@ static int chunks_of(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1,
 // Digit plan: the (bits, digits) pair that reaches the wanted precision at
 // the lowest modelled cost over the actual tiles -- tensor work grows as
 // S(S+1)/2 per K block, and each accumulator drain costs about as much as
-// DRAIN_UNITS single-digit K blocks.
-constexpr double DRAIN_UNITS = 50.0;
+// DRAIN_UNITS single-digit K blocks (small: with two accumulator sets the
+// drain overlaps the next chunk's products).  QS_SPLIT_DRAIN_UNITS and
+// QS_SPLIT_BITS override the model for tuning.
+static double drain_units() {
+  const char *e = std::getenv("QS_SPLIT_DRAIN_UNITS");
+  return e ? std::atof(e) : 12.0;
+}
 
 DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                             const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
@@ -757,7 +874,10 @@ DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vecto
   DigitPlan best{0, 0, 0};
   double best_cost = 1e300;
   const int64_t nb = (int64_t)blk_M.size();
-  for (int b = 8; b >= 5; --b) {
+  const double DRAIN_UNITS = drain_units();
+  const char *fb = std::getenv("QS_SPLIT_BITS");
+  const int bhi = fb ? std::atoi(fb) : 8, blo = fb ? std::atoi(fb) : 5;
+  for (int b = bhi; b >= blo; --b) {
     int S = forced_slices > 0 ? forced_slices : (need - 1 + b - 1) / b;
     S = std::max(S, 2);
     if (S > 8) continue;
@@ -816,6 +936,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   if (nE > INT32_MAX || nF > INT32_MAX) fail(QS_ERR_SHAPE, "split: exponent arrays too large");
   int64_t arena = 0;
   std::vector<int2> rt, ct;
+  std::vector<int4> xt;
   std::vector<int4> at, bt;
   std::vector<SplitTile> tiles;
   for (int64_t g = 0; g < nb; ++g) {
@@ -850,8 +971,17 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
       arena += (int64_t)s.MT * s.KB * S * A_DIGIT_BYTES;
       s.bs_off = arena;
       arena += (int64_t)s.NT * s.KB * S * B_DIGIT_BYTES;
-      for (int m0 = 0; m0 < d.M; m0 += 256) rt.push_back(make_int2((int)p, m0));
-      for (int n0 = 0; n0 < d.N; n0 += 256) ct.push_back(make_int2((int)p, n0));
+      // exponent tasks: lines contiguous along k get a warp each (coalesced),
+      // strided lines a thread each (neighbouring lanes read neighbouring
+      // elements)
+      if (d.trans & 1)
+        for (int m0 = 0; m0 < d.M; m0 += 8) xt.push_back(make_int4((int)p, m0, 0, 0));
+      else
+        for (int m0 = 0; m0 < d.M; m0 += 256) rt.push_back(make_int2((int)p, m0));
+      if (d.trans & 2)
+        for (int n0 = 0; n0 < d.N; n0 += 256) ct.push_back(make_int2((int)p, n0));
+      else
+        for (int n0 = 0; n0 < d.N; n0 += 8) xt.push_back(make_int4((int)p, n0, 1, 0));
       for (int mt = 0; mt < s.MT; ++mt)
         for (int kb = 0; kb < s.KB; ++kb) at.push_back(make_int4((int)p, mt, kb, 0));
       for (int nt = 0; nt < s.NT; ++nt)
@@ -900,6 +1030,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   SplitPair *d_pairs = dev_upload(ctx, sp);
   int2 *d_rt = dev_upload(ctx, rt);
   int2 *d_ct = dev_upload(ctx, ct);
+  int4 *d_xt = dev_upload(ctx, xt);
   int4 *d_at = dev_upload(ctx, at);
   int4 *d_bt = dev_upload(ctx, bt);
   SplitTile *d_tiles = dev_upload(ctx, tiles);
@@ -908,7 +1039,8 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   switch (S) {
 #define QS_CASE(SS)                                                                                      \
   case SS:                                                                                               \
-    launch_split_s<SS>(ctx, cplx, d_pairs, d_rt, (int)rt.size(), d_ct, (int)ct.size(), d_at, (int)at.size(), \
+    launch_split_s<SS>(ctx, cplx, d_pairs, d_rt, (int)rt.size(), d_ct, (int)ct.size(), d_xt, (int)xt.size(), \
+                       d_at, (int)at.size(),                                                             \
                        d_bt, (int)bt.size(), d_tiles, (int)tiles.size(), A, B, C, dE, nE, dF, nF, d_arena, b, \
                        kchunk);                                                                          \
     break;
@@ -926,6 +1058,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   dev_free(ctx, d_pairs);
   dev_free(ctx, d_rt);
   dev_free(ctx, d_ct);
+  dev_free(ctx, d_xt);
   dev_free(ctx, d_at);
   dev_free(ctx, d_bt);
   dev_free(ctx, d_tiles);

@@ -1,0 +1,147 @@
+"""Block eigendecomposition / SVD / Gram-Schmidt through the C-ABI.
+
+* ``eigQS(H, Nkeep=, Etrunc=, deps=)`` mirrors the abelian use of the MEX
+  ``eigQS`` (Source/eigQS.cc:27-122 -> QSpace::EigenSymmetric,
+  Source/QSpace.cc:4673-4939): every symmetry block of a block-diagonal
+  rank-2 QSpace is diagonalised on the GPU in FP64, the global truncation
+  (markSet) keeps the Nkeep lowest levels, and the kept / discarded
+  eigenvectors come back as QSpaces AK / AD with eigenvalues EK / ED.
+* ``eig_blocks``, ``svd_blocks``, ``gs_reortho``: the raw block operations on
+  device buffers (torch tensors used as plain device memory).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import check
+from .qspace import Context, QSpace, default_context
+
+c_i64 = _capi.c_int64_p
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(c_i64)
+
+
+def eig_blocks(blocks: list, ctx: Context | None = None):
+    """Eigen-decomposition of a list of Hermitian matrices on the GPU.
+    Returns (list of ascending eigenvalue arrays, list of eigenvector
+    matrices)."""
+    import torch
+    ctx = ctx or default_context()
+    cplx = any(np.iscomplexobj(b) for b in blocks)
+    dt = np.complex128 if cplx else np.float64
+    n = np.array([b.shape[0] for b in blocks], np.int64)
+    sizes = n * n
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    eoffs = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+    H = np.concatenate([np.asarray(b, dt).reshape(-1, order="F") for b in blocks]) if blocks else np.zeros(0, dt)
+    dev = torch.device("cuda", ctx.device)
+    dH = torch.from_numpy(H.view(np.float64)).to(dev)
+    dU = torch.empty_like(dH)
+    dE = torch.empty(max(int(n.sum()), 1), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    check(ctx.lib.qs_eig_blocks(ctx.h, len(blocks), _ptr(n), _ptr(offs), _ptr(eoffs), C.c_void_p(dH.data_ptr()),
+                                C.c_void_p(dE.data_ptr()), C.c_void_p(dU.data_ptr()), 1 if cplx else 0))
+    ctx.sync()
+    E = dE.cpu().numpy()
+    U = dU.cpu().numpy()
+    if cplx:
+        U = U.view(np.complex128)
+    Es = [E[eoffs[i]:eoffs[i] + n[i]].copy() for i in range(len(blocks))]
+    Us = [U[offs[i]:offs[i] + sizes[i]].reshape((n[i], n[i]), order="F").copy() for i in range(len(blocks))]
+    return Es, Us
+
+
+def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0):
+    """Global truncation (markSet) on the host through the C-ABI."""
+    lib = _capi.load()
+    n = np.array([len(e) for e in E_blocks], np.int64)
+    E = np.concatenate([np.asarray(e, np.float64) for e in E_blocks]) if E_blocks else np.zeros(0)
+    keep = np.zeros(max(len(E), 1), np.uint8)
+    nk, et = C.c_int64(), C.c_double()
+    check(lib.qs_mark_keep(len(n), _ptr(n), E.ctypes.data_as(_capi.c_double_p), None, int(nkeep), float(etrunc),
+                           float(deps), keep.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(nk), C.byref(et)))
+    offs = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+    return [keep[o:o + k].astype(bool) for o, k in zip(offs, n)], nk.value, et.value
+
+
+def eigQS(H: QSpace, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0, ctx: Context | None = None):
+    """Block eigendecomposition + truncation of a block-diagonal rank-2
+    abelian QSpace.  Returns (Etot, I) with Etot the ascending eigenvalues of
+    all blocks and I = {'AK','AD','EK','ED','NK'} as in eigQS."""
+    if H.rank != 2:
+        raise ValueError("eigQS: rank-2 QSpace required")
+    for i in range(H.nblk):
+        if not np.array_equal(H.Q[0][i], H.Q[1][i]):
+            raise ValueError("eigQS: block-diagonal (symmetric) QSpace required")
+    blocks = [np.asarray(d).reshape(H.block_dims(i)) for i, d in enumerate(H.data)]
+    Es, Us = eig_blocks(blocks, ctx)
+    keep, nk, _ = mark_keep(Es, Nkeep, Etrunc, deps)
+    parts = {}
+    for tag, sel in (("K", True), ("D", False)):
+        Q0, Q1, data, EQ, Ed = [], [], [], [], []
+        for i, (e, u, k) in enumerate(zip(Es, Us, keep)):
+            idx = np.flatnonzero(k == sel)
+            if idx.size == 0:
+                continue
+            Q0.append(H.Q[0][i])
+            Q1.append(H.Q[1][i])
+            data.append(u[:, idx])
+            Ed.append(np.diag(e[idx]))
+        if data:
+            parts["A" + tag] = QSpace([np.asarray(Q0), np.asarray(Q1)], data, dict(H.info))
+            parts["E" + tag] = QSpace([np.asarray(Q0), np.asarray(Q1)], Ed, {})
+        else:
+            parts["A" + tag] = QSpace([], [], {})
+            parts["E" + tag] = QSpace([], [], {})
+    parts["NK"] = nk
+    Etot = np.sort(np.concatenate(Es)) if Es else np.zeros(0)
+    return Etot, parts
+
+
+def svd_blocks(blocks: list, ctx: Context | None = None):
+    """Thin SVD of real blocks on the GPU: returns lists U, S, Vt."""
+    import torch
+    ctx = ctx or default_context()
+    m = np.array([b.shape[0] for b in blocks], np.int64)
+    n = np.array([b.shape[1] for b in blocks], np.int64)
+    k = np.minimum(m, n)
+    cum = lambda x: np.concatenate([[0], np.cumsum(x)[:-1]]).astype(np.int64)
+    offs, uoffs, soffs, voffs = cum(m * n), cum(m * k), cum(k), cum(k * n)
+    A = np.concatenate([np.asarray(b, np.float64).reshape(-1, order="F") for b in blocks])
+    dev = torch.device("cuda", ctx.device)
+    dA = torch.from_numpy(A).to(dev)
+    dU = torch.zeros(max(int((m * k).sum()), 1), dtype=torch.float64, device=dev)
+    dS = torch.zeros(max(int(k.sum()), 1), dtype=torch.float64, device=dev)
+    dV = torch.zeros(max(int((k * n).sum()), 1), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    check(ctx.lib.qs_svd_blocks(ctx.h, len(blocks), _ptr(m), _ptr(n), _ptr(offs), _ptr(uoffs), _ptr(soffs),
+                                _ptr(voffs), C.c_void_p(dA.data_ptr()), C.c_void_p(dU.data_ptr()),
+                                C.c_void_p(dS.data_ptr()), C.c_void_p(dV.data_ptr())))
+    ctx.sync()
+    U, S, V = dU.cpu().numpy(), dS.cpu().numpy(), dV.cpu().numpy()
+    Us = [U[uoffs[i]:uoffs[i] + m[i] * k[i]].reshape((m[i], k[i]), order="F") for i in range(len(blocks))]
+    Ss = [S[soffs[i]:soffs[i] + k[i]] for i in range(len(blocks))]
+    Vs = [V[voffs[i]:voffs[i] + k[i] * n[i]].reshape((k[i], n[i]), order="F") for i in range(len(blocks))]
+    return Us, Ss, Vs
+
+
+def gs_reortho(V: np.ndarray, v: np.ndarray, ctx: Context | None = None):
+    """Double classical Gram-Schmidt of v against the orthonormal columns of
+    V on the GPU, then normalisation.  Returns (v_new, |v| before)."""
+    import torch
+    ctx = ctx or default_context()
+    dev = torch.device("cuda", ctx.device)
+    n, nv = V.shape
+    dV = torch.from_numpy(np.asfortranarray(V, np.float64).reshape(-1, order="F")).to(dev)
+    dv = torch.from_numpy(np.asarray(v, np.float64).copy()).to(dev)
+    torch.cuda.synchronize(dev)
+    nrm = C.c_double()
+    check(ctx.lib.qs_gs_reortho(ctx.h, n, nv, C.c_void_p(dV.data_ptr()), C.c_void_p(dv.data_ptr()),
+                                C.byref(nrm)))
+    ctx.sync()
+    return dv.cpu().numpy(), nrm.value

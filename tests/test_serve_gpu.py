@@ -1,0 +1,66 @@
+"""Serving loop: every result is the same alone and in the mix (bit
+identical: deterministic kernels); admission by HBM footprint; host-side
+failure injection (bad request, refused admission, cancellation)."""
+import numpy as np
+import pytest
+
+from qspace_gb300 import contract_dev, upload
+from qspace_gb300._capi import QSError
+from qspace_gb300.serve import Server
+from qspace_gb300.workloads import mps_site_tensor
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(a, b):
+    A, B = a.download(), b.download()
+    assert A.nblk == B.nblk
+    for qa, qb in zip(A.Q, B.Q):
+        assert np.array_equal(qa, qb)
+    for x, y in zip(A.data, B.data):
+        assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
+def test_results_identical_alone_and_in_the_mix(ctx):
+    tensors = [upload(mps_site_tensor(s), ctx) for s in range(6)]
+    jobs = []
+    for i, t in enumerate(tensors):
+        for prec in ("fp64", "split"):
+            jobs.append((t, "12*", t, "12", prec))
+    alone = [contract_dev(a, ia, b, ib, prec=p) for (a, ia, b, ib, p) in jobs]
+    with Server(nslots=4, hbm_budget=1 << 30, ctx=ctx) as srv:
+        tickets = [srv.submit(a, ia, b, ib, prec=p) for (a, ia, b, ib, p) in jobs * 3]
+        lat = []
+        for k, t in enumerate(tickets):
+            T, ms = srv.wait(t)
+            lat.append(ms)
+            _same(T, alone[k % len(jobs)])
+        assert len(lat) == len(tickets) and min(lat) > 0
+
+
+def test_admission_refused_and_bad_request(ctx):
+    A = upload(mps_site_tensor(0), ctx)
+    with Server(nslots=2, hbm_budget=1024, ctx=ctx) as srv:
+        with pytest.raises(QSError) as e:
+            srv.submit(A, "12*", A, "12")
+        assert e.value.code == 5  # QS_ERR_OOM: admission refused
+    with Server(nslots=2, hbm_budget=1 << 30, ctx=ctx) as srv:
+        with pytest.raises(QSError) as e:
+            srv.submit(A, "1,1", A, "12")
+        assert e.value.code == 1
+        # contracted dims differ: refused when the request is planned
+        with pytest.raises(QSError) as e:
+            srv.submit(A, "1", A, "2")
+        assert e.value.code == 2
+
+
+def test_cancel_queued_request(ctx):
+    A = upload(mps_site_tensor(4), ctx)
+    with Server(nslots=1, hbm_budget=1 << 30, ctx=ctx) as srv:
+        tickets = [srv.submit(A, "12*", A, "12", prec="split") for _ in range(40)]
+        srv.cancel(tickets[-1])
+        with pytest.raises(QSError) as e:
+            srv.wait(tickets[-1])
+        assert e.value.code == 9
+        for t in tickets[:-1]:
+            srv.wait(t)
