@@ -80,6 +80,8 @@ typedef struct {
                              complex elements)                                 */
   const double *data;     /* blocks, column-major, back to back                */
   int32_t is_complex;     /* 0: float64, 1: complex128 interleaved             */
+  const char *itags;      /* leg tags "L,s,R*" (a trailing '*' marks an
+                             outgoing leg), or NULL: info.itags of the struct */
 } qs_qspace_view;
 
 typedef struct {
@@ -144,6 +146,9 @@ QS_EXPORT qs_status qs_result_info(const qs_result *C, int32_t *rank, int32_t *q
                          int64_t *nblk, int64_t *nelem, int32_t *is_complex);
 /* Copies labels (nblk*rank*qdim), dims (nblk*rank), offsets (nblk) and data
  * (nelem, x2 doubles when complex) into caller buffers; any may be NULL. */
+/* Leg tags of the result as "a,b*,c" into buf (len bytes, NUL-terminated);
+ * empty when the operands had none. */
+QS_EXPORT qs_status qs_result_itags(const qs_result *C, char *buf, size_t len);
 QS_EXPORT qs_status qs_result_copy(const qs_result *C, int32_t *q, int64_t *dims,
                          int64_t *offs, double *data);
 QS_EXPORT void qs_result_free(qs_result *C);
@@ -156,6 +161,7 @@ QS_EXPORT qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t 
                              int64_t *dims, int64_t *offs, double *data);
 /* Device pointer of the block data (for callers that keep data on device). */
 QS_EXPORT const double *qs_tensor_data(const qs_tensor *T);
+QS_EXPORT qs_status qs_tensor_itags(const qs_tensor *T, char *buf, size_t len);
 QS_EXPORT void qs_tensor_free(qs_tensor *T);
 /* Same contraction as qs_contractQS with device-resident operands and result. */
 QS_EXPORT qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char *ia,

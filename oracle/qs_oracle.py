@@ -276,6 +276,11 @@ def contract(A: dict, ia, B: dict, ib, perm=None, return_plan: bool = False):
     ica, conja = parse_ctr_idx(ia)
     icb, conjb = parse_ctr_idx(ib)
     ra, rb = rank_of(A), rank_of(B)
+    # conjugation / itag sequence of QSpace::contract (see _conj_sequence)
+    ica_s, icb_s = _co_sort(A, ica, B, icb)
+    A, conja = _conj_sequence_operand(A, ica_s, conja, front_first=True)
+    B, conjb = _conj_sequence_operand(B, icb_s, conjb, front_first=False)
+    conja = _itag_conj_rule(A, ica_s, conja, B, icb_s, conjb)
     if nblk_of(A) == 0 or nblk_of(B) == 0:
         return _empty_like(0)
     qdA = np.asarray(A["Q"][0]).reshape(nblk_of(A), -1).shape[1]
@@ -291,12 +296,24 @@ def contract(A: dict, ia, B: dict, ib, perm=None, return_plan: bool = False):
     ikb = [k for k in range(rb) if k not in icb]
     rc = len(ika) + len(ikb)
     P = _parse_perm(perm, rc)
+    info = {}
+    it_a = (A.get("info") or {}).get("itags")
+    it_b = (B.get("info") or {}).get("itags")
+    if it_a and it_b:
+        def cj(t, c):
+            if not c:
+                return t
+            return t[:-1] if t.endswith("*") else t + "*"
+        tags = [cj(it_a[k], conja) for k in ika] + [cj(it_b[k], conjb) for k in ikb]
+        if P is not None:
+            tags = [tags[P[k]] for k in range(rc)]
+        info["itags"] = tags
 
     QAc, QAk = qrows(A, ica), qrows(A, ika)
     QBc, QBk = qrows(B, icb), qrows(B, ikb)
     Ia, Ib = _match_index(QAc, QBc)
     if len(Ia) == 0:
-        return _empty_like(rc)
+        return {"Q": [], "data": [], "info": info}
     QC = np.concatenate([QAk[Ia], QBk[Ib]], axis=1)
     if rc:
         p = lexsort_rows(QC)
@@ -336,22 +353,51 @@ def contract(A: dict, ia, B: dict, ib, perm=None, return_plan: bool = False):
         out_data = [np.transpose(d.reshape(d.shape + (1,) * (rc - d.ndim)), P)
                     for d in out_data]
     Qout, out_data = skip_zero_blocks(Qout, out_data)
-    info = {}
-    it_a = (A.get("info") or {}).get("itags")
-    it_b = (B.get("info") or {}).get("itags")
-    if it_a and it_b:
-        def cj(t, c):
-            if not c:
-                return t
-            return t[:-1] if t.endswith("*") else t + "*"
-        tags = [cj(it_a[k], conja) for k in ika] + [cj(it_b[k], conjb) for k in ikb]
-        if P is not None:
-            tags = [tags[P[k]] for k in range(rc)]
-        info["itags"] = tags
     C = {"Q": Qout, "data": out_data, "info": info}
     if return_plan:
         return C, {"ica": ica, "icb": icb, "pairs": pairs}
     return C
+
+
+def _conj_sequence_operand(X: dict, ic: list, conj: bool, front_first: bool):
+    """permute_to (Source/QSpace.hh:2824-2866): an operand whose contracted
+    legs are neither leading nor trailing in pairing order is permuted; its
+    conjugation flag goes into that permutation, which conjugates the data
+    and the itags, and the flag is cleared.  Returns (operand, conj flag)."""
+    r, n = rank_of(X), len(ic)
+    in_place = ic == list(range(n)) or ic == list(range(r - n, r))
+    if in_place or not conj:
+        return X, conj
+    Y = dict(X)
+    Y["data"] = [np.conj(np.asarray(d)) for d in X["data"]]
+    tags = (X.get("info") or {}).get("itags")
+    if tags:
+        Y["info"] = dict(X.get("info") or {})
+        Y["info"]["itags"] = [t[:-1] if t.endswith("*") else t + "*" for t in tags]
+    return Y, False
+
+
+def _itag_conj_rule(A, ica, conja, B, icb, conjb) -> bool:
+    """itag check of contract_getIdxSet (Source/QSpace.cc:4230-4271) with
+    itag_::sameAs (Source/wbindex.cc:989-1005): contracted legs must carry
+    the same name, all with the same relative direction; if all point the
+    same way and the conj flags do not differ, A is conjugated."""
+    ta = (A.get("info") or {}).get("itags")
+    tb = (B.get("info") or {}).get("itags")
+    if not ta or not tb:
+        return conja
+    zflag = 0
+    for a, b in zip(ica, icb):
+        na, nb = ta[a].rstrip("*"), tb[b].rstrip("*")
+        if na != nb and na and nb:
+            raise ValueError(f"itag mismatch {ta[a]} <> {tb[b]}")
+        q = 1 if ta[a].endswith("*") == tb[b].endswith("*") else -1
+        if zflag and q != zflag:
+            raise ValueError("itag mismatch (mixed directions)")
+        zflag = zflag or q
+    if zflag > 0 and conja == conjb:
+        return not conja
+    return conja
 
 
 def _empty_like(rc: int) -> dict:

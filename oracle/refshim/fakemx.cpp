@@ -403,7 +403,15 @@ int mexPrintf(const char *fmt, ...) {
   return n;
 }
 const char *mexFunctionName(void) { return g_name.c_str(); }
-int mexCallMATLAB(int, mxArray *[], int, mxArray *[], const char *) { return 1; }
+// Only the environment probes the MEX files make at start-up are answered
+// (isdeployed / usejava -> false); anything else reports failure.
+int mexCallMATLAB(int nlhs, mxArray *plhs[], int, mxArray *[], const char *name) {
+  if (name && (!std::strcmp(name, "isdeployed") || !std::strcmp(name, "usejava"))) {
+    if (nlhs > 0 && plhs) plhs[0] = mxCreateLogicalScalar(false);
+    return 0;
+  }
+  return 1;
+}
 int mexEvalString(const char *) { return 0; }
 const mxArray *mexGetVariablePtr(const char *, const char *) { return nullptr; }
 mxArray *mexGetVariable(const char *, const char *) { return nullptr; }
@@ -423,6 +431,24 @@ int matDeleteVariable(MATFile *, const char *) { return 0; }
 
 // ----------------------------------------------------------- driver entry
 typedef void (*mexfn_t)(int, mxArray *[], int, const mxArray *[]);
+
+// Debugging aid (FAKEMX_BACKTRACE=1): print a backtrace on SIGSEGV.
+}
+#include <execinfo.h>
+#include <signal.h>
+#include <unistd.h>
+static void fakemx_segv(int) {
+  void *bt[64];
+  int n = backtrace(bt, 64);
+  backtrace_symbols_fd(bt, n, 2);
+  _exit(139);
+}
+static struct FakemxInit {
+  FakemxInit() {
+    if (std::getenv("FAKEMX_BACKTRACE")) signal(SIGSEGV, fakemx_segv);
+  }
+} fakemx_init;
+extern "C" {
 
 // Runs one MEX call; returns 0 on success, 1 when the MEX raised an error
 // (message in fakemx_last_error()).

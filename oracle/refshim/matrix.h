@@ -3,9 +3,13 @@
  * project's fake runtime (fakemx.cpp).  Test infrastructure only. */
 #ifndef FAKEMX_MATRIX_H
 #define FAKEMX_MATRIX_H
+#include <float.h>
+#include <stdbool.h>
 #include <stddef.h>
 #include <stdint.h>
-#include <stdbool.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
 
 typedef size_t mwSize;
 typedef size_t mwIndex;

@@ -21,7 +21,7 @@ c_double_p = C.POINTER(C.c_double)
 class QSpaceView(C.Structure):
     _fields_ = [("rank", C.c_int32), ("qdim", C.c_int32), ("nblk", C.c_int64),
                 ("q", c_int32_p), ("dims", c_int64_p), ("offs", c_int64_p),
-                ("data", c_double_p), ("is_complex", C.c_int32)]
+                ("data", c_double_p), ("is_complex", C.c_int32), ("itags", C.c_char_p)]
 
 
 class Opts(C.Structure):
@@ -83,6 +83,8 @@ SIGNATURES = {
     "qs_result_info": (C.c_int, [C.c_void_p, c_int32_p, c_int32_p, c_int64_p, c_int64_p, c_int32_p]),
     "qs_result_copy": (C.c_int, [C.c_void_p, c_int32_p, c_int64_p, c_int64_p, c_double_p]),
     "qs_result_free": (_V, [C.c_void_p]),
+    "qs_result_itags": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "qs_tensor_itags": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "qs_tensor_upload": (C.c_int, [C.c_void_p, C.POINTER(QSpaceView), C.POINTER(C.c_void_p)]),
     "qs_tensor_info": (C.c_int, [C.c_void_p, c_int32_p, c_int32_p, c_int64_p, c_int64_p, c_int32_p]),
     "qs_tensor_download": (C.c_int, [C.c_void_p, C.c_void_p, c_int32_p, c_int64_p, c_int64_p,

@@ -140,7 +140,12 @@ std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double
     stats->bytes = pl.bytes;
     stats->npairs = (int64_t)pl.pairs.size();
   }
-  if (pl.C.nblk == 0) return empty_tensor(ctx, 0, Am.qdim, cplx);
+  if (pl.C.nblk == 0) {
+    // no matching sectors: an empty QSpace that still carries the itags
+    auto T = empty_tensor(ctx, 0, Am.qdim, cplx);
+    for (int k = 0; k < (int)pl.C.itags.size(); ++k) T->meta.itags.push_back(pl.C.itags[pl.P.empty() ? k : pl.P[k]]);
+    return T;
+  }
   const int es = cplx ? 2 : 1;
 
   // Operands in the element type of the result, in the layout the plan wants.
@@ -156,7 +161,7 @@ std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double
     if (lay.permute) {
       double *o = dev_alloc<double>(ctx, (size_t)m.nelem * es);
       tmp.push_back(o);
-      std::vector<PermDesc> pd = make_perm_descs(m, lay.perm, false, m.offs);
+      std::vector<PermDesc> pd = make_perm_descs(m, lay.perm, lay.conj, m.offs);
       run_permute(ctx, pd, cur, o, cplx);
       cur = o;
     }
@@ -226,6 +231,12 @@ std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double
   QMeta &M = T->meta;
   M.rank = pl.rc;
   M.qdim = pl.C.qdim;
+  // output itags, permuted like the legs (QSpace::Permute)
+  if (!pl.C.itags.empty()) {
+    if (pl.P.empty()) M.itags = pl.C.itags;
+    else
+      for (int k = 0; k < pl.rc; ++k) M.itags.push_back(pl.C.itags[pl.P[k]]);
+  }
   M.cplx = cplx;
   M.nblk = (int64_t)keep.size();
   const int r = pl.rc, qd = pl.C.qdim;
@@ -473,6 +484,27 @@ qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q, int64_
 
 const double *qs_tensor_data(const qs_tensor *T) { return T ? T->d : nullptr; }
 
+static void copy_tags(const std::vector<std::string> &t, char *buf, size_t len) {
+  if (!buf || !len) fail(QS_ERR_ARG, "null buffer");
+  const std::string s = join_itags(t);
+  if (s.size() + 1 > len) fail(QS_ERR_ARG, "itag buffer too small (%zu bytes needed)", s.size() + 1);
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+}
+
+qs_status qs_tensor_itags(const qs_tensor *T, char *buf, size_t len) {
+  QS_API_BEGIN
+  if (!T) fail(QS_ERR_ARG, "null tensor");
+  copy_tags(T->meta.itags, buf, len);
+  QS_API_END
+}
+
+qs_status qs_result_itags(const qs_result *C, char *buf, size_t len) {
+  QS_API_BEGIN
+  if (!C) fail(QS_ERR_ARG, "null result");
+  copy_tags(C->meta.itags, buf, len);
+  QS_API_END
+}
+
 void qs_tensor_free(qs_tensor *T) { delete T; }
 
 qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char *ia, const qs_tensor *B,
@@ -496,6 +528,12 @@ static std::unique_ptr<qs_tensor> permute_core(Ctx *ctx, const QMeta &m, const d
   M.qdim = m.qdim;
   M.nblk = m.nblk;
   M.cplx = m.cplx;
+  // itags follow the legs; 'conj' flips them as it conjugates the data
+  // (QSpace::permute / Conj, Source/QSpace.hh:2670-2790, 1372-1380)
+  for (int k = 0; k < (int)m.itags.size() && !m.itags.empty(); ++k) {
+    const std::string &t = m.itags[P.empty() ? k : P[k]];
+    M.itags.push_back(conj ? conj_itag(t) : t);
+  }
   const int r = m.rank, qd = m.qdim;
   int64_t ne = 0;
   for (int64_t i = 0; i < m.nblk; ++i) {

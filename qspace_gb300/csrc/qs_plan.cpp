@@ -69,7 +69,38 @@ QMeta meta_from_view(const qs_qspace_view *v) {
   m.nelem = ext;
   m.check("QSpace");
   if (m.nblk && !v->data && ext > 0) fail(QS_ERR_ARG, "null data pointer");
+  m.itags = parse_itags(v->itags);
+  if (!m.itags.empty() && (int)m.itags.size() != m.rank)
+    fail(QS_ERR_LABEL, "invalid number of itags (%zu/%d)", m.itags.size(), m.rank);
   return m;
+}
+
+std::vector<std::string> parse_itags(const char *s) {
+  std::vector<std::string> t;
+  if (!s || !*s) return t;
+  std::string cur;
+  for (const char *p = s;; ++p) {
+    if (*p == ',' || *p == 0) {
+      size_t a = cur.find_first_not_of(' '), b = cur.find_last_not_of(' ');
+      t.push_back(a == std::string::npos ? std::string() : cur.substr(a, b - a + 1));
+      cur.clear();
+      if (*p == 0) break;
+    } else {
+      cur.push_back(*p);
+    }
+  }
+  return t;
+}
+
+std::string join_itags(const std::vector<std::string> &t) {
+  std::string s;
+  for (size_t i = 0; i < t.size(); ++i) s += (i ? "," : "") + t[i];
+  return s;
+}
+
+std::string conj_itag(const std::string &t) {
+  if (!t.empty() && t.back() == '*') return t.substr(0, t.size() - 1);
+  return t + "*";
 }
 
 // ------------------------------------------------------------ index strings
@@ -236,6 +267,44 @@ ContractPlan plan_contract(const QMeta &A, const char *ia, const QMeta &B,
     pl.lb.perm = pl.icb.idx;
     pl.lb.perm.insert(pl.lb.perm.end(), pl.ikb.begin(), pl.ikb.end());
     pl.lb.ctr_front = true;
+  }
+
+  // A permuted operand takes its conjugation into the permutation
+  // (permute_to, Source/QSpace.hh:2855-2858, then QSpace::permute): the
+  // permuted copy holds the conjugated data and conjugated itags, and the
+  // flag itself is cleared.
+  std::vector<std::string> tagA = A.itags, tagB = B.itags;
+  if (pl.la.permute && pl.ica.conj) {
+    pl.la.conj = A.cplx;
+    for (auto &t : tagA) t = conj_itag(t);
+    pl.ica.conj = false;
+  }
+  if (pl.lb.permute && pl.icb.conj) {
+    pl.lb.conj = B.cplx;
+    for (auto &t : tagB) t = conj_itag(t);
+    pl.icb.conj = false;
+  }
+
+  // itags (contract_getIdxSet, Source/QSpace.cc:4230-4271, with
+  // itag_::sameAs, Source/wbindex.cc:989-1005): contracted legs carry the
+  // same name (an empty tag matches leniently) and all pairs agree on the
+  // relative direction; if all point the same way and the conjugation flags
+  // do not differ, A's flag is toggled (the reference warns).
+  if (!tagA.empty() && !tagB.empty()) {
+    int zflag = 0;
+    for (int i = 0; i < nc; ++i) {
+      const std::string &ta = tagA[pl.ica.idx[i]], &tb = tagB[pl.icb.idx[i]];
+      const bool ca = !ta.empty() && ta.back() == '*', cb = !tb.empty() && tb.back() == '*';
+      const std::string na = ca ? ta.substr(0, ta.size() - 1) : ta, nb = cb ? tb.substr(0, tb.size() - 1) : tb;
+      int q = (na == nb || na.empty() || nb.empty()) ? 1 : 0;
+      if (q && ca != cb) q = -1;
+      if (zflag && q != zflag) q = 0;
+      if (!zflag) zflag = q;
+      if (!q) fail(QS_ERR_LABEL, "contract() itag mismatch %s <> %s @ i=%d", ta.c_str(), tb.c_str(), i + 1);
+    }
+    if (zflag > 0 && pl.ica.conj == pl.icb.conj) pl.ica.conj = !pl.ica.conj;
+    for (int k : pl.ika) pl.C.itags.push_back(pl.ica.conj ? conj_itag(tagA[k]) : tagA[k]);
+    for (int k : pl.ikb) pl.C.itags.push_back(pl.icb.conj ? conj_itag(tagB[k]) : tagB[k]);
   }
 
   pl.C.rank = pl.rc;

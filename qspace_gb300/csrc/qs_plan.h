@@ -20,6 +20,7 @@ struct QMeta {
   std::vector<int64_t> offs;  // nblk
   int64_t nelem = 0;          // extent of the data arena (elements)
   bool cplx = false;
+  std::vector<std::string> itags;  // leg tags ("L", "R*"), empty: none
 
   const int32_t *qrow(int64_t i) const { return q.data() + i * rank * qdim; }
   const int64_t *drow(int64_t i) const { return dims.data() + i * rank; }
@@ -37,6 +38,9 @@ struct QMeta {
 };
 
 QMeta meta_from_view(const qs_qspace_view *v);
+std::vector<std::string> parse_itags(const char *s);
+std::string join_itags(const std::vector<std::string> &t);
+std::string conj_itag(const std::string &t);
 
 // Contraction index: 0-based legs + conj flag.
 struct CtrIdx {
@@ -51,6 +55,7 @@ struct OperandLayout {
   bool permute = false;       // materialise a permuted copy first
   std::vector<int> perm;      // leg order of the permuted copy (0-based)
   bool ctr_front = false;     // contracted legs lead (else they trail)
+  bool conj = false;          // the permuted copy is conjugated
 };
 
 struct ContractPlan {

@@ -98,7 +98,10 @@ class QSpace:
         v.offs = offs.ctypes.data_as(_capi.c_int64_p)
         v.data = buf.ctypes.data_as(_capi.c_double_p)
         v.is_complex = 1 if cplx else 0
-        return v, (q, dims, offs, buf)
+        tags = self.info.get("itags")
+        tb = ",".join(tags).encode() if tags else None
+        v.itags = tb
+        return v, (q, dims, offs, buf, tb)
 
     @classmethod
     def unpack(cls, rank, qdim, q, dims, offs, data, cplx, info=None) -> "QSpace":
@@ -239,39 +242,6 @@ def _legs(ix) -> list[int]:
     return [int(x) - 1 for x in np.atleast_1d(ix)]
 
 
-def _out_itags(A: QSpace, ia, B: QSpace, ib, perm) -> list | None:
-    ta, tb = A.info.get("itags"), B.info.get("itags")
-    if not ta or not tb:
-        return None
-    la, lb = _legs(ia), _legs(ib)
-    ka = [k for k in range(A.rank) if k not in la]
-    kb = [k for k in range(B.rank) if k not in lb]
-
-    def cj(t, c):
-        if not c:
-            return t
-        return t[:-1] if t.endswith("*") else t + "*"
-
-    tags = [cj(ta[k], _conj_flag(ia)) for k in ka] + [cj(tb[k], _conj_flag(ib)) for k in kb]
-    p, n = _perm_arg(perm)
-    if p is not None:
-        pl = [p[i] - 1 for i in range(n)] + list(range(n, len(tags)))
-        tags = [tags[pl[i]] for i in range(len(tags))]
-    return tags
-
-
-def _check_itags(A: QSpace, ia, B: QSpace, ib):
-    """itag consistency of contracted legs (contract_getIdxSet,
-    Source/QSpace.cc:4230-4271): names must match up to the conjugation
-    mark."""
-    ta, tb = A.info.get("itags"), B.info.get("itags")
-    if not ta or not tb:
-        return
-    for a, b in zip(_legs(ia), _legs(ib)):
-        if a < len(ta) and b < len(tb) and ta[a].rstrip("*") != tb[b].rstrip("*"):
-            raise _capi.QSError(3, f"contract() itag mismatch {ta[a]} <> {tb[b]}")
-
-
 # ---------------------------------------------------------------- host calls
 def _result_to_qspace(lib, res, info=None) -> QSpace:
     r, qd, nb, ne, cx = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64(), C.c_int32()
@@ -283,7 +253,12 @@ def _result_to_qspace(lib, res, info=None) -> QSpace:
     data = np.empty(max(ne.value * (2 if cx.value else 1), 1), np.float64)
     check(lib.qs_result_copy(res, q.ctypes.data_as(_capi.c_int32_p), dims.ctypes.data_as(_capi.c_int64_p),
                              offs.ctypes.data_as(_capi.c_int64_p), data.ctypes.data_as(_capi.c_double_p)))
+    tb = C.create_string_buffer(4096)
+    check(lib.qs_result_itags(res, tb, 4096))
     lib.qs_result_free(res)
+    if tb.value:
+        info = dict(info or {})
+        info["itags"] = tb.value.decode().split(",")
     return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, bool(cx.value), info)
 
 
@@ -295,7 +270,6 @@ def contractQS(A: QSpace, ia, B: QSpace, ib, perm=None, *, prec: str = "fp64", n
     ``prec``: 'fp64' (plain drop-in) or 'split' (BF16 digits on tcgen05).
     """
     ctx = ctx or default_context()
-    _check_itags(A, ia, B, ib)
     va, ka = A.pack()
     vb, kb = B.pack()
     p, n = _perm_arg(perm)
@@ -304,8 +278,7 @@ def contractQS(A: QSpace, ia, B: QSpace, ib, perm=None, *, prec: str = "fp64", n
     res = C.c_void_p()
     check(ctx.lib.qs_contractQS(ctx.h, C.byref(va), _idx_str(ia), C.byref(vb), _idx_str(ib), p, n,
                                 C.byref(o), C.byref(res), C.byref(st)))
-    tags = _out_itags(A, ia, B, ib, perm)
-    out = _result_to_qspace(ctx.lib, res, {"itags": tags} if tags else None)
+    out = _result_to_qspace(ctx.lib, res, None)
     if stats is not None:
         stats.update(st.as_dict())
     del ka, kb
@@ -321,11 +294,7 @@ def permuteQS(A: QSpace, perm, conj=False, *, ctx: Context | None = None) -> QSp
     p, n = _perm_arg(perm)
     res = C.c_void_p()
     check(ctx.lib.qs_permuteQS(ctx.h, C.byref(va), p, n, 1 if conj else 0, C.byref(res)))
-    info = dict(A.info)
-    if A.info.get("itags") and p is not None:
-        t = A.info["itags"]
-        pl = [p[i] - 1 for i in range(n)] + list(range(n, len(t)))
-        info["itags"] = [t[pl[i]] for i in range(len(t))]
+    info = {k: v for k, v in A.info.items() if k != "itags"}
     return _result_to_qspace(ctx.lib, res, info)
 
 
@@ -356,7 +325,12 @@ class Tensor:
                                               dims.ctypes.data_as(_capi.c_int64_p),
                                               offs.ctypes.data_as(_capi.c_int64_p),
                                               data.ctypes.data_as(_capi.c_double_p)))
-        return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, cx, self.info)
+        tb = C.create_string_buffer(4096)
+        check(self.ctx.lib.qs_tensor_itags(self.h, tb, 4096))
+        info = dict(self.info)
+        if tb.value:
+            info["itags"] = tb.value.decode().split(",")
+        return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, cx, info)
 
     def free(self):
         if self.h:

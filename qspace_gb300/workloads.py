@@ -82,7 +82,7 @@ def grouped_pairs(seed: int = 0, npairs: int = 2000, lo: int = 8, hi: int = 1024
 
 
 def random_abelian(rng: np.random.Generator, legs: list, nblk_max: int = 40,
-                   complex_data: bool = False, density: float = 0.6) -> QSpace:
+                   complex_data: bool = False, density: float = 0.6, itags=None) -> QSpace:
     """Random abelian QSpace over the given leg sector tables.
 
     ``legs``: one list per leg of (label tuple, dim).  Blocks are a random
@@ -107,7 +107,7 @@ def random_abelian(rng: np.random.Generator, legs: list, nblk_max: int = 40,
         if complex_data:
             x = x + 1j * rng.standard_normal(shape)
         data.append(x)
-    return QSpace(Q, data, {})
+    return QSpace(Q, data, {"itags": list(itags)} if itags else {})
 
 
 def random_leg(rng: np.random.Generator, nsec: int = 4, dmax: int = 5, qdim: int = 1, qmax: int = 3):

@@ -48,9 +48,14 @@ def test_admission_refused_and_bad_request(ctx):
         with pytest.raises(QSError) as e:
             srv.submit(A, "1,1", A, "12")
         assert e.value.code == 1
-        # contracted dims differ: refused when the request is planned
+        # matching sectors whose contracted dims differ: refused when the
+        # request is planned
+        from qspace_gb300 import QSpace
+        q = np.array([[0]], np.int32)
+        X = upload(QSpace([q, q.copy()], [np.ones((2, 3))]), ctx)
+        Y = upload(QSpace([q, q.copy()], [np.ones((4, 3))]), ctx)
         with pytest.raises(QSError) as e:
-            srv.submit(A, "1", A, "2")
+            srv.submit(X, "1", Y, "1")
         assert e.value.code == 2
 
 
