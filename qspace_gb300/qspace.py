@@ -8,8 +8,9 @@ reference's names, argument meaning and error behaviour:
 * ``contractQS(A, ia, B, ib[, perm])`` -- Source/contractQS.cc:505-632;
 * ``permuteQS(A, perm[, 'conj'])``     -- Source/permuteQS.cc:198-258.
 
-All numerical work runs on the GPU through the C-ABI; only label bookkeeping
-of itags happens here.  ``Tensor`` is a device-resident QSpace.
+All numerical work, label matching and itag bookkeeping run in the library
+behind the C-ABI; this module only packs and unpacks host buffers.
+``Tensor`` is a device-resident QSpace.
 """
 from __future__ import annotations
 
@@ -216,30 +217,6 @@ def _idx_str(ix) -> bytes:
     # numeric (1-based) indices: bracketed and blank separated so that a
     # single multi-digit leg is not read in compact form
     return ("[" + " ".join(str(x) for x in v) + " ]").encode()
-
-
-def _conj_flag(ix) -> bool:
-    if not isinstance(ix, str):
-        return False
-    s = ix.rstrip()
-    n = 0
-    while s.endswith("*"):
-        n += 1
-        s = s[:-1].rstrip()
-    return bool(n % 2)
-
-
-def _legs(ix) -> list[int]:
-    if isinstance(ix, str):
-        s = ix.rstrip().rstrip("*").strip().strip("[]")
-        if any(c in s for c in ",; "):
-            return [int(x) - 1 for x in s.replace(",", " ").replace(";", " ").split()]
-        out = []
-        for c in s:
-            out.append(int(c) - 1 if c.isdigit() else
-                       (ord(c) - 65 + 10 - 1 if c.isupper() else ord(c) - 97 + 36 - 1))
-        return out
-    return [int(x) - 1 for x in np.atleast_1d(ix)]
 
 
 # ---------------------------------------------------------------- host calls
