@@ -216,6 +216,33 @@ QS_EXPORT qs_status qs_grouped_gemm_host(qs_ctx *ctx, const qs_pair_list *pairs,
                                double *C, int64_t c_elems,
                                const qs_opts *opts, qs_stats *stats);
 
+/* ------------------------------------- split grouped GEMM, no allocation
+ * No reference counterpart: QSpace has no GPU path.  The same product as
+ * qs_grouped_gemm with QS_PREC_SPLIT (opts NULL: split, tol 1e-12; any other
+ * prec is QS_ERR_ARG), for callers that must not allocate device memory
+ * while they run -- a host whose device memory is fully handed to another
+ * allocator, or a serving loop that must not let cudaFree synchronise the
+ * device.  It allocates no device memory: no cudaMalloc/cudaMallocAsync/
+ * cudaFree, no memory pool, no library workspace (its host-side planning uses
+ * ordinary host memory).  Its device scratch (work lists,
+ * exponents, BF16 digits) is one file-scope array of
+ * QS_STATIC_SCRATCH_BYTES per device and process; a pair list that needs
+ * more is refused with QS_ERR_OOM before anything is launched.
+ *  - The first call on each device looks the array up (cudaGetSymbolAddress)
+ *    and clears its 4-byte error word, the only part that must start at
+ *    zero; make that first call before any stream capture.  Everything else
+ *    in the array is written before it is read in every call.
+ *  - All calls in a process share the array of their device: calls that
+ *    overlap in time (two host threads, two contexts) race on it and corrupt
+ *    each other's results.  Serialise them.
+ *  - A, B, C are device pointers as for qs_grouped_gemm; the call returns
+ *    after the product is complete (it synchronises the context's stream to
+ *    read the error word). */
+#define QS_STATIC_SCRATCH_BYTES 33554432 /* 32 MiB */
+QS_EXPORT qs_status qs_grouped_gemm_split_static(qs_ctx *ctx, const qs_pair_list *pairs,
+                                                 const double *A, const double *B, double *C,
+                                                 const qs_opts *opts, qs_stats *stats);
+
 /* ------------------------------------------------------- eigQS blocks
  * Hermitian eigendecomposition of every symmetry block on the device in FP64
  * (the OpenMP loop of QSpace::EigenSymmetric, Source/QSpace.cc:4789-4811,

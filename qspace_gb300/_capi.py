@@ -100,6 +100,8 @@ SIGNATURES = {
                                  C.POINTER(C.c_void_p)]),
     "qs_grouped_gemm": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
+    "qs_grouped_gemm_split_static": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
     "qs_grouped_gemm_host": (C.c_int, [C.c_void_p, C.POINTER(PairList), c_double_p, C.c_int64,
                                        c_double_p, C.c_int64, c_double_p, C.c_int64,
                                        C.POINTER(Opts), C.POINTER(Stats)]),

@@ -22,9 +22,9 @@
 //    depth of a block exceeds that bound, the K loop is cut into chunks whose
 //    accumulators are drained and added exactly (int64).
 //  * The S digit tiles of B are laid side by side along N, so one
-//    tcgen05.mma with A-digit t and N = (S-t)*64 produces all products
+//    tcgen05.mma with A-digit t and N = (S-t)*32 produces all products
 //    d_t * d'_u (u = 0..S-1-t) at once and drops each into the TMEM columns of
-//    accumulator group g = t+u (column offset 64*g).  S(S+1)/2 digit
+//    accumulator group g = t+u (column offset 32*g).  S(S+1)/2 digit
 //    products therefore take about S + S/2 wide MMA instructions per K step.
 //  * The CG factor of each pair is folded into A's digits with an exact
 //    integer product (53 x 53 bits) before rounding, so pairs with different
@@ -34,7 +34,7 @@
 //    (scale 2^(E_i+F_j-2b), round to nearest even): no FP64 instruction, as
 //    the FP64 pipe of GB300 is narrow.  Partial sums of later accumulator
 //    chunks are added exactly as int64 in the output slot.  One CTA owns one
-//    128x64 output tile and sums the block pairs in plan order:
+//    128x32 output tile at a time and sums the block pairs in plan order:
 //    deterministic, no atomics.
 //
 // Data movement: a slicing kernel writes the digits of every pair operand once
@@ -43,7 +43,7 @@
 // whole digit tiles with 1-D TMA bulk copies (cp.async.bulk + mbarrier
 // transaction counts) into a multi-stage shared-memory ring.  Warp roles:
 // warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2..9 =
-// epilogue (one TMEM lane quarter each).  Every mbarrier wait is bounded; on
+// epilogue (two per TMEM lane quarter).  Every mbarrier wait is bounded; on
 // timeout the kernel records an error code, stops issuing work, waits a
 // bounded time for what is in flight, frees its TMEM and returns.
 #include <cuda_bf16.h>
@@ -791,7 +791,8 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
                     const int2 *d_ct, int nct, const int4 *d_xt, int nxt, const int4 *d_at, int nat,
                     const int4 *d_bt, int nbt,
                     const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
-                    int *dE, int64_t nE, int *dF, int64_t nF, uint8_t *arena, int b, int kchunk) {
+                    int *dE, int64_t nE, int *dF, int64_t nF, uint8_t *arena, int b, int kchunk,
+                    int *err) {
   cudaStream_t st = ctx->stream;
   const int fg = (int)std::min<int64_t>(std::max<int64_t>((nE + nF + 255) / 256, 1), 4096);
   ctx->mark(0);
@@ -818,7 +819,7 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
   ctx->mark(1);
   const int grid = std::min(ntiles, std::max(ctx->num_sms, 1));
   gemm_split_kernel<S><<<grid, 320, sm, st>>>(d_tiles, ntiles, d_pairs, arena, dE, dF, C, b, nst, kchunk,
-                                              ctx->d_err);
+                                              err);
   QS_LAUNCHED(ctx);
   ctx->mark(2);
 }
@@ -909,24 +910,52 @@ DigitPlan choose_digits(int64_t kreal, double tol, int forced_slices) {
   return choose_digits_for(one, {0, 1}, {TMS}, {TNS}, 1, tol, forced_slices);
 }
 
-SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
-                      const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
-                      const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
-                      bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc) {
+// Host-side work lists of one planned split product.
+struct SplitWork {
+  int S = 0, b = 0, kchunk = 0;
+  int64_t nE = 0, nF = 0, arena = 0;
+  std::vector<SplitPair> sp;
+  std::vector<int2> rt, ct;
+  std::vector<int4> xt, at, bt;
+  std::vector<SplitTile> tiles;
+};
+
+// Their device copies, the exponent arrays and the digit arena.
+struct SplitDev {
+  SplitPair *pairs = nullptr;
+  int2 *rt = nullptr, *ct = nullptr;
+  int4 *xt = nullptr, *at = nullptr, *bt = nullptr;
+  SplitTile *tiles = nullptr;
+  int *E = nullptr, *F = nullptr;
+  uint8_t *arena = nullptr;
+};
+
+// Host half of the split path: digit plan, per-pair digit geometry and arena
+// offsets, and the device work lists (exponent lines, slicing tiles, output
+// tiles in launch order).
+static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                              const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                              const std::vector<int64_t> &c_off, bool cplx, int forced_slices, double tol,
+                              const std::vector<int32_t> *blk_ldc, SplitWork &w) {
   SplitResult res;
   const int64_t nb = (int64_t)blk_M.size();
   const int cm = cplx ? 2 : 1;
   DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices);
   const int S = dp.nslices, b = dp.bits;
   const int kchunk = kchunk_of(b, S);
+  w.S = S;
+  w.b = b;
+  w.kchunk = kchunk;
   res.nslices = S;
   res.bits = b;
   res.err_bound = dp.err_bound;
 
   // per-pair digit geometry and arena offsets
-  std::vector<SplitPair> sp(pairs.size());
+  std::vector<SplitPair> &sp = w.sp;
+  sp.resize(pairs.size());
   std::vector<int64_t> eoff(nb), foff(nb);
-  int64_t nE = 0, nF = 0;
+  int64_t &nE = w.nE, &nF = w.nF;
+  nE = nF = 0;
   for (int64_t g = 0; g < nb; ++g) {
     eoff[g] = nE;
     foff[g] = nF;
@@ -934,11 +963,12 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
     nF += blk_N[g];
   }
   if (nE > INT32_MAX || nF > INT32_MAX) fail(QS_ERR_SHAPE, "split: exponent arrays too large");
-  int64_t arena = 0;
-  std::vector<int2> rt, ct;
-  std::vector<int4> xt;
-  std::vector<int4> at, bt;
-  std::vector<SplitTile> tiles;
+  int64_t &arena = w.arena;
+  arena = 0;
+  std::vector<int2> &rt = w.rt, &ct = w.ct;
+  std::vector<int4> &xt = w.xt;
+  std::vector<int4> &at = w.at, &bt = w.bt;
+  std::vector<SplitTile> &tiles = w.tiles;
   for (int64_t g = 0; g < nb; ++g) {
     // every pair's CG factor is folded into its A digits (exact integer
     // product), so the pairs of a block share the accumulators
@@ -1025,24 +1055,20 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   res.slice_bytes = arena;
   res.ntiles = (int64_t)tiles.size();
 
-  // device buffers: one allocation for the digit arena (pooled scratch)
-  uint8_t *d_arena = static_cast<uint8_t *>(ctx->ensure_scratch((size_t)std::max<int64_t>(arena, 256)));
-  SplitPair *d_pairs = dev_upload(ctx, sp);
-  int2 *d_rt = dev_upload(ctx, rt);
-  int2 *d_ct = dev_upload(ctx, ct);
-  int4 *d_xt = dev_upload(ctx, xt);
-  int4 *d_at = dev_upload(ctx, at);
-  int4 *d_bt = dev_upload(ctx, bt);
-  SplitTile *d_tiles = dev_upload(ctx, tiles);
-  int *dE = dev_alloc<int>(ctx, (size_t)nE);
-  int *dF = dev_alloc<int>(ctx, (size_t)nF);
-  switch (S) {
+  return res;
+}
+
+// Device half: launches the exponent, slicing and GEMM kernels of a planned
+// split product on the context's stream, with every work list, exponent
+// array and the digit arena already on the device.
+static void launch_split(Ctx *ctx, const SplitWork &w, bool cplx, const SplitDev &d, const double *A,
+                         const double *B, double *C, int *err) {
+  switch (w.S) {
 #define QS_CASE(SS)                                                                                      \
   case SS:                                                                                               \
-    launch_split_s<SS>(ctx, cplx, d_pairs, d_rt, (int)rt.size(), d_ct, (int)ct.size(), d_xt, (int)xt.size(), \
-                       d_at, (int)at.size(),                                                             \
-                       d_bt, (int)bt.size(), d_tiles, (int)tiles.size(), A, B, C, dE, nE, dF, nF, d_arena, b, \
-                       kchunk);                                                                          \
+    launch_split_s<SS>(ctx, cplx, d.pairs, d.rt, (int)w.rt.size(), d.ct, (int)w.ct.size(), d.xt,        \
+                       (int)w.xt.size(), d.at, (int)w.at.size(), d.bt, (int)w.bt.size(), d.tiles,        \
+                       (int)w.tiles.size(), A, B, C, d.E, w.nE, d.F, w.nF, d.arena, w.b, w.kchunk, err); \
     break;
     QS_CASE(2)
     QS_CASE(3)
@@ -1053,17 +1079,88 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
     QS_CASE(8)
 #undef QS_CASE
     default:
-      fail(QS_ERR_INTERNAL, "split: unsupported digit count %d", S);
+      fail(QS_ERR_INTERNAL, "split: unsupported digit count %d", w.S);
   }
-  dev_free(ctx, d_pairs);
-  dev_free(ctx, d_rt);
-  dev_free(ctx, d_ct);
-  dev_free(ctx, d_xt);
-  dev_free(ctx, d_at);
-  dev_free(ctx, d_bt);
-  dev_free(ctx, d_tiles);
-  dev_free(ctx, dE);
-  dev_free(ctx, dF);
+}
+
+SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                      const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                      const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
+                      bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc) {
+  SplitWork w;
+  SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w);
+  if (w.tiles.empty()) return res;
+  // device buffers: one allocation for the digit arena (pooled scratch)
+  SplitDev d;
+  d.arena = static_cast<uint8_t *>(ctx->ensure_scratch((size_t)std::max<int64_t>(w.arena, 256)));
+  d.pairs = dev_upload(ctx, w.sp);
+  d.rt = dev_upload(ctx, w.rt);
+  d.ct = dev_upload(ctx, w.ct);
+  d.xt = dev_upload(ctx, w.xt);
+  d.at = dev_upload(ctx, w.at);
+  d.bt = dev_upload(ctx, w.bt);
+  d.tiles = dev_upload(ctx, w.tiles);
+  d.E = dev_alloc<int>(ctx, (size_t)w.nE);
+  d.F = dev_alloc<int>(ctx, (size_t)w.nF);
+  launch_split(ctx, w, cplx, d, A, B, C, ctx->d_err);
+  dev_free(ctx, d.pairs);
+  dev_free(ctx, d.rt);
+  dev_free(ctx, d.ct);
+  dev_free(ctx, d.xt);
+  dev_free(ctx, d.at);
+  dev_free(ctx, d.bt);
+  dev_free(ctx, d.tiles);
+  dev_free(ctx, d.E);
+  dev_free(ctx, d.F);
+  return res;
+}
+
+SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                             const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                             const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
+                             bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
+                             uint8_t *scratch, size_t cap, int *err) {
+  SplitWork w;
+  SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w);
+  if (w.tiles.empty()) return res;
+  size_t used = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = used;
+    used += (std::max<size_t>(bytes, 1) + 255) / 256 * 256;
+    return o;
+  };
+  const size_t o_pairs = take(w.sp.size() * sizeof(SplitPair));
+  const size_t o_rt = take(w.rt.size() * sizeof(int2)), o_ct = take(w.ct.size() * sizeof(int2));
+  const size_t o_xt = take(w.xt.size() * sizeof(int4)), o_at = take(w.at.size() * sizeof(int4));
+  const size_t o_bt = take(w.bt.size() * sizeof(int4));
+  const size_t o_tiles = take(w.tiles.size() * sizeof(SplitTile));
+  const size_t o_E = take((size_t)w.nE * sizeof(int)), o_F = take((size_t)w.nF * sizeof(int));
+  const size_t o_arena = take((size_t)w.arena);
+  if (used > cap)
+    fail(QS_ERR_OOM, "split (static scratch): this pair list needs %zu bytes of scratch (%lld of them "
+         "BF16 digits), more than the %zu available", used, (long long)w.arena, cap);
+  SplitDev d;
+  d.pairs = reinterpret_cast<SplitPair *>(scratch + o_pairs);
+  d.rt = reinterpret_cast<int2 *>(scratch + o_rt);
+  d.ct = reinterpret_cast<int2 *>(scratch + o_ct);
+  d.xt = reinterpret_cast<int4 *>(scratch + o_xt);
+  d.at = reinterpret_cast<int4 *>(scratch + o_at);
+  d.bt = reinterpret_cast<int4 *>(scratch + o_bt);
+  d.tiles = reinterpret_cast<SplitTile *>(scratch + o_tiles);
+  d.E = reinterpret_cast<int *>(scratch + o_E);
+  d.F = reinterpret_cast<int *>(scratch + o_F);
+  d.arena = scratch + o_arena;
+  auto put = [&](void *dst, const void *src, size_t bytes) {
+    if (bytes) QS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  };
+  put(d.pairs, w.sp.data(), w.sp.size() * sizeof(SplitPair));
+  put(d.rt, w.rt.data(), w.rt.size() * sizeof(int2));
+  put(d.ct, w.ct.data(), w.ct.size() * sizeof(int2));
+  put(d.xt, w.xt.data(), w.xt.size() * sizeof(int4));
+  put(d.at, w.at.data(), w.at.size() * sizeof(int4));
+  put(d.bt, w.bt.data(), w.bt.size() * sizeof(int4));
+  put(d.tiles, w.tiles.data(), w.tiles.size() * sizeof(SplitTile));
+  launch_split(ctx, w, cplx, d, A, B, C, err);
   return res;
 }
 

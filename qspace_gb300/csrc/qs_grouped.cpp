@@ -13,7 +13,8 @@
 namespace qs {
 void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
                  const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
-                 int64_t c_elems);
+                 int64_t c_elems, uint8_t *static_scratch = nullptr, size_t static_cap = 0,
+                 int *static_err = nullptr);
 }
 
 using namespace qs;
@@ -22,10 +23,11 @@ namespace qs {
 
 // Validates the pair list, builds the device work lists and launches the
 // FP64 or the split path.  When the element counts are known (host form),
-// every access is checked against them.
+// every access is checked against them.  With `static_scratch` the split
+// path carves its device buffers from that scratch instead of allocating.
 void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
                  const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
-                 int64_t c_elems) {
+                 int64_t c_elems, uint8_t *static_scratch, size_t static_cap, int *static_err) {
   if (!pl) fail(QS_ERR_ARG, "null pair list");
   const int64_t n = pl->npairs;
   if (n < 0) fail(QS_ERR_ARG, "negative pair count");
@@ -103,13 +105,19 @@ void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double
     stats->nblk_out = (int64_t)bM.size();
   }
   if (prec == QS_PREC_SPLIT) {
-    SplitResult sr = run_split(ctx, pairs, grp, bM, bN, coff, A, B, C, cplx, opts ? opts->nslices : 0,
-                               opts && opts->tol > 0 ? opts->tol : 1e-12, &bldc);
+    const int ns = opts ? opts->nslices : 0;
+    const double tol = opts && opts->tol > 0 ? opts->tol : 1e-12;
+    SplitResult sr = static_scratch
+                         ? run_split_static(ctx, pairs, grp, bM, bN, coff, A, B, C, cplx, ns, tol, &bldc,
+                                            static_scratch, static_cap, static_err)
+                         : run_split(ctx, pairs, grp, bM, bN, coff, A, B, C, cplx, ns, tol, &bldc);
     if (stats) {
       stats->nslices = sr.nslices;
       stats->digit_bits = sr.bits;
       stats->err_bound = sr.err_bound;
     }
+  } else if (static_scratch) {
+    fail(QS_ERR_ARG, "the static-scratch entry point runs the split path only");
   } else if (prec == QS_PREC_FP64) {
     std::vector<TileDesc> tiles = make_tiles(grp, bM, bN, coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &bldc);
     PairDesc *dp = dev_upload(ctx, pairs);

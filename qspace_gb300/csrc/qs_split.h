@@ -33,4 +33,15 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs,
                       int forced_slices, double tol,
                       const std::vector<int32_t> *blk_ldc = nullptr);
 
+// The same product with every device buffer carved from caller-provided
+// scratch (`cap` bytes, 256-byte aligned) instead of allocated; the bounded
+// waits report to `err`.  A plan that does not fit is refused (QS_ERR_OOM)
+// before anything is copied or launched.
+SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs,
+                             const std::vector<int64_t> &grp, const std::vector<int32_t> &blk_M,
+                             const std::vector<int32_t> &blk_N, const std::vector<int64_t> &c_off,
+                             const double *A, const double *B, double *C, bool cplx,
+                             int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
+                             uint8_t *scratch, size_t cap, int *err);
+
 }  // namespace qs
