@@ -40,6 +40,17 @@ void *Ctx::ensure_scratch(size_t bytes) {
   return scratch;
 }
 
+void Ctx::ensure_copy_streams() {
+  if (!h2d) QS_CUDA(cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking));
+  if (!d2h) QS_CUDA(cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking));
+}
+
+void Ctx::destroy_copy_streams() {
+  if (h2d) cudaStreamDestroy(h2d);
+  if (d2h) cudaStreamDestroy(d2h);
+  h2d = d2h = nullptr;
+}
+
 // Chunk tables for the permute kernel.
 static void run_permute(Ctx *ctx, const std::vector<PermDesc> &descs, const double *in, double *out,
                         bool cplx) {
@@ -373,6 +384,7 @@ void qs_ctx_destroy(qs_ctx *ctx) {
   if (ctx->c.d_err) cudaFree(ctx->c.d_err);
   for (auto &e : ctx->c.ev)
     if (e) cudaEventDestroy(e);
+  ctx->c.destroy_copy_streams();
   cudaStreamDestroy(ctx->c.stream);
   delete ctx;
 }

@@ -17,8 +17,6 @@ namespace qs {
 namespace {
 constexpr int TM = 64, TN = 64;
 
-__device__ __forceinline__ double cmul_re(double2 a, double2 b) { return a.x * b.x - a.y * b.y; }
-
 template <bool CPLX>
 struct Elem;
 template <>

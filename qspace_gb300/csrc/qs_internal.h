@@ -54,6 +54,10 @@ struct Ctx {
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
   void *ensure_scratch(size_t bytes);
+  // copy streams of the pipelined host-buffer path (created on first use)
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  void ensure_copy_streams();
+  void destroy_copy_streams();
   // cuSOLVER handle (created on first use)
   void *solver = nullptr;
   // phase timing: events around operand preparation and the GEMM kernel

@@ -160,6 +160,7 @@ void qs_server_destroy(qs_server *s) {
     cudaStreamSynchronize(c->stream);
     destroy_solver(c.get());
     cudaFree(c->d_err);
+    c->destroy_copy_streams();
     cudaStreamDestroy(c->stream);
   }
   delete s;
