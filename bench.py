@@ -3,11 +3,16 @@
 
 Workload (N=1, per rank): the batched grouped contraction of 2000 independent
 block pairs C_p = afac_p * A_p B_p, M, N, K = round(exp(U(ln 8, ln 1024))),
-complex128 N(0,1) entries, afac_p ~ U(-1, 1), seed 0 -- one persistent
-grouped launch per step.  Metric: FP64-equivalent TFLOP/s (8 M N K per
-complex pair) at <= 1e-12 relative error; the split BF16 path is the
-headline, the plain FP64 path is reported beside it; per-step latency
-p50/p99.  Inputs (2.8 GB) are larger than L2, so no flush is needed.
+complex128 N(0,1) entries, afac_p ~ U(-1, 1), seed 0.  A step is one pass
+of the grouped product over the batch through a reusable plan
+(qs_grouped_plan_*): planned once, digit width autotuned on the first run,
+the persistent grouped launch replayed as a CUDA graph -- the way a DMRG
+or NRG driver repeats products over one block structure.  The one-shot call
+(qs_grouped_gemm, planned every call) is reported beside it.  Metric:
+FP64-equivalent TFLOP/s (8 M N K per complex pair) at <= 1e-12 relative
+error; the split BF16 path is the headline, the plain FP64 path is reported
+beside it; per-step latency p50/p99.  Inputs (2.8 GB) are larger than L2,
+so no flush is needed.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -45,6 +50,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--mode", default="plan", choices=["plan", "oneshot"],
+                    help="plan: reusable plan replayed as a CUDA graph; oneshot: qs_grouped_gemm per step")
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -190,9 +198,23 @@ def main():
         den += float(np.sum(np.abs(r) ** 2))
     rel_vs_oracle = (num / den) ** 0.5
 
-    # ---- timed region
+    # ---- timed region: plan replays (tuning and graph recording happen in
+    # the first run, before the warm-up)
+    plan = db.plan(a.prec, autotune=not a.no_autotune) if a.mode == "plan" else None
+
+    def step(prec=a.prec, p=plan):
+        if p is not None:
+            db.run_plan(p)
+        else:
+            db.run(prec)
+
+    if plan is not None:
+        st = {}
+        db.run_plan(plan, st)
+        ctx.sync()
+        tuned_ms = st.get("device_ms")
     for _ in range(a.warmup):
-        db.run(a.prec)
+        step()
     ctx.sync()
     if pg:
         pg.barrier()
@@ -204,7 +226,7 @@ def main():
     with torch.cuda.stream(stream):
         evs[0].record(stream)
         for k in range(a.steps):
-            db.run(a.prec)
+            step()
             evs[k + 1].record(stream)
     ctx.sync()
     torch.cuda.synchronize()
@@ -220,16 +242,37 @@ def main():
         total_ms = float(t.item())
     ms = total_ms / a.steps
     value = ws * flops / (ms * 1e-3) / 1e12
+    # what was timed is checked too
+    rel_timed = float(torch.linalg.vector_norm(db.dC - c64) / torch.linalg.vector_norm(c64))
 
-    # ---- live roofline of the dominant kernel (CUDA events on its stream)
+    # ---- the one-shot call (planned every call), same batch
+    oneshot = None
+    if plan is not None:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        db.run(a.prec)
+        ctx.sync()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(a.steps):
+                db.run(a.prec)
+            e1.record(stream)
+        ctx.sync()
+        oms = e0.elapsed_time(e1) / a.steps
+        oneshot = {"value": flops / (oms * 1e-3) / 1e12, "ms_per_step": oms, "api": "qs_grouped_gemm"}
+
+    # ---- live roofline of the dominant kernel (CUDA events on its stream),
+    # from direct launches of the same plan (same digit plan, no graph)
     ctx.set_timing(True)
     prep, gemm = [], []
+    tplan = db.plan(a.prec, autotune=not a.no_autotune, graph=False) if plan is not None else None
     for _ in range(3):
-        db.run(a.prec)
+        step(p=tplan)
         p_, g_ = ctx.phase_ms()
         prep.append(p_)
         gemm.append(g_)
     ctx.set_timing(False)
+    if tplan is not None:
+        tplan.close()
     gemm_ms = statistics.median(gemm)
     prep_ms = statistics.median(prep)
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
@@ -252,14 +295,17 @@ def main():
     plain = None
     if a.prec == "split" and a.plain_steps > 0:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        db.run("fp64")
+        pplan = db.plan("fp64") if plan is not None else None
+        step("fp64", pplan)
         ctx.sync()
         with torch.cuda.stream(stream):
             e0.record(stream)
             for _ in range(a.plain_steps):
-                db.run("fp64")
+                step("fp64", pplan)
             e1.record(stream)
         ctx.sync()
+        if pplan is not None:
+            pplan.close()
         pms = e0.elapsed_time(e1) / a.plain_steps
         plain = {"value": flops / (pms * 1e-3) / 1e12, "ms_per_step": pms}
 
@@ -300,8 +346,13 @@ def main():
                 "data": "synthetic (seeded normal)",
                 "config": {"workload": WORKLOAD, "npairs": a.npairs, "seed": a.seed, "prec": a.prec,
                            "nslices": st.get("nslices"), "digit_bits": st.get("digit_bits"),
-                           "parallelism": f"replicas x{ws}", "l2": "inputs 2.8 GB > L2, no flush"},
-                "rel_err_vs_fp64_gpu": rel_vs_fp64, "rel_err_vs_oracle_sample": rel_vs_oracle,
+                           "parallelism": f"replicas x{ws}", "l2": "inputs 2.8 GB > L2, no flush",
+                           "mode": a.mode + ("" if a.mode == "oneshot" else
+                                             " (reusable plan, CUDA graph replay"
+                                             + (", autotuned digit width)" if not a.no_autotune else ")"))},
+                "rel_err_vs_fp64_gpu": rel_vs_fp64, "rel_err_vs_fp64_gpu_timed": rel_timed,
+                "rel_err_vs_oracle_sample": rel_vs_oracle, "oneshot": oneshot,
+                "autotune_ms": tuned_ms if plan is not None else None,
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

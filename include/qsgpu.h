@@ -93,6 +93,7 @@ typedef struct {
 
 #define QS_FLAG_NO_GRAPH 1      /* do not capture/replay the launch in a CUDA graph */
 #define QS_FLAG_DETERMINISTIC 2 /* fixed reduction order (always true today)   */
+#define QS_FLAG_AUTOTUNE 4      /* reusable plans: time the digit widths on the first run */
 
 /* Per-call statistics (optional out-parameter). */
 typedef struct {
@@ -215,6 +216,26 @@ QS_EXPORT qs_status qs_grouped_gemm_host(qs_ctx *ctx, const qs_pair_list *pairs,
                                const double *B, int64_t b_elems,
                                double *C, int64_t c_elems,
                                const qs_opts *opts, qs_stats *stats);
+
+/* ------------------------------------------------ reusable grouped plans
+ * No reference counterpart (the reference plans every contraction anew).  A
+ * plan validates a pair list once, keeps its work lists and digit arena on
+ * the device, and records its launch sequence as a CUDA graph on the first
+ * run; later runs with the same A, B, C replay the graph (other pointers
+ * record it again).  Repeated products over one block structure -- the
+ * Davidson iterations of a DMRG site update, the steps of an NRG run --
+ * then skip host planning.  opts->flags: QS_FLAG_NO_GRAPH launches directly;
+ * QS_FLAG_AUTOTUNE times every digit width that meets opts->tol on the first
+ * run and keeps the fastest (remembered per pair-list shape in the process;
+ * stats->device_ms reports the winner's time).  A, B, C are device pointers
+ * as for qs_grouped_gemm; runs are asynchronous on the context's stream.  A
+ * plan is destroyed before its context. */
+typedef struct qs_grouped_plan qs_grouped_plan;
+QS_EXPORT qs_status qs_grouped_plan_create(qs_ctx *ctx, const qs_pair_list *pairs, const qs_opts *opts,
+                                           qs_grouped_plan **out);
+QS_EXPORT qs_status qs_grouped_plan_run(qs_grouped_plan *plan, const double *A, const double *B, double *C,
+                                        qs_stats *stats);
+QS_EXPORT void qs_grouped_plan_destroy(qs_grouped_plan *plan);
 
 /* ------------------------------------- split grouped GEMM, no allocation
  * No reference counterpart: QSpace has no GPU path.  The same product as

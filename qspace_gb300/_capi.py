@@ -53,6 +53,8 @@ class ServerCfg(C.Structure):
 
 QS_PREC_FP64 = 0
 QS_PREC_SPLIT = 1
+QS_FLAG_NO_GRAPH = 1
+QS_FLAG_AUTOTUNE = 4
 
 STATUS = {0: "QS_OK", 1: "QS_ERR_ARG", 2: "QS_ERR_SHAPE", 3: "QS_ERR_LABEL", 4: "QS_ERR_CUDA",
           5: "QS_ERR_OOM", 6: "QS_ERR_TIMEOUT", 7: "QS_ERR_UNSUPPORTED", 8: "QS_ERR_INTERNAL",
@@ -100,6 +102,10 @@ SIGNATURES = {
                                  C.POINTER(C.c_void_p)]),
     "qs_grouped_gemm": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
+    "qs_grouped_plan_create": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.POINTER(Opts),
+                                         C.POINTER(C.c_void_p)]),
+    "qs_grouped_plan_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Stats)]),
+    "qs_grouped_plan_destroy": (None, [C.c_void_p]),
     "qs_grouped_gemm_split_static": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
     "qs_grouped_gemm_host": (C.c_int, [C.c_void_p, C.POINTER(PairList), c_double_p, C.c_int64,

@@ -40,6 +40,69 @@ void *Ctx::ensure_scratch(size_t bytes) {
   return scratch;
 }
 
+// Copies `bytes` from host memory to `dst` (device) on the context stream
+// through the page-locked ring, read by a copy kernel (not a copy engine).
+// A region of the ring is reused only after the copy that last read it has
+// completed.
+void Ctx::stage_upload(void *dst, const void *src, size_t bytes) {
+  if (!bytes) return;
+  const int64_t n = (int64_t)((bytes + 255) & ~size_t(255));
+  if ((size_t)n > stage_cap / 2) {
+    // grow: wait for every staged copy, then replace the buffer
+    QS_CUDA(cudaStreamSynchronize(stream));
+    for (auto &m : stage_q) stage_ev.push_back(m.ev);
+    stage_q.clear();
+    if (stage_buf) cudaFreeHost(stage_buf);
+    stage_buf = stage_dev = nullptr;
+    stage_cap = 0;
+    const size_t cap = std::max<size_t>({(size_t)n * 4, stage_cap * 2, (size_t)4 << 20});
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(&stage_buf), cap, cudaHostAllocMapped);
+    if (e != cudaSuccess) {
+      stage_buf = nullptr;
+      fail(QS_ERR_OOM, "page-locked staging buffer of %zu bytes: %s", cap, cudaGetErrorString(e));
+    }
+    e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&stage_dev), stage_buf, 0);
+    if (e != cudaSuccess) {
+      cudaFreeHost(stage_buf);
+      stage_buf = stage_dev = nullptr;
+      fail(QS_ERR_CUDA, "staging buffer device address: %s", cudaGetErrorString(e));
+    }
+    stage_cap = cap;
+    stage_head = 0;
+  }
+  const int64_t cap = (int64_t)stage_cap;
+  int64_t h = stage_head;
+  if (h % cap + n > cap) h += cap - h % cap;  // wrap to the start
+  while (!stage_q.empty() && stage_q.front().start < h + n - cap) {
+    QS_CUDA(cudaEventSynchronize(stage_q.front().ev));
+    stage_ev.push_back(stage_q.front().ev);
+    stage_q.pop_front();
+  }
+  std::memcpy(stage_buf + h % cap, src, bytes);
+  launch_stage_copy(this, stage_dev + h % cap, dst, bytes);
+  cudaEvent_t ev;
+  if (stage_ev.empty()) {
+    QS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  } else {
+    ev = stage_ev.back();
+    stage_ev.pop_back();
+  }
+  QS_CUDA(cudaEventRecord(ev, stream));
+  stage_q.push_back({ev, h});
+  stage_head = h + n;
+}
+
+void Ctx::destroy_staging() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (auto &m : stage_q) cudaEventDestroy(m.ev);
+  for (auto e : stage_ev) cudaEventDestroy(e);
+  stage_q.clear();
+  stage_ev.clear();
+  if (stage_buf) cudaFreeHost(stage_buf);
+  stage_buf = stage_dev = nullptr;
+  stage_cap = 0;
+}
+
 void Ctx::ensure_copy_streams() {
   if (!h2d) QS_CUDA(cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking));
   if (!d2h) QS_CUDA(cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking));
@@ -385,6 +448,7 @@ void qs_ctx_destroy(qs_ctx *ctx) {
   for (auto &e : ctx->c.ev)
     if (e) cudaEventDestroy(e);
   ctx->c.destroy_copy_streams();
+  ctx->c.destroy_staging();
   cudaStreamDestroy(ctx->c.stream);
   delete ctx;
 }
@@ -394,7 +458,15 @@ void *qs_ctx_stream(qs_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr;
 qs_status qs_ctx_sync(qs_ctx *ctx) {
   QS_API_BEGIN
   if (!ctx) fail(QS_ERR_ARG, "null ctx");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
   QS_CUDA(cudaStreamSynchronize(ctx->c.stream));
+  // a bounded device wait that ran out in an asynchronous call is reported here
+  int kerr = 0;
+  QS_CUDA(cudaMemcpy(&kerr, ctx->c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (kerr) {
+    QS_CUDA(cudaMemset(ctx->c.d_err, 0, sizeof(int)));
+    fail(QS_ERR_TIMEOUT, "a bounded device wait ran out (code %d)", kerr);
+  }
   QS_API_END
 }
 

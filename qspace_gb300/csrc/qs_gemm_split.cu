@@ -51,6 +51,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <memory>
+#include <type_traits>
 
 #include "qs_internal.h"
 #include "qs_split.h"
@@ -867,7 +869,7 @@ static double drain_units() {
 
 DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                             const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
-                            double tol, int forced_slices) {
+                            double tol, int forced_slices, int forced_bits = 0) {
   if (!(tol > 0)) tol = 1e-12;
   // bits of precision wanted: the tolerance plus a margin for the growth of
   // the error with the summed depth relative to |C|.
@@ -877,7 +879,8 @@ DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vecto
   const int64_t nb = (int64_t)blk_M.size();
   const double DRAIN_UNITS = drain_units();
   const char *fb = std::getenv("QS_SPLIT_BITS");
-  const int bhi = fb ? std::atoi(fb) : 8, blo = fb ? std::atoi(fb) : 5;
+  int bhi = fb ? std::atoi(fb) : 8, blo = fb ? std::atoi(fb) : 5;
+  if (forced_bits > 0) bhi = blo = forced_bits;
   for (int b = bhi; b >= blo; --b) {
     int S = forced_slices > 0 ? forced_slices : (need - 1 + b - 1) / b;
     S = std::max(S, 2);
@@ -936,11 +939,11 @@ struct SplitDev {
 static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                               const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                               const std::vector<int64_t> &c_off, bool cplx, int forced_slices, double tol,
-                              const std::vector<int32_t> *blk_ldc, SplitWork &w) {
+                              const std::vector<int32_t> *blk_ldc, SplitWork &w, int forced_bits = 0) {
   SplitResult res;
   const int64_t nb = (int64_t)blk_M.size();
   const int cm = cplx ? 2 : 1;
-  DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices);
+  DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices, forced_bits);
   const int S = dp.nslices, b = dp.bits;
   const int kchunk = kchunk_of(b, S);
   w.S = S;
@@ -1162,6 +1165,86 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
   put(d.tiles, w.tiles.data(), w.tiles.size() * sizeof(SplitTile));
   launch_split(ctx, w, cplx, d, A, B, C, err);
   return res;
+}
+
+// Digit widths b whose plan meets `tol` (with `forced_slices` digits when
+// that is set): the candidates an autotuner times.
+std::vector<int> split_candidate_bits(double tol, int forced_slices) {
+  if (!(tol > 0)) tol = 1e-12;
+  const int need = (int)std::ceil(-std::log2(tol)) + 8;
+  std::vector<int> out;
+  for (int b = 8; b >= 5; --b) {
+    int S = forced_slices > 0 ? forced_slices : (need - 1 + b - 1) / b;
+    S = std::max(S, 2);
+    if (S > 8 || kchunk_of(b, S) < TKS) continue;
+    out.push_back(b);
+  }
+  return out;
+}
+
+// A planned split product that can be launched many times: its work lists,
+// exponent arrays and digit arena are plain device allocations owned by the
+// handle, so their addresses stay fixed (a CUDA graph can replay the launch).
+struct SplitPlanHandle {
+  SplitWork w;
+  SplitDev d;
+  bool cplx = false;
+  SplitResult res;
+  std::vector<void *> owned;
+};
+
+SplitPlanHandle *split_plan_create(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                                   const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                                   const std::vector<int64_t> &c_off, const std::vector<int32_t> &blk_ldc,
+                                   bool cplx, int forced_slices, double tol, int bits, SplitResult *res) {
+  std::unique_ptr<SplitPlanHandle> h(new SplitPlanHandle);
+  h->cplx = cplx;
+  h->res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, &blk_ldc, h->w, bits);
+  if (res) *res = h->res;
+  if (h->w.tiles.empty()) return h.release();
+  try {
+    auto own = [&](size_t bytes) -> void * {
+      void *p = nullptr;
+      cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+      if (e != cudaSuccess)
+        fail(e == cudaErrorMemoryAllocation ? QS_ERR_OOM : QS_ERR_CUDA, "split plan: cudaMalloc(%zu): %s", bytes,
+             cudaGetErrorString(e));
+      h->owned.push_back(p);
+      return p;
+    };
+    auto put = [&](const auto &v) {
+      using T = typename std::decay_t<decltype(v)>::value_type;
+      T *p = static_cast<T *>(own(v.size() * sizeof(T)));
+      if (!v.empty()) QS_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+      return p;
+    };
+    SplitDev &d = h->d;
+    d.pairs = put(h->w.sp);
+    d.rt = put(h->w.rt);
+    d.ct = put(h->w.ct);
+    d.xt = put(h->w.xt);
+    d.at = put(h->w.at);
+    d.bt = put(h->w.bt);
+    d.tiles = put(h->w.tiles);
+    d.E = static_cast<int *>(own((size_t)h->w.nE * sizeof(int)));
+    d.F = static_cast<int *>(own((size_t)h->w.nF * sizeof(int)));
+    d.arena = static_cast<uint8_t *>(own((size_t)h->w.arena));
+  } catch (...) {
+    for (void *p : h->owned) cudaFree(p);
+    throw;
+  }
+  return h.release();
+}
+
+void split_plan_launch(Ctx *ctx, SplitPlanHandle *h, const double *A, const double *B, double *C) {
+  if (!h->w.tiles.empty()) launch_split(ctx, h->w, h->cplx, h->d, A, B, C, ctx->d_err);
+}
+
+// The caller makes sure no launch of the handle is still running.
+void split_plan_destroy(SplitPlanHandle *h) {
+  if (!h) return;
+  for (void *p : h->owned) cudaFree(p);
+  delete h;
 }
 
 }  // namespace qs

@@ -4,12 +4,14 @@
 // factors, grouped by output block, executed in one grouped launch.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 
 #include "qs_internal.h"
 #include "qs_plan.h"
 #include "qs_split.h"
+#include "qs_grouped.h"
 
 namespace qs {
 void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
@@ -22,22 +24,9 @@ using namespace qs;
 
 namespace qs {
 
-// Host-side form of a validated pair list: device descriptors per pair, the
-// output blocks (runs of equal c_blk) with their shapes, and per-pair element
-// ranges of A, B and C.
-struct GroupedPlan {
-  bool cplx = false;
-  std::vector<PairDesc> pairs;
-  std::vector<int64_t> grp;  // pairs of block g: [grp[g], grp[g+1])
-  std::vector<int32_t> bM, bN, bldc;
-  std::vector<int64_t> coff;
-  std::vector<int64_t> a_end, b_end;  // one past the last element a pair reads
-  double flops = 0, bytes = 0;
-};
-
 // Validates the pair list.  When the element counts are known (host form),
 // every access is checked against them.
-static GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elems, int64_t c_elems) {
+GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elems, int64_t c_elems) {
   if (!pl) fail(QS_ERR_ARG, "null pair list");
   const int64_t n = pl->npairs;
   if (n < 0) fail(QS_ERR_ARG, "negative pair count");
@@ -204,7 +193,11 @@ static void grouped_host(Ctx *c, const qs_pair_list *pl, const double *A, int64_
   const size_t nb = g.bM.size();
   // chunk boundaries (in output blocks) by cumulative input bytes
   const double in_bytes = 8.0 * es * double(a_elems + b_elems);
-  const int nchunk = (int)std::max<double>(1.0, std::min<double>(8.0, std::floor(in_bytes / (128.0 * (1 << 20)))));
+  // QS_HOST_CHUNK_MB / QS_HOST_MAX_CHUNKS override the chunking for tuning
+  const char *e_mb = std::getenv("QS_HOST_CHUNK_MB"), *e_max = std::getenv("QS_HOST_MAX_CHUNKS");
+  const double chunk_bytes = (e_mb ? std::atof(e_mb) : 64.0) * (1 << 20);
+  const double max_chunks = e_max ? std::atof(e_max) : 16.0;
+  const int nchunk = (int)std::max<double>(1.0, std::min<double>(max_chunks, std::floor(in_bytes / chunk_bytes)));
   std::vector<size_t> cut{0};
   if (nb) {
     std::vector<double> w(nb, 0.0);
@@ -260,7 +253,10 @@ static void grouped_host(Ctx *c, const qs_pair_list *pl, const double *A, int64_
     QS_CUDA(cudaEventRecord(ready, c->stream));
     QS_CUDA(cudaStreamWaitEvent(c->h2d, ready, 0));
     QS_CUDA(cudaStreamWaitEvent(c->d2h, ready, 0));
+    // all copies in are queued first: the copy stream never waits for the
+    // host to plan a chunk
     int64_t wa = 0, wb = 0, wc = 0;
+    std::vector<cudaEvent_t> in(nch);
     for (size_t k = 0; k < nch; ++k) {
       if (ahi[k] > wa) {
         QS_CUDA(cudaMemcpyAsync(dA + wa * es, A + wa * es, (size_t)(ahi[k] - wa) * eb, cudaMemcpyHostToDevice, c->h2d));
@@ -270,9 +266,11 @@ static void grouped_host(Ctx *c, const qs_pair_list *pl, const double *A, int64_
         QS_CUDA(cudaMemcpyAsync(dB + wb * es, B + wb * es, (size_t)(bhi[k] - wb) * eb, cudaMemcpyHostToDevice, c->h2d));
         wb = bhi[k];
       }
-      cudaEvent_t in = event();
-      QS_CUDA(cudaEventRecord(in, c->h2d));
-      QS_CUDA(cudaStreamWaitEvent(c->stream, in, 0));
+      in[k] = event();
+      QS_CUDA(cudaEventRecord(in[k], c->h2d));
+    }
+    for (size_t k = 0; k < nch; ++k) {
+      QS_CUDA(cudaStreamWaitEvent(c->stream, in[k], 0));
       grouped_exec(c, g, cut[k], cut[k + 1], dA, dB, dC, opts, &sr, nullptr, 0, nullptr);
       if (ordered && k + 1 < nch && chi[k] > wc) {
         cudaEvent_t done = event();

@@ -1,0 +1,28 @@
+// Validated form of a qs_pair_list, shared by the one-shot grouped entry
+// points (qs_grouped.cpp) and the reusable plans (qs_plan_api.cpp).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "qs_internal.h"
+
+namespace qs {
+
+// Device descriptors per pair, the output blocks (runs of equal c_blk) with
+// their shapes, and per-pair element ranges of A and B.
+struct GroupedPlan {
+  bool cplx = false;
+  std::vector<PairDesc> pairs;
+  std::vector<int64_t> grp;  // pairs of block g: [grp[g], grp[g+1])
+  std::vector<int32_t> bM, bN, bldc;
+  std::vector<int64_t> coff;
+  std::vector<int64_t> a_end, b_end;  // one past the last element a pair reads
+  double flops = 0, bytes = 0;
+};
+
+// Validates the pair list.  When the element counts are known (>= 0), every
+// access is checked against them.
+GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elems, int64_t c_elems);
+
+}  // namespace qs

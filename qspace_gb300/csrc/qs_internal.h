@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <deque>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -54,6 +55,20 @@ struct Ctx {
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
   void *ensure_scratch(size_t bytes);
+  // page-locked staging ring for work-list uploads: copies from it are
+  // asynchronous, so the host plans the next call while the device works
+  char *stage_buf = nullptr;      // host address
+  char *stage_dev = nullptr;      // the same memory as the device sees it
+  size_t stage_cap = 0;
+  int64_t stage_head = 0;  // virtual write position (grows monotonically)
+  struct StageMark {
+    cudaEvent_t ev;
+    int64_t start;
+  };
+  std::deque<StageMark> stage_q;    // copies in flight, oldest first
+  std::vector<cudaEvent_t> stage_ev;  // recycled events
+  void stage_upload(void *dst, const void *src, size_t bytes);
+  void destroy_staging();
   // copy streams of the pipelined host-buffer path (created on first use)
   cudaStream_t h2d = nullptr, d2h = nullptr;
   void ensure_copy_streams();
@@ -125,6 +140,8 @@ void launch_block_nonzero(Ctx *ctx, const int64_t *d_offs, const int64_t *d_size
                           int64_t nblk, const double *data, int is_complex,
                           int *d_flags);
 void launch_widen(Ctx *ctx, const double *in, double *out, int64_t n);
+// copies `bytes` from mapped page-locked host memory to device memory with a kernel
+void launch_stage_copy(Ctx *ctx, const void *src, void *dst, size_t bytes);
 
 // qs_linalg.cu
 void destroy_solver(Ctx *ctx);
@@ -145,9 +162,7 @@ void dev_free(Ctx *ctx, void *p);
 template <class T>
 T *dev_upload(Ctx *ctx, const std::vector<T> &v) {
   T *p = dev_alloc<T>(ctx, v.size());
-  if (!v.empty())
-    QS_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T),
-                            cudaMemcpyHostToDevice, ctx->stream));
+  if (!v.empty()) ctx->stage_upload(p, v.data(), v.size() * sizeof(T));
   return p;
 }
 

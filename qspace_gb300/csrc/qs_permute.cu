@@ -7,6 +7,8 @@
 // writes its chunk in output order (coalesced stores) and gathers the inputs
 // through the permuted strides.  When the permutation keeps the first leg in
 // place the gathers are unit-stride runs as well.
+#include <algorithm>
+
 #include "qs_internal.h"
 
 namespace qs {
@@ -91,6 +93,28 @@ void launch_block_nonzero(Ctx *ctx, const int64_t *d_offs, const int64_t *d_size
   if (nblk <= 0) return;
   block_nonzero_kernel<<<(unsigned)nblk, 128, 0, ctx->stream>>>(d_offs, d_sizes, data,
                                                                  is_complex, d_flags);
+  QS_LAUNCHED(ctx);
+}
+
+// Work-list upload from the page-locked staging ring: the SMs read the
+// mapped host memory, so these small copies never queue on the copy engines
+// behind bulk operand transfers.
+__global__ void stage_copy_kernel(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst, size_t bytes) {
+  const size_t n16 = bytes / 16;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (size_t i = t0; i < n16; i += stride)
+    reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+  const size_t t = n16 * 16 + t0;  // the last bytes % 16
+  if (t < bytes) dst[t] = src[t];
+}
+
+void launch_stage_copy(Ctx *ctx, const void *src, void *dst, size_t bytes) {
+  if (!bytes) return;
+  const size_t n16 = std::max<size_t>(bytes / 16, 1);
+  const int grid = (int)std::min<size_t>((n16 + 255) / 256, (size_t)std::max(ctx->num_sms, 1) * 4);
+  stage_copy_kernel<<<grid, 256, 0, ctx->stream>>>(static_cast<const uint8_t *>(src), static_cast<uint8_t *>(dst),
+                                                   bytes);
   QS_LAUNCHED(ctx);
 }
 

@@ -161,6 +161,7 @@ void qs_server_destroy(qs_server *s) {
     destroy_solver(c.get());
     cudaFree(c->d_err);
     c->destroy_copy_streams();
+    c->destroy_staging();
     cudaStreamDestroy(c->stream);
   }
   delete s;

@@ -44,4 +44,15 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs,
                              int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
                              uint8_t *scratch, size_t cap, int *err);
 
+// Reusable split plans (stable device addresses, for CUDA graph replay).
+struct SplitPlanHandle;
+std::vector<int> split_candidate_bits(double tol, int forced_slices);
+// bits = 0: the cost model picks the digit width
+SplitPlanHandle *split_plan_create(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                                   const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                                   const std::vector<int64_t> &c_off, const std::vector<int32_t> &blk_ldc,
+                                   bool cplx, int forced_slices, double tol, int bits, SplitResult *res);
+void split_plan_launch(Ctx *ctx, SplitPlanHandle *h, const double *A, const double *B, double *C);
+void split_plan_destroy(SplitPlanHandle *h);
+
 }  // namespace qs

@@ -162,12 +162,50 @@ class DeviceBatch:
         if stats is not None:
             stats.update(st.as_dict())
 
+    def plan(self, prec="split", nslices=0, tol=1e-12, autotune=False, graph=True) -> "GroupedPlan":
+        return GroupedPlan(self.pk, prec, nslices, tol, autotune, graph, self.ctx)
+
+    def run_plan(self, plan: "GroupedPlan", stats: dict | None = None):
+        plan.run(self.dA.data_ptr(), self.dB.data_ptr(), self.dC.data_ptr(), stats)
+
     def result(self) -> list:
         self.ctx.sync()
         c = self.dC.cpu().numpy()
         if self.pk.cplx:
             c = c.view(np.complex128)
         return self.pk.unpack_c(c)
+
+
+class GroupedPlan:
+    """A reusable plan (qs_grouped_plan_*) over one pair list: planned once,
+    replayed as a CUDA graph; ``autotune`` times the digit widths on the
+    first run."""
+
+    def __init__(self, pk: Packed, prec="split", nslices=0, tol=1e-12, autotune=False, graph=True,
+                 ctx: Context | None = None):
+        self.pk = pk
+        self.ctx = ctx or default_context()
+        flags = (_capi.QS_FLAG_AUTOTUNE if autotune else 0) | (0 if graph else _capi.QS_FLAG_NO_GRAPH)
+        self.pl = pk.pair_list()
+        h = C.c_void_p()
+        check(self.ctx.lib.qs_grouped_plan_create(self.ctx.h, C.byref(self.pl),
+                                                  C.byref(make_opts(prec, nslices, tol, flags)), C.byref(h)))
+        self.h = h
+
+    def run(self, dA: int, dB: int, dC: int, stats: dict | None = None):
+        st = Stats()
+        check(self.ctx.lib.qs_grouped_plan_run(self.h, C.c_void_p(dA), C.c_void_p(dB), C.c_void_p(dC),
+                                               C.byref(st)))
+        if stats is not None:
+            stats.update(st.as_dict())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.qs_grouped_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def run_device(w: dict, prec="fp64", nslices=0, tol=1e-12, ctx=None, stats=None) -> list:
