@@ -365,11 +365,12 @@ int64_t contract_footprint(const QMeta &Am, const QMeta &Bm, const char *ia, con
   if (pl.la.permute || (pl.C.cplx && !Am.cplx)) fp += Am.nelem * es * 2;
   if (pl.lb.permute || (pl.C.cplx && !Bm.cplx)) fp += Bm.nelem * es * 2;
   if (opts && opts->prec == QS_PREC_SPLIT) {
-    // at most 8 BF16 digits of every pair operand, padded to 128x32 / 64x32
+    // at most 8 BF16 digits of every pair operand in the real form (2M x 2K
+    // and 2K x N when complex), padded to 128 x 32 / 32 x 32 tiles
     const int64_t cm = pl.C.cplx ? 2 : 1;
     for (const PairDesc &d : pl.pairs) {
-      const int64_t Mr = d.M * cm, Kr = std::max<int64_t>(d.K * cm, 1);
-      const int64_t rows = (Mr + 127) / 128 * 128 + (d.N + 63) / 64 * 64;
+      const int64_t Kr = std::max<int64_t>(d.K * cm, 1);
+      const int64_t rows = (d.M * cm + 127) / 128 * 128 + (d.N + 31) / 32 * 32;
       fp += rows * ((Kr + 31) / 32 * 32) * 2 * 8;
     }
   }

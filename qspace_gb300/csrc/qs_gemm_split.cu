@@ -42,8 +42,8 @@
 // layout (8 rows x 16 bytes per core matrix); the GEMM kernel then moves
 // whole digit tiles with 1-D TMA bulk copies (cp.async.bulk + mbarrier
 // transaction counts) into a multi-stage shared-memory ring.  Warp roles:
-// warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, warps 2..9 =
-// epilogue (two per TMEM lane quarter).  Every mbarrier wait is bounded; on
+// warp 0 = TMA producer, warp 1 = TMEM owner and MMA issuer, the other
+// warps = epilogue (EPI_WARPS / 4 per TMEM lane quarter).  Every mbarrier wait is bounded; on
 // timeout the kernel records an error code, stops issuing work, waits a
 // bounded time for what is in flight, frees its TMEM and returns.
 #include <cuda_bf16.h>
@@ -70,6 +70,8 @@ constexpr int EMPTY_EXP = -30000;
 constexpr int SMEM_HDR = 1024;
 constexpr int SMEM_LIMIT = 227 * 1024;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;  // bounded mbarrier polls (seconds)
+constexpr int EPI_WARPS = 16;     // epilogue warps (4 per TMEM lane quarter)
+constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;
 
 struct SplitPair {
   int64_t a_off, b_off;    // element offsets of op(A)/op(B) storage
@@ -511,39 +513,33 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // Recombination without the FP64 pipe.  The S accumulators hold exact
 // integers (|acc_g| <= 2^24); their weighted sum
 //   V = sum_g acc_g 2^(b(S-1-g) - r)
-// is formed in int64 (r low bits of the smallest group are rounded away so
-// that V and the sum over accumulator chunks keep headroom), then turned into
-// an FP64 value V * 2^scale by integer bit assembly (round to nearest even).
-template <int S, int W>
-__device__ __forceinline__ long long combine_groups(const float (&acc)[S][W], int cc, int b, int r) {
-  long long V = 0;
-#pragma unroll
-  for (int g = 0; g < S; ++g) {
-    const long long a = (long long)__float2int_rn(acc[g][cc]);
-    const int sh = b * (S - 1 - g) - r;
-    if (sh >= 0) V += a << sh;
-    else V += (a + (1LL << (-sh - 1))) >> (-sh);
-  }
-  return V;
+// is formed in 64-bit fixed point (r low bits of the smallest groups are
+// rounded away so that V and the sum over accumulator chunks keep headroom),
+// then turned into an FP64 value V * 2^scale by integer bit assembly (round
+// to nearest even).
+// Wrapping 32 x 32 -> 64-bit multiply-add: acc + (int64)a * m (mod 2^64).
+__device__ __forceinline__ unsigned long long mad_wide(int a, int m, unsigned long long acc) {
+  unsigned long long d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(m), "l"(acc));
+  return d;
 }
+
+// How accumulator group g enters the fixed-point sum V = sum_g acc_g 2^sh_g
+// (sh_g = b(S-1-g) - r): sh >= 32 adds acc * 2^(sh-32) to the high 32-bit
+// word, 0 <= sh <= 30 adds acc * 2^sh to the low 64-bit word, sh < 0 adds
+// acc / 2^-sh rounded.  All words wrap; V itself fits in int64, so
+// V = hi * 2^32 + lo (mod 2^64) is exact.
+struct GroupWeight {
+  int mh, ml, rs;
+};
 
 __device__ __forceinline__ double fixed_to_double(long long V, int scale) {
   if (V == 0) return 0.0;
-  const unsigned long long sgn = (unsigned long long)V & 0x8000000000000000ull;
-  const unsigned long long a = V < 0 ? (unsigned long long)(-V) : (unsigned long long)V;
-  const int lz = __clzll(a);
-  const unsigned long long m = a << lz;  // leading one at bit 63
-  unsigned long long mant = m >> 11;
-  const unsigned long long rem = m & 0x7FFull;
-  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
-  int e = 63 - lz + scale;  // value = 1.f * 2^e
-  if (mant >> 53) {
-    mant >>= 1;
-    ++e;
-  }
-  const int be = e + 1023;
-  if (be <= 0 || be >= 2047) return ldexp((double)V, scale);  // subnormal / overflow: rare path
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  const double d = __ll2double_rn(V);
+  const long long bits = __double_as_longlong(d);
+  const int e = (int)((bits >> 52) & 0x7ff) + scale;
+  if (e <= 0 || e >= 2047) return ldexp(d, scale);
+  return __longlong_as_double(bits + ((long long)scale << 52));
 }
 
 // Chunking rule shared by the host and the MMA issuer: a new chunk starts
@@ -561,7 +557,7 @@ __device__ __forceinline__ int kblock_depth(int Kr, int kb) { return min(TKS, Kr
 __device__ __forceinline__ int tile_of(int r, int c, int G) { return r * G + ((r & 1) ? (G - 1 - c) : c); }
 
 template <int S>
-__global__ void __launch_bounds__(320, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
 gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPair *__restrict__ pairs,
                   const uint8_t *__restrict__ arena, const int *__restrict__ E,
                   const int *__restrict__ F, double *__restrict__ C, int b, int nstages,
@@ -589,7 +585,7 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&acc_full[s], 1);
-      mbar_init(&acc_empty[s], 8);  // one arrive per epilogue warp
+      mbar_init(&acc_empty[s], EPI_WARPS);  // one arrive per epilogue warp
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -715,12 +711,12 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       }
     }
   } else {
-    // ------------------------------------------- epilogue (warps 2..9)
-    // warp w reads TMEM lane quarter w % 4; warps 2..5 take columns 0..15,
-    // warps 6..9 columns 16..31 of each tile.
+    // ------------------------------------------- epilogue (warps 2..)
+    // warp w reads TMEM lane quarter w % 4; each run of four warps covers
+    // all quarters for CW consecutive columns of the tile.
     const int q = warp & 3;
-    constexpr int CW = TNS / 2;
-    const int cbase = warp < 6 ? 0 : CW;
+    constexpr int CW = TNS * 4 / EPI_WARPS;
+    const int cbase = ((warp - 2) >> 2) * CW;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
     const int scale_b = -b * (S + 1);
     int u = 0;
@@ -731,9 +727,28 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       const SplitTile T = tiles[ti];
       const int i_glob = T.mt * TMS + q * 32 + lane;
       const bool rv = i_glob < T.Mr;
-      long long V[CW];
+      // exponents of this thread's outputs, fetched now so that their load
+      // latency hides behind the accumulation
+      const int j0 = T.nt * TNS + cbase;
+      const int Ei = rv ? E[T.eoff + i_glob] : 0;
+      int Fj[CW];
 #pragma unroll
-      for (int jj = 0; jj < CW; ++jj) V[jj] = 0;
+      for (int jj = 0; jj < CW; ++jj) Fj[jj] = (rv && j0 + jj < T.N) ? F[T.foff + j0 + jj] : 0;
+      GroupWeight gw[S];
+#pragma unroll
+      for (int g = 0; g < S; ++g) {
+        const int sh = b * (S - 1 - g) - T.rshift;
+        gw[g].mh = sh >= 32 ? (1 << (sh - 32)) : 0;
+        gw[g].ml = (sh >= 0 && sh <= 30) ? (1 << sh) : 0;
+        gw[g].rs = sh < 0 ? -sh : 0;
+      }
+      unsigned long long Vl[CW];
+      unsigned int Vh[CW];
+#pragma unroll
+      for (int jj = 0; jj < CW; ++jj) {
+        Vl[jj] = 0;
+        Vh[jj] = 0;
+      }
       for (int ch = 0; ch < T.nchunk; ++ch, ++u) {
         // one lane polls; the warp proceeds together (tcgen05.ld is .aligned)
         int w = 1;
@@ -749,7 +764,23 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
           for (int g = 0; g < S; ++g) tmem_ld4(set_base + (uint32_t)(g * TNS + cbase + c4), acc[g]);
           tmem_wait_ld();
 #pragma unroll
-          for (int cc = 0; cc < 4; ++cc) V[c4 + cc] += combine_groups<S, 4>(acc, cc, b, T.rshift);
+          for (int g = 0; g < S; ++g) {
+            const GroupWeight w = gw[g];
+            if (w.rs == 0) {
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) {
+                const int a = __float2int_rn(acc[g][cc]);
+                Vh[c4 + cc] += (unsigned int)a * (unsigned int)w.mh;
+                Vl[c4 + cc] = mad_wide(a, w.ml, Vl[c4 + cc]);
+              }
+            } else {
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) {
+                const int a = __float2int_rn(acc[g][cc]);
+                Vl[c4 + cc] = mad_wide((a + (1 << (w.rs - 1))) >> w.rs, 1, Vl[c4 + cc]);
+              }
+            }
+          }
         }
         tc_fence_before();
         __syncwarp();
@@ -757,12 +788,14 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       }
       if (!ok) break;
       if (rv) {
-        const int Ei = E[T.eoff + i_glob];
         double *crow = C + T.c_off + (int64_t)i_glob;
 #pragma unroll
         for (int jj = 0; jj < CW; ++jj) {
-          const int j = T.nt * TNS + cbase + jj;
-          if (j < T.N) crow[(int64_t)j * T.ldc] = fixed_to_double(V[jj], Ei + F[T.foff + j] + T.rshift + scale_b);
+          const int j = j0 + jj;
+          if (j < T.N) {
+            const long long V = (long long)(((unsigned long long)Vh[jj] << 32) + Vl[jj]);
+            crow[(int64_t)j * T.ldc] = fixed_to_double(V, Ei + Fj[jj] + T.rshift + scale_b);
+          }
         }
       }
     }
@@ -820,7 +853,7 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
   QS_CUDA(cudaFuncSetAttribute(gemm_split_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   ctx->mark(1);
   const int grid = std::min(ntiles, std::max(ctx->num_sms, 1));
-  gemm_split_kernel<S><<<grid, 320, sm, st>>>(d_tiles, ntiles, d_pairs, arena, dE, dF, C, b, nst, kchunk,
+  gemm_split_kernel<S><<<grid, GEMM_THREADS, sm, st>>>(d_tiles, ntiles, d_pairs, arena, dE, dF, C, b, nst, kchunk,
                                               err);
   QS_LAUNCHED(ctx);
   ctx->mark(2);
@@ -1025,7 +1058,12 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
     // nchunk * 2^(24.2 + b(S-1) - r) < 2^63
     int lg = 0;
     while ((1 << lg) < nchunk) ++lg;
-    const int rshift = std::max(0, 25 + b * (S - 1) + lg - 63);
+    int rshift = std::max(0, 25 + b * (S - 1) + lg - 63);
+    // the epilogue adds each group with a shift of at most 30 into its low
+    // 64-bit word or of at least 32 into its high 32-bit word: no group may
+    // land exactly on bit 31
+    for (int t = 0; t < S; ++t)
+      if (b * (S - 1 - t) - rshift == 31) ++rshift;
     const int MT = (blk_M[g] * cm + TMS - 1) / TMS, NT = (blk_N[g] + TNS - 1) / TNS;
     for (int nt = 0; nt < NT; ++nt)
       for (int mt = 0; mt < MT; ++mt) {
