@@ -126,10 +126,9 @@ __host__ __device__ inline Factor make_factor(double f) {
   return r;
 }
 
-// Balanced digits of N = round(x f 2^(b*S - E)); |x f| < 2^E is guaranteed
-// by construction of E.  Integer operations only.
-template <int S>
-__device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S], const Factor &F) {
+// N = round(x f 2^(b*S - E)); |x f| < 2^E is guaranteed by construction of
+// E, so |N| <= 2^(bS) (b*S <= 62).  Integer operations only.
+__device__ __forceinline__ long long scaled_int(double x, int E, int bS, const Factor &F) {
   const long long bits = __double_as_longlong(x);
   int be = (int)((bits >> 52) & 0x7ff);
   unsigned long long mant = bits & 0xFFFFFFFFFFFFFull;
@@ -139,7 +138,7 @@ __device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S],
   if (mant != 0 && F.fe > -100000) {
     if (F.fm == 0) {
       // N = round(mant * 2^shift)
-      const int shift = be - 1075 + b * S - E;
+      const int shift = be - 1075 + bS - E;
       if (shift >= 0) N = (long long)(mant << min(shift, 62));
       else if (shift > -62) N = (long long)((mant + (1ull << (-shift - 1))) >> (-shift));
     } else {
@@ -148,33 +147,46 @@ __device__ __forceinline__ void make_digits(double x, int E, int b, int (&d)[S],
       // < 2^-63, far below the 2^-(bS) of the digits), then the rounding shift
       // (|x f| < 2^E holds by construction of E)
       const unsigned long long P = __umul64hi(mant << 11, F.fm << 11);
-      const int shift = be - 1075 + F.fe + 42 + b * S - E;
+      const int shift = be - 1075 + F.fe + 42 + bS - E;
       if (shift >= 0) N = (long long)(P << min(shift, 62));
       else if (shift > -64) N = (long long)((P >> (-shift - 1)) + 1 >> 1);
       neg ^= F.neg;
     }
     if (neg) N = -N;
   }
-  const long long half = 1LL << (b - 1), mask = (1LL << b) - 1;
-#pragma unroll
-  for (int t = S - 1; t >= 1; --t) {
-    const long long r = ((N + half) & mask) - half;
-    d[t] = (int)r;
-    N = (N - r) >> b;
-  }
-  d[0] = (int)N;
+  return N;
 }
 
-// BF16 bits of a small integer |d| <= 2^22 (digits are |d| <= 256, nine
-// significant bits at most, so the BF16 value is exact): the FP32 value is
-// formed with the 1.5*2^23 offset (one integer add, one FP32 add), its upper
-// half is the BF16 pattern.  Avoids the int-to-float conversion unit.
-__device__ __forceinline__ uint32_t bf16_bits(int d) {
-  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
-  return __float_as_uint(f) >> 16;
+// Balanced base-2^B digits of N as floats (exact small integers):
+//   N = sum_t d_t 2^(B(S-1-t)),  d_t in [-2^(B-1), 2^(B-1)) for t >= 1,
+//   |d_0| <= 2^B.
+// With H = sum_{t>=1} 2^(B-1) 2^(B(S-1-t)), the low B(S-1) bits of M = N + H
+// are the base-2^B digits d_t + 2^(B-1), and d_0 = floor(M / 2^(B(S-1))).
+// Each digit is a funnel shift, one logic op (mask | 2^23 exponent) and one
+// FP32 subtraction; all values are exact in BF16 (at most 8 significant bits).
+template <int S, int B>
+__device__ __forceinline__ void digits_f(long long N, float (&d)[S]) {
+  constexpr long long HALF = 1LL << (B - 1);
+  constexpr unsigned MASK = (1u << B) - 1;
+  long long H = 0;
+#pragma unroll
+  for (int t = 1; t < S; ++t) H = (H << B) + HALF;
+  const long long M = N + H;
+  const unsigned lo = (unsigned)M, hi = (unsigned)((unsigned long long)M >> 32);
+#pragma unroll
+  for (int t = 1; t < S; ++t) {
+    const int sh = B * (S - 1 - t);
+    const unsigned w = sh >= 32 ? (hi >> (sh - 32)) : (sh == 0 ? lo : __funnelshift_r(lo, hi, sh));
+    d[t] = __int_as_float((int)((w & MASK) | 0x4B000000u)) - (8388608.0f + (float)HALF);
+  }
+  const int d0 = (int)(M >> (B * (S - 1)));
+  d[0] = __int_as_float(0x4B400000 + d0) - 12582912.0f;
 }
-__device__ __forceinline__ uint32_t pack_bf16(int lo, int hi) {
-  return (bf16_bits(hi) << 16) | bf16_bits(lo);
+
+// Two BF16 values packed as (lo, hi) halves of a 32-bit word.
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
 }
 
 // --------------------------------------------------------- exponent passes
@@ -295,17 +307,11 @@ __global__ void fill_int_kernel(int *p, int64_t n, int v) {
 // ------------------------------------------------------------ slicing
 // A~ digit tile (mt, kb): 128 rows x 32 k, core matrix (row group g, k core c)
 // at byte ((g*4 + c)*128), row r%8 at +16*(r%8), k%8 at +2*(k%8).
-template <bool CPLX, int S>
-__global__ void __launch_bounds__(256)
-slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-               const double *__restrict__ A, const int *__restrict__ E,
-               uint8_t *__restrict__ arena, int b) {
-  const int4 tk = tasks[blockIdx.x];  // (pair, mt, kb, -)
-  const SplitPair P = pairs[tk.x];
-  const int mt = tk.y, kb = tk.z;
+template <bool CPLX, int S, int B>
+__device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb, const double *__restrict__ A,
+                                             const int *__restrict__ E, uint8_t *__restrict__ tile) {
   const bool ta = P.trans & 1, ca = P.trans & 4;
   const Factor Fa{P.fm, P.fe, P.fneg != 0};
-  uint8_t *tile = arena + P.as_off + ((int64_t)(mt * P.KB + kb) * S) * A_DIGIT_BYTES;
   if constexpr (CPLX) {
     // one task = one complex row m (real rows 2m, 2m+1 of A~) x 4 complex k:
     // the digits of re and im are cut once and placed as
@@ -326,14 +332,13 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
           re = a.x;
           im = ca ? -a.y : a.y;
         }
-        int dr[S], di[S];
-        make_digits<S>(re, Ei, b, dr, Fa);
-        make_digits<S>(im, Ei, b, di, Fa);
+        float dr[S], di[S];
+        digits_f<S, B>(scaled_int(re, Ei, B * S, Fa), dr);
+        digits_f<S, B>(scaled_int(im, Ei, B * S, Fa), di);
 #pragma unroll
         for (int t = 0; t < S; ++t) {
-          const uint32_t hr = bf16_bits(dr[t]), hi = bf16_bits(di[t]);
-          p0[t][j] = ((hi ^ 0x8000u) << 16) | hr;  // ( re, -im )
-          p1[t][j] = (hr << 16) | hi;              // ( im,  re )
+          p0[t][j] = pack2(dr[t], -di[t]);  // ( re, -im )
+          p1[t][j] = pack2(di[t], dr[t]);   // ( im,  re )
         }
       }
       const int r0 = 2 * ml, r1 = r0 + 1;
@@ -346,46 +351,56 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
       }
     }
   } else {
-  for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
-    const int r = w % TMS, q = w / TMS;
-    const int rr = mt * TMS + r;
-    const bool rv = rr < P.Mr;
-    const int Ei = rv ? E[P.eoff + rr] : 0;
-    uint32_t pk[S][4];
+    for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
+      const int r = w % TMS, q = w / TMS;
+      const int rr = mt * TMS + r;
+      const bool rv = rr < P.Mr;
+      const int Ei = rv ? E[P.eoff + rr] : 0;
+      uint32_t pk[S][4];
 #pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      int dd[2][S];
+      for (int e = 0; e < 8; e += 2) {
+        float dd[2][S];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int kk = kb * TKS + q * 8 + e + h;
-        double v = 0.0;
-        if (rv && kk < P.Kr)
-          v = A[P.a_off + (ta ? (int64_t)kk + (int64_t)rr * P.lda : (int64_t)rr + (int64_t)kk * P.lda)];
-        make_digits<S>(v, Ei, b, dd[h], Fa);
+        for (int h = 0; h < 2; ++h) {
+          const int kk = kb * TKS + q * 8 + e + h;
+          double v = 0.0;
+          if (rv && kk < P.Kr)
+            v = A[P.a_off + (ta ? (int64_t)kk + (int64_t)rr * P.lda : (int64_t)rr + (int64_t)kk * P.lda)];
+          digits_f<S, B>(scaled_int(v, Ei, B * S, Fa), dd[h]);
+        }
+#pragma unroll
+        for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(dd[0][t], dd[1][t]);
       }
+      uint8_t *dst = tile + ((r >> 3) * 4 + q) * 128 + (r & 7) * 16;
 #pragma unroll
-      for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack_bf16(dd[0][t], dd[1][t]);
+      for (int t = 0; t < S; ++t)
+        *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
     }
-    uint8_t *dst = tile + ((r >> 3) * 4 + q) * 128 + (r & 7) * 16;
-#pragma unroll
-    for (int t = 0; t < S; ++t)
-      *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
-  }
   }
 }
 
-// B~ digit tile (nt, kb): 64 columns x 32 k, same core-matrix layout with the
-// column index in the role of the row.
 template <bool CPLX, int S>
 __global__ void __launch_bounds__(256)
-slice_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-               const double *__restrict__ B, const int *__restrict__ F,
+slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
+               const double *__restrict__ A, const int *__restrict__ E,
                uint8_t *__restrict__ arena, int b) {
-  const int4 tk = tasks[blockIdx.x];
+  const int4 tk = tasks[blockIdx.x];  // (pair, mt, kb, -)
   const SplitPair P = pairs[tk.x];
-  const int nt = tk.y, kb = tk.z;
+  uint8_t *tile = arena + P.as_off + ((int64_t)(tk.y * P.KB + tk.z) * S) * A_DIGIT_BYTES;
+  switch (b) {  // the host admits b = 5..8 only
+    case 5: slice_a_tile<CPLX, S, 5>(P, tk.y, tk.z, A, E, tile); break;
+    case 6: slice_a_tile<CPLX, S, 6>(P, tk.y, tk.z, A, E, tile); break;
+    case 7: slice_a_tile<CPLX, S, 7>(P, tk.y, tk.z, A, E, tile); break;
+    default: slice_a_tile<CPLX, S, 8>(P, tk.y, tk.z, A, E, tile); break;
+  }
+}
+
+// B~ digit tile (nt, kb): 32 columns x 32 k, the same core-matrix layout
+// with the column index in the role of the row.
+template <bool CPLX, int S, int B>
+__device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb, const double *__restrict__ Bm,
+                                             const int *__restrict__ F, uint8_t *__restrict__ tile) {
   const bool tb = P.trans & 2, cb = P.trans & 8;
-  uint8_t *tile = arena + P.bs_off + ((int64_t)(nt * P.KB + kb) * S) * B_DIGIT_BYTES;
   for (int w = threadIdx.x; w < TNS * (TKS / 8); w += blockDim.x) {
     const int c = w % TNS, q = w / TNS;
     const int n = nt * TNS + c;
@@ -394,30 +409,52 @@ slice_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
     uint32_t pk[S][4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
-      int dd[2][S];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int kk = kb * TKS + q * 8 + e + h;
-        double v = 0.0;
-        if (nv && kk < P.Kr) {
-          if (CPLX) {
-            const int k = kk >> 1, kap = kk & 1;
-            const double2 x = reinterpret_cast<const double2 *>(B)[
-                P.b_off + (tb ? (int64_t)n + (int64_t)k * P.ldb : (int64_t)k + (int64_t)n * P.ldb)];
-            v = kap ? (cb ? -x.y : x.y) : x.x;
-          } else {
-            v = B[P.b_off + (tb ? (int64_t)n + (int64_t)kk * P.ldb : (int64_t)kk + (int64_t)n * P.ldb)];
-          }
+      float dd[2][S];
+      if constexpr (CPLX) {
+        // rows 2k, 2k+1 of B~ are (Re, Im) of one complex element
+        const int k = (kb * TKS + q * 8 + e) >> 1;
+        double re = 0.0, im = 0.0;
+        if (nv && 2 * k < P.Kr) {
+          const double2 x = reinterpret_cast<const double2 *>(Bm)[
+              P.b_off + (tb ? (int64_t)n + (int64_t)k * P.ldb : (int64_t)k + (int64_t)n * P.ldb)];
+          re = x.x;
+          im = cb ? -x.y : x.y;
         }
-        make_digits<S>(v, Fj, b, dd[h], Factor{0ull, 0, false});
+        digits_f<S, B>(scaled_int(re, Fj, B * S, Factor{0ull, 0, false}), dd[0]);
+        digits_f<S, B>(scaled_int(im, Fj, B * S, Factor{0ull, 0, false}), dd[1]);
+      } else {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int kk = kb * TKS + q * 8 + e + h;
+          double v = 0.0;
+          if (nv && kk < P.Kr)
+            v = Bm[P.b_off + (tb ? (int64_t)n + (int64_t)kk * P.ldb : (int64_t)kk + (int64_t)n * P.ldb)];
+          digits_f<S, B>(scaled_int(v, Fj, B * S, Factor{0ull, 0, false}), dd[h]);
+        }
       }
 #pragma unroll
-      for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack_bf16(dd[0][t], dd[1][t]);
+      for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(dd[0][t], dd[1][t]);
     }
     uint8_t *dst = tile + ((c >> 3) * 4 + q) * 128 + (c & 7) * 16;
 #pragma unroll
     for (int t = 0; t < S; ++t)
       *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+  }
+}
+
+template <bool CPLX, int S>
+__global__ void __launch_bounds__(128)
+slice_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
+               const double *__restrict__ Bm, const int *__restrict__ F,
+               uint8_t *__restrict__ arena, int b) {
+  const int4 tk = tasks[blockIdx.x];
+  const SplitPair P = pairs[tk.x];
+  uint8_t *tile = arena + P.bs_off + ((int64_t)(tk.y * P.KB + tk.z) * S) * B_DIGIT_BYTES;
+  switch (b) {
+    case 5: slice_b_tile<CPLX, S, 5>(P, tk.y, tk.z, Bm, F, tile); break;
+    case 6: slice_b_tile<CPLX, S, 6>(P, tk.y, tk.z, Bm, F, tile); break;
+    case 7: slice_b_tile<CPLX, S, 7>(P, tk.y, tk.z, Bm, F, tile); break;
+    default: slice_b_tile<CPLX, S, 8>(P, tk.y, tk.z, Bm, F, tile); break;
   }
 }
 
@@ -828,6 +865,7 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d
                     const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
                     int *dE, int64_t nE, int *dF, int64_t nF, uint8_t *arena, int b, int kchunk,
                     int *err) {
+  if (b < 5 || b > 8 || b * S > 62) fail(QS_ERR_INTERNAL, "split: unsupported digit plan b=%d S=%d", b, S);
   cudaStream_t st = ctx->stream;
   const int fg = (int)std::min<int64_t>(std::max<int64_t>((nE + nF + 255) / 256, 1), 4096);
   ctx->mark(0);
@@ -917,7 +955,7 @@ DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vecto
   for (int b = bhi; b >= blo; --b) {
     int S = forced_slices > 0 ? forced_slices : (need - 1 + b - 1) / b;
     S = std::max(S, 2);
-    if (S > 8) continue;
+    if (S > 8 || b * S > 62) continue;
     const int kchunk = kchunk_of(b, S);
     if (kchunk < TKS) continue;
     double cost = 0;
@@ -1214,7 +1252,7 @@ std::vector<int> split_candidate_bits(double tol, int forced_slices) {
   for (int b = 8; b >= 5; --b) {
     int S = forced_slices > 0 ? forced_slices : (need - 1 + b - 1) / b;
     S = std::max(S, 2);
-    if (S > 8 || kchunk_of(b, S) < TKS) continue;
+    if (S > 8 || b * S > 62 || kchunk_of(b, S) < TKS) continue;
     out.push_back(b);
   }
   return out;
