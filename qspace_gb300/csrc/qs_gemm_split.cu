@@ -641,7 +641,8 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
   if (warp == 0) {
     if (lane == 0) {
       // ------------------------------------------------ TMA producer
-      int it = 0;
+      int it = 0, st = 0;  // stage it % nstages, its phase bit ph
+      uint32_t ph = 0;
       bool ok = true;
       for (int r = 0; ok; ++r) {
         const int ti = tile_of(r, cta, G);
@@ -653,13 +654,15 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
           const uint8_t *a_src = arena + P.as_off + (int64_t)T.mt * KB * A_BYTES;
           const uint8_t *b_src = arena + P.bs_off + (int64_t)T.nt * KB * B_BYTES;
           for (int kb = 0; kb < KB; ++kb, ++it) {
-            const int st = it % nstages;
-            const uint32_t ph = (uint32_t)((it / nstages) & 1);
             if (!mbar_wait(&empty[st], ph ^ 1u, abort_flag, err, 1)) { ok = false; break; }
             uint8_t *sa = stages + (size_t)st * STAGE_BYTES;
             mbar_expect_tx(&full[st], STAGE_BYTES);
             bulk_g2s(sa, a_src + (int64_t)kb * A_BYTES, A_BYTES, &full[st]);
             bulk_g2s(sa + A_BYTES, b_src + (int64_t)kb * B_BYTES, B_BYTES, &full[st]);
+            if (++st == nstages) {
+              st = 0;
+              ph ^= 1u;
+            }
           }
         }
       }
@@ -681,6 +684,12 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
 #pragma unroll
       for (int j = 0; j < S; ++j) idesc[j] = make_idesc(TNS * (j + 1));
       int it = 0, u = 0;  // u: accumulator uses (chunks) handed to the epilogue
+      int st = 0;         // stage it % nstages, its phase bit ph
+      uint32_t ph = 0;
+      // shared-memory descriptors of stage 0; stage st adds st * STAGE_BYTES
+      // to the start address field (addresses stay below 2^18, so the 14-bit
+      // field never carries)
+      const uint64_t desc0 = make_desc(smem_u32(stages), 128, 512);
       bool ok = true;
       // before filling set u & 1 for use u >= 2, wait until use u - 2 is read
       auto acquire = [&](int uu) -> bool {
@@ -711,25 +720,26 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
               depth = 0;
             }
             depth += dk;
-            const int st = it % nstages;
-            const uint32_t ph = (uint32_t)((it / nstages) & 1);
             if (!mbar_wait(&full[st], ph, abort_flag, err, 3)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(stages + (size_t)st * STAGE_BYTES);
-            const uint32_t b0 = a0 + A_BYTES;
+            const uint64_t dst0 = desc0 + (uint64_t)((st * STAGE_BYTES) >> 4);
             const uint32_t dset = tmem + (uint32_t)((u & 1) * SET_COLS);
 #pragma unroll
             for (int ks = 0; ks < TKS / 16; ++ks) {
 #pragma unroll
               for (int t = 0; t < S; ++t) {
-                const uint64_t ad = make_desc(a0 + t * A_DIGIT_BYTES + ks * 256, 128, 512);
-                const uint64_t bd = make_desc(b0 + ks * 256, 128, 512);
+                const uint64_t ad = dst0 + (uint64_t)((t * A_DIGIT_BYTES + ks * 256) >> 4);
+                const uint64_t bd = dst0 + (uint64_t)((A_BYTES + ks * 256) >> 4);
                 const uint32_t acc = (fresh && ks == 0 && t == 0) ? 0u : 1u;
                 umma_bf16(dset + (uint32_t)(t * TNS), ad, bd, idesc[S - 1 - t], acc);
               }
             }
             fresh = false;
             umma_commit(&empty[st]);
+            if (++st == nstages) {
+              st = 0;
+              ph ^= 1u;
+            }
           }
         }
         if (!ok) break;
