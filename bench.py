@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--mode", default="plan", choices=["plan", "oneshot"],
                     help="plan: reusable plan replayed as a CUDA graph; oneshot: qs_grouped_gemm per step")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the slice-count, RDM-latency and serving rows")
+    ap.add_argument("--serve-rates", default="500,5000", help="offered requests/s of the serving rows")
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
     return ap.parse_args()
 
 
@@ -111,6 +114,20 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def world_throughput(flops_local: float, ms_local: float, pg=None, device=None) -> tuple:
+    """Whole-job throughput of independent replicas: the flops all ranks
+    processed over the slowest rank's time.  Returns (TFLOP/s, max ms)."""
+    if pg is None:
+        return flops_local / (ms_local * 1e-3) / 1e12, ms_local
+    import torch
+    t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    f = torch.tensor([flops_local], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.all_reduce(f, op=pg.ReduceOp.SUM)
+    ms = float(t.item())
+    return float(f.item()) / (ms * 1e-3) / 1e12, ms
+
+
 def percentile(xs, q):
     xs = sorted(xs)
     if not xs:
@@ -127,6 +144,64 @@ def measured_peaks():
         return d.get("bf16_tflops"), d.get("hbm_gbs"), "measured"
     except OSError:
         return 1900.0, 6800.0, "fallback"
+
+
+# DRAM traffic of the split GEMM kernel, from one ncu capture of the same
+# kernel on the 300-pair case of this workload (dram__bytes_read.sum 1.215 GB
+# against a 1.163 GB digit arena; dram__bytes_write.sum 0.176 GB against
+# 0.232 GB of output): the kernel reads its digit arena about once and writes
+# the output once, so the full launch is scaled by arena and output bytes.
+GEMM_DRAM_READ_PER_ARENA_BYTE = 1.214957e9 / 1162555392
+GEMM_DRAM_WRITE_PER_OUTPUT_BYTE = 176.067072e6 / 231684512
+
+
+def split_arena_bytes(pk, S: int) -> float:
+    """Bytes of the BF16 digit arena of the batch: 128 x 32 A tiles and 32 x 32
+    B tiles of the real form (2M x 2K and 2K x N per complex pair), S digits."""
+    import numpy as np
+    cm = 2 if pk.cplx else 1
+    M, N, K = (x.astype(np.int64) for x in (pk.M, pk.N, pk.K))
+    MT, NT = (cm * M + 127) // 128, (N + 31) // 32
+    KB = np.maximum(1, (cm * K + 31) // 32)
+    return float(np.sum(MT * KB * S * 8192 + NT * KB * S * 2048))
+
+
+def serve_bench(ctx, prec: str, rate: float, seconds: float, seed: int = 0) -> dict:
+    """Serving loop under load: reduced density matrices contractQS(A,'12*',A,'12')
+    of U(1)xU(1) MPS site tensors whose kept bond dimension D is drawn from
+    256..4096, submitted with Poisson arrivals at `rate` requests/s from
+    device-resident tensors.  Returns achieved requests/s and p50/p99 latency
+    (submit to completion) over the requests completed."""
+    import numpy as np
+    from qspace_gb300 import upload
+    from qspace_gb300.serve import Server
+    from qspace_gb300.workloads import mps_site_tensor
+    hosts = [mps_site_tensor(seed + i, D) for i, D in enumerate((256, 512, 1024, 2048, 4096))]
+    pool = [upload(A, ctx) for A in hosts]
+    # flops of one request: each block meets itself, 2 (dl ds) dr^2
+    fl = [sum(2.0 * x.shape[0] * x.shape[1] * x.shape[2] ** 2 for x in A.data) for A in hosts]
+    rng = np.random.default_rng(seed)
+    lat, tickets, done_flops = [], [], 0.0
+    with Server(nslots=4, hbm_budget=16 << 30, ctx=ctx) as srv:
+        for T in pool:   # warm-up: every size once
+            srv.wait(srv.submit(T, "12*", T, "12", prec=prec))
+        t0 = time.perf_counter()
+        nxt = t0
+        while time.perf_counter() - t0 < seconds:
+            now = time.perf_counter()
+            if now >= nxt:
+                i = int(rng.integers(len(pool)))
+                tickets.append(srv.submit(pool[i], "12*", pool[i], "12", prec=prec))
+                done_flops += fl[i]
+                nxt += rng.exponential(1.0 / rate)
+            else:
+                time.sleep(min(nxt - now, 0.001))
+        for t in tickets:
+            lat.append(srv.wait(t)[1])
+        wall = time.perf_counter() - t0
+    return {"offered_rps": rate, "achieved_rps": len(tickets) / wall, "requests": len(tickets),
+            "p50_ms": percentile(lat, 0.5), "p99_ms": percentile(lat, 0.99), "prec": prec,
+            "tflops": done_flops / wall / 1e12}
 
 
 def run_reference(a, ws, rank):
@@ -236,12 +311,9 @@ def main():
     ck = clocks.stop()
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(a.steps)]
     total_ms = evs[0].elapsed_time(evs[-1])
-    if pg:
-        t = torch.tensor([total_ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms = total_ms / a.steps
-    value = ws * flops / (ms * 1e-3) / 1e12
+    # all ranks' flops over the slowest rank's time (independent replicas)
+    value, max_total_ms = world_throughput(a.steps * flops, total_ms, pg, "cuda" if pg else None)
+    ms = max_total_ms / a.steps
     # what was timed is checked too
     rel_timed = float(torch.linalg.vector_norm(db.dC - c64) / torch.linalg.vector_norm(c64))
 
@@ -282,8 +354,11 @@ def main():
         # real products of (2M) x (2K) x N per complex pair
         digit_flops = S * (S + 1) / 2 * float(np.sum(2.0 * (2 * pk.M.astype(float)) * pk.N * (2 * pk.K.astype(float))))
         achieved = digit_flops / (gemm_ms * 1e-3) / 1e12
+        traffic = (GEMM_DRAM_READ_PER_ARENA_BYTE * split_arena_bytes(pk, S)
+                   + GEMM_DRAM_WRITE_PER_OUTPUT_BYTE * 16.0 * float(np.sum(pk.M.astype(float) * pk.N)))
         roof = {"bound": "tensor", "kernel": "gemm_split_kernel", "achieved": achieved, "peak": bf16_peak,
-                "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": traffic,
+                "traffic_note": "bytes per launch, scaled from an ncu capture of the 300-pair case",
                 "peak_kind": f"bf16 dense, {peak_kind}", "kernel_ms": gemm_ms, "prep_ms": prep_ms,
                 "algorithmic": f"{S}x{S + 1}/2 BF16 digit products of the real 2M x 2K x N form per pair"}
     else:
@@ -308,6 +383,50 @@ def main():
             pplan.close()
         pms = e0.elapsed_time(e1) / a.plain_steps
         plain = {"value": flops / (pms * 1e-3) / 1e12, "ms_per_step": pms}
+
+    # ---- fewer digits: 3 and 4 slices (below the 1e-12 target), error stated
+    slices = []
+    if a.prec == "split" and not a.no_extras:
+        for ns in (3, 4):
+            sp = db.plan("split", nslices=ns)
+            sst = {}
+            db.run_plan(sp, sst)
+            ctx.sync()
+            err = float(torch.linalg.vector_norm(db.dC - c64) / torch.linalg.vector_norm(c64))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                for _ in range(3):
+                    db.run_plan(sp)
+                e1.record(stream)
+            ctx.sync()
+            sms = e0.elapsed_time(e1) / 3
+            sp.close()
+            slices.append({"nslices": ns, "digit_bits": sst.get("digit_bits"), "value": flops / (sms * 1e-3) / 1e12,
+                           "ms_per_step": sms, "rel_err_vs_fp64_gpu": err})
+
+    # ---- one reduced density matrix contractQS(A,'12*',A,'12') through the
+    # host API: the CPU-runnable U(1)xU(1) case (latency-bound, ~1 MFLOP)
+    rdm = None
+    if not a.no_extras:
+        from qspace_gb300 import contractQS
+        from qspace_gb300.workloads import mps_site_tensor
+        A1 = mps_site_tensor(0)
+        rdm = {}
+        for pr in ("fp64", "split"):
+            contractQS(A1, "12*", A1, "12", prec=pr, ctx=ctx)
+            ts = []
+            for _ in range(20):
+                t0 = time.perf_counter()
+                contractQS(A1, "12*", A1, "12", prec=pr, ctx=ctx)
+                ts.append(time.perf_counter() - t0)
+            rdm[pr + "_ms_p50"] = 1e3 * statistics.median(ts)
+
+    # ---- serving loop under Poisson load (split and plain), device-resident tensors
+    serving = None
+    if rank == 0 and not a.no_extras:
+        serving = [serve_bench(ctx, pr, float(r), a.serve_seconds)
+                   for r in a.serve_rates.split(",") for pr in ("split", "fp64")]
 
     # ---- end to end through the host C-ABI (pinned host buffers in and out)
     e2e = None
@@ -356,6 +475,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "slices": slices, "rdm_latency": rdm, "serving": serving,
                 "clocks": ck}
         print(json.dumps(line))
     if pg:

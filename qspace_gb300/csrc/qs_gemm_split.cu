@@ -813,13 +813,14 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
 #pragma unroll
           for (int g = 0; g < S; ++g) {
             const GroupWeight w = gw[g];
-            if (w.rs == 0) {
+            // exactly one of the three forms applies to a group (uniform branch)
+            if (w.mh != 0) {
 #pragma unroll
-              for (int cc = 0; cc < 4; ++cc) {
-                const int a = __float2int_rn(acc[g][cc]);
-                Vh[c4 + cc] += (unsigned int)a * (unsigned int)w.mh;
-                Vl[c4 + cc] = mad_wide(a, w.ml, Vl[c4 + cc]);
-              }
+              for (int cc = 0; cc < 4; ++cc)
+                Vh[c4 + cc] += (unsigned int)__float2int_rn(acc[g][cc]) * (unsigned int)w.mh;
+            } else if (w.rs == 0) {
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) Vl[c4 + cc] = mad_wide(__float2int_rn(acc[g][cc]), w.ml, Vl[c4 + cc]);
             } else {
 #pragma unroll
               for (int cc = 0; cc < 4; ++cc) {
