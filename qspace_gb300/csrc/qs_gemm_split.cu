@@ -191,40 +191,59 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 
 // --------------------------------------------------------- exponent passes
 // Row exponents of op(A~) (per output block, max over its pairs).
+// A block of 256 threads covers rows [m0, m0 + min(256, M - m0)) and depths
+// [k0, k1): R threads per depth phase (R a power of two >= the row count),
+// 256 / R phases splitting the depth, so short blocks keep every thread
+// loading and neighbouring threads read neighbouring rows.  Deep operands
+// are split into several tasks along k (maxima combine atomically).
 template <bool CPLX>
 __global__ void __launch_bounds__(256)
-exp_rows_kernel(const SplitPair *__restrict__ pairs, const int2 *__restrict__ tasks,
+exp_rows_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
                 const double *__restrict__ A, int *__restrict__ E) {
-  const int2 tk = tasks[blockIdx.x];
+  __shared__ int keys[256];
+  const int4 tk = tasks[blockIdx.x];  // (pair, m0, k0, k1)
   const SplitPair P = pairs[tk.x];
-  const int m = tk.y + threadIdx.x;
-  if (m >= P.M) return;
+  const int rows = min(P.M - tk.y, 256);
+  int R = 1;
+  while (R < rows) R <<= 1;
+  const int KS = 256 / R;
+  const int r = threadIdx.x % R, ph = threadIdx.x / R;
+  const int m = tk.y + r;
   const bool ta = P.trans & 1;
   const int64_t sk = ta ? 1 : P.lda, base = P.a_off + (ta ? (int64_t)m * P.lda : (int64_t)m);
   int key = 0;
-  int k = 0;
-  // four independent loads in flight per thread
-  for (; k + 4 <= P.K; k += 4) {
-    if (CPLX) {
-      const double2 *a = reinterpret_cast<const double2 *>(A) + base;
-      const double2 v0 = a[(k + 0) * sk], v1 = a[(k + 1) * sk], v2 = a[(k + 2) * sk], v3 = a[(k + 3) * sk];
-      key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
-                         max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
-    } else {
-      const double *a = A + base;
-      key = max(key, max(max(exp_key(a[(k + 0) * sk]), exp_key(a[(k + 1) * sk])),
-                         max(exp_key(a[(k + 2) * sk]), exp_key(a[(k + 3) * sk]))));
+  if (r < rows) {
+    int k = tk.z + ph;
+    // four independent loads in flight per thread
+    for (; k + 3 * KS < tk.w; k += 4 * KS) {
+      if (CPLX) {
+        const double2 *a = reinterpret_cast<const double2 *>(A) + base;
+        const double2 v0 = a[(int64_t)k * sk], v1 = a[(int64_t)(k + KS) * sk], v2 = a[(int64_t)(k + 2 * KS) * sk],
+                      v3 = a[(int64_t)(k + 3 * KS) * sk];
+        key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
+                           max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
+      } else {
+        const double *a = A + base;
+        key = max(key, max(max(exp_key(a[(int64_t)k * sk]), exp_key(a[(int64_t)(k + KS) * sk])),
+                           max(exp_key(a[(int64_t)(k + 2 * KS) * sk]), exp_key(a[(int64_t)(k + 3 * KS) * sk]))));
+      }
+    }
+    for (; k < tk.w; k += KS) {
+      if (CPLX) {
+        const double2 v = reinterpret_cast<const double2 *>(A)[base + (int64_t)k * sk];
+        key = max(key, max(exp_key(v.x), exp_key(v.y)));
+      } else {
+        key = max(key, exp_key(A[base + (int64_t)k * sk]));
+      }
     }
   }
-  for (; k < P.K; ++k) {
-    if (CPLX) {
-      const double2 v = reinterpret_cast<const double2 *>(A)[base + k * sk];
-      key = max(key, max(exp_key(v.x), exp_key(v.y)));
-    } else {
-      key = max(key, exp_key(A[base + k * sk]));
-    }
+  if (KS > 1) {
+    keys[threadIdx.x] = key;
+    __syncthreads();
+    if (ph != 0) return;
+    for (int p = 1; p < KS; ++p) key = max(key, keys[p * R + r]);
   }
-  if (!key) return;
+  if (r >= rows || !key) return;
   const int e = key - 1022 + P.e_afac;
   if (CPLX) {
     atomicMax(&E[P.eoff + 2 * m], e);
@@ -870,7 +889,7 @@ int pick_stages() {
 }
 
 template <int S>
-void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int2 *d_rt, int nrt,
+void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d_rt, int nrt,
                     const int2 *d_ct, int nct, const int4 *d_xt, int nxt, const int4 *d_at, int nat,
                     const int4 *d_bt, int nbt,
                     const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
@@ -1000,7 +1019,8 @@ struct SplitWork {
   int S = 0, b = 0, kchunk = 0;
   int64_t nE = 0, nF = 0, arena = 0;
   std::vector<SplitPair> sp;
-  std::vector<int2> rt, ct;
+  std::vector<int4> rt;
+  std::vector<int2> ct;
   std::vector<int4> xt, at, bt;
   std::vector<SplitTile> tiles;
 };
@@ -1008,7 +1028,8 @@ struct SplitWork {
 // Their device copies, the exponent arrays and the digit arena.
 struct SplitDev {
   SplitPair *pairs = nullptr;
-  int2 *rt = nullptr, *ct = nullptr;
+  int4 *rt = nullptr;
+  int2 *ct = nullptr;
   int4 *xt = nullptr, *at = nullptr, *bt = nullptr;
   SplitTile *tiles = nullptr;
   int *E = nullptr, *F = nullptr;
@@ -1050,7 +1071,8 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
   if (nE > INT32_MAX || nF > INT32_MAX) fail(QS_ERR_SHAPE, "split: exponent arrays too large");
   int64_t &arena = w.arena;
   arena = 0;
-  std::vector<int2> &rt = w.rt, &ct = w.ct;
+  std::vector<int4> &rt = w.rt;
+  std::vector<int2> &ct = w.ct;
   std::vector<int4> &xt = w.xt;
   std::vector<int4> &at = w.at, &bt = w.bt;
   std::vector<SplitTile> &tiles = w.tiles;
@@ -1092,7 +1114,8 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
       if (d.trans & 1)
         for (int m0 = 0; m0 < d.M; m0 += 8) xt.push_back(make_int4((int)p, m0, 0, 0));
       else
-        for (int m0 = 0; m0 < d.M; m0 += 256) rt.push_back(make_int2((int)p, m0));
+        for (int m0 = 0; m0 < d.M; m0 += 256)
+          for (int k0 = 0; k0 < d.K; k0 += 256) rt.push_back(make_int4((int)p, m0, k0, std::min(d.K, k0 + 256)));
       if (d.trans & 2)
         for (int n0 = 0; n0 < d.N; n0 += 256) ct.push_back(make_int2((int)p, n0));
       else
@@ -1220,7 +1243,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
     return o;
   };
   const size_t o_pairs = take(w.sp.size() * sizeof(SplitPair));
-  const size_t o_rt = take(w.rt.size() * sizeof(int2)), o_ct = take(w.ct.size() * sizeof(int2));
+  const size_t o_rt = take(w.rt.size() * sizeof(int4)), o_ct = take(w.ct.size() * sizeof(int2));
   const size_t o_xt = take(w.xt.size() * sizeof(int4)), o_at = take(w.at.size() * sizeof(int4));
   const size_t o_bt = take(w.bt.size() * sizeof(int4));
   const size_t o_tiles = take(w.tiles.size() * sizeof(SplitTile));
@@ -1231,7 +1254,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
          "BF16 digits), more than the %zu available", used, (long long)w.arena, cap);
   SplitDev d;
   d.pairs = reinterpret_cast<SplitPair *>(scratch + o_pairs);
-  d.rt = reinterpret_cast<int2 *>(scratch + o_rt);
+  d.rt = reinterpret_cast<int4 *>(scratch + o_rt);
   d.ct = reinterpret_cast<int2 *>(scratch + o_ct);
   d.xt = reinterpret_cast<int4 *>(scratch + o_xt);
   d.at = reinterpret_cast<int4 *>(scratch + o_at);
@@ -1244,7 +1267,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
     if (bytes) QS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
   };
   put(d.pairs, w.sp.data(), w.sp.size() * sizeof(SplitPair));
-  put(d.rt, w.rt.data(), w.rt.size() * sizeof(int2));
+  put(d.rt, w.rt.data(), w.rt.size() * sizeof(int4));
   put(d.ct, w.ct.data(), w.ct.size() * sizeof(int2));
   put(d.xt, w.xt.data(), w.xt.size() * sizeof(int4));
   put(d.at, w.at.data(), w.at.size() * sizeof(int4));
