@@ -170,6 +170,19 @@ QS_EXPORT qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char 
                           const int32_t *perm, int32_t nperm,
                           const qs_opts *opts, qs_tensor **C, qs_stats *stats);
 
+/* Cell contraction C = contractQS({X_0, X_1, ..., X_{n-1}} [,perm])
+ * (Source/contractQS.cc:634-808, contractQS_itags) on device-resident
+ * tensors: right to left, C = X_{n-1}, then C = X_k * C for k = n-2..0 over
+ * the legs whose itags match (same name, opposite direction; the same
+ * direction when one of the two carries a conj flag; Source/wbindex.cc:
+ * 1512-1595).  conj[k] != 0 is the '*' option of X_k (conj may be NULL).
+ * Every leg needs a non-empty itag.  perm (1-based; a partial permutation is
+ * extended) applies to the final result; an empty intermediate result gives
+ * an empty result. */
+QS_EXPORT qs_status qs_contract_itags(qs_ctx *ctx, int32_t n, const qs_tensor *const *T,
+                                      const int32_t *conj, const int32_t *perm, int32_t nperm,
+                                      const qs_opts *opts, qs_tensor **C);
+
 /* ---------------------------------------------------------- permuteQS
  * B = permuteQS(A, perm [,'conj']) (Source/permuteQS.cc:198-258;
  * QSpace::Permute Source/QSpace.hh:2670-2719): legs of labels and of every

@@ -421,6 +421,66 @@ def _parse_perm(perm, rc):
     return p
 
 
+def itag_pairs(ta: list, ca: bool, tb: list, cb: bool):
+    """Legs that an itag (cell) contraction pairs up: iTags::getCtr
+    (Source/wbindex.cc:1512-1595) with itag_::sameAs (:989-1007).  Same name
+    and opposite direction, or the same direction when exactly one operand
+    carries a conj flag; if nothing matches the other polarity is used and
+    A's conj flag toggles.  Returns (ia, ib, flipA), 0-based."""
+    def name(t):
+        return t.split("*")[0]
+
+    def d(t):
+        return "*" in t
+
+    cflag = ca != cb
+    for it in range(2):
+        q = 1 if cflag else -1
+        ma, mb, nc, e = [0] * len(ta), [0] * len(tb), 0, 0
+        for i, x in enumerate(ta):
+            for j, y in enumerate(tb):
+                if name(x) != name(y) or (1 if d(x) == d(y) else -1) != q:
+                    continue
+                if not ma[i] and not mb[j]:
+                    ma[i], mb[j], nc = j + 1, i + 1, nc + 1
+                else:
+                    e += 1
+        if nc or e:
+            break
+        cflag = not cflag
+    if e:
+        raise ValueError("itag contraction: non-unique itags")
+    if not nc:
+        raise ValueError("itag contraction: no matching itags")
+    ia = [i for i in range(len(ta)) if ma[i]]
+    ib = [ma[i] - 1 for i in ia]
+    return ia, ib, it == 1
+
+
+def contract_cell(items: list, perm=None) -> dict:
+    """contractQS({X0, X1, '*', ...} [,perm]): right to left, C = X_{n-1},
+    C = X_k * C over itag-matched legs (contractQS_itags, Source/contractQS.cc:
+    634-808); a '*' after a QSpace is its conj option; an empty operand gives
+    an empty result."""
+    X = []
+    for x in items:
+        if isinstance(x, str):
+            X[-1] = (X[-1][0], not X[-1][1])
+        else:
+            X.append((x, False))
+    B, cb = X[-1]
+    for k in range(len(X) - 2, -1, -1):
+        A, ca = X[k]
+        if not A["data"] or not B["data"]:
+            return {"Q": [], "data": [], "info": {}}
+        ia, ib, flip = itag_pairs(A["info"]["itags"], ca, B["info"]["itags"], cb)
+        sa = ",".join(str(i + 1) for i in ia) + ("*" if ca != flip else "")
+        sb = ",".join(str(j + 1) for j in ib) + ("*" if cb else "")
+        B = contract(A, sa, B, sb, perm if k == 0 else None)
+        cb = False
+    return B
+
+
 def permute(A: dict, perm, conj: bool = False) -> dict:
     """permuteQS(A, perm [,'conj']) for abelian QSpaces (Source/permuteQS.cc:
     198-258; ``QSpace::Permute`` Source/QSpace.hh:2670-2719): the legs of the

@@ -107,7 +107,8 @@ def to_mx(A: dict):
     n = len(A["data"])
     Qc = lib.mxCreateCellMatrix(1, r)
     for k in range(r):
-        q = np.asarray(A["Q"][k], dtype=np.float64).reshape(n, -1)
+        q = np.asarray(A["Q"][k], dtype=np.float64)
+        q = q.reshape(n, -1) if n else q.reshape(0, q.shape[-1] if q.ndim == 2 else 1)
         lib.mxSetCell(Qc, k, _mx_array(q))
     D = lib.mxCreateCellMatrix(n, 1)
     for i, blk in enumerate(A["data"]):
@@ -194,6 +195,27 @@ def contractQS(A: dict, ia, B: dict, ib, perm=None) -> dict:
         if isinstance(perm, str):  # '3,1,2' -> [3, 1, 2] (numeric perm argument)
             perm = [int(x) for x in perm.replace(",", " ").split()] if any(c in perm for c in ", ") \
                 else [int(c) for c in perm]
+        args.append(_arg(perm))
+    try:
+        out = call("contractQS", args, 1)[0]
+        res = from_mx(out) if out else {"Q": [], "data": [], "info": {}}
+        if out:
+            lib.mxDestroyArray(out)
+        return res
+    finally:
+        for a in args:
+            lib.mxDestroyArray(a)
+
+
+def contractQS_cell(items: list, perm=None) -> dict:
+    """The reference's cell contraction contractQS({X0, X1, '*', ...} [,perm]):
+    items are QSpace dicts or option strings ('*' after a QSpace)."""
+    lib = _fake()
+    cell = lib.mxCreateCellMatrix(1, len(items))
+    for k, x in enumerate(items):
+        lib.mxSetCell(cell, k, _mx_string(x) if isinstance(x, str) else to_mx(x))
+    args = [cell]
+    if perm is not None:
         args.append(_arg(perm))
     try:
         out = call("contractQS", args, 1)[0]

@@ -100,6 +100,8 @@ SIGNATURES = {
                                C.POINTER(C.c_void_p)]),
     "qs_permute_dev": (C.c_int, [C.c_void_p, C.c_void_p, c_int32_p, C.c_int32, C.c_int32,
                                  C.POINTER(C.c_void_p)]),
+    "qs_contract_itags": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), c_int32_p, c_int32_p,
+                                    C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)]),
     "qs_grouped_gemm": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
     "qs_grouped_plan_create": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.POINTER(Opts),

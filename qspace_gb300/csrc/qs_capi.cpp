@@ -414,6 +414,105 @@ static qs_result *download(Ctx *ctx, const qs_tensor *T) {
 
 }  // namespace qs
 
+// ------------------------------------------------- itag chain contraction
+// Legs of A and B that contract (Source/wbindex.cc:1512-1595, iTags::getCtr,
+// with itag_::sameAs :989-1007): the same tag name with opposite directions,
+// or with equal directions when exactly one of the two operands carries a
+// conj flag.  When nothing matches that way the other polarity is used and
+// A's conj flag is toggled (the reference does so after a warning).
+static void itag_pairs(const QMeta &A, bool ca, const QMeta &B, bool cb, std::vector<int> &ia,
+                       std::vector<int> &ib, bool &flipA) {
+  const int ra = A.rank, rb = B.rank;
+  if ((int)A.itags.size() != ra || (int)B.itags.size() != rb)
+    fail(QS_ERR_LABEL, "itag contraction needs itags on every leg ('%s' <> '%s')", join_itags(A.itags).c_str(),
+         join_itags(B.itags).c_str());
+  auto name = [](const std::string &t) { return t.substr(0, t.find('*')); };
+  auto dir = [](const std::string &t) { return t.find('*') != std::string::npos; };
+  for (const std::string &t : A.itags)
+    if (name(t).empty()) fail(QS_ERR_LABEL, "itag contraction needs non-empty itags");
+  for (const std::string &t : B.itags)
+    if (name(t).empty()) fail(QS_ERR_LABEL, "itag contraction needs non-empty itags");
+  std::vector<int> ma(ra, 0), mb(rb, 0);
+  int nc = 0, e = 0, it = 0;
+  bool cflag = ca != cb;
+  for (; it < 2; ++it) {
+    const int q = cflag ? 1 : -1;
+    for (int i = 0; i < ra; ++i)
+      for (int j = 0; j < rb; ++j) {
+        if (name(A.itags[i]) != name(B.itags[j])) continue;
+        const int sgn = dir(A.itags[i]) != dir(B.itags[j]) ? -1 : 1;
+        if (sgn != q) continue;
+        if (!ma[i] && !mb[j]) {
+          ma[i] = j + 1;
+          mb[j] = i + 1;
+          ++nc;
+        } else {
+          ++e;
+        }
+      }
+    if (nc || e) break;
+    cflag = !cflag;
+  }
+  if (e)
+    fail(QS_ERR_LABEL, "itag contraction: non-unique itags ('%s' <> '%s')", join_itags(A.itags).c_str(),
+         join_itags(B.itags).c_str());
+  if (!nc)
+    fail(QS_ERR_LABEL, "itag contraction: no matching itags ('%s' <> '%s')", join_itags(A.itags).c_str(),
+         join_itags(B.itags).c_str());
+  ia.clear();
+  ib.clear();
+  for (int i = 0; i < ra; ++i)
+    if (ma[i]) {
+      ia.push_back(i + 1);
+      ib.push_back(ma[i]);
+    }
+  flipA = it == 1;
+}
+
+static std::string idx_string(const std::vector<int> &ix, bool conj) {
+  std::string s = "[";
+  for (int i : ix) s += std::to_string(i) + " ";
+  s += "]";
+  if (conj) s += "*";
+  return s;
+}
+
+// Cell contraction {X_0, ..., X_{n-1}} (Source/contractQS.cc:634-808,
+// contractQS_itags): right to left, C = X_{n-1}; C = X_k * C for k = n-2..0
+// over the legs matched by itag; the permutation applies to the final result;
+// an empty operand makes the result empty.
+static std::unique_ptr<qs_tensor> contract_itags_core(Ctx *ctx, int n, const qs_tensor *const *T,
+                                                      const int32_t *conj, const int32_t *perm, int32_t nperm,
+                                                      const qs_opts *opts) {
+  if (n < 2) fail(QS_ERR_ARG, "itag contraction needs at least two tensors");
+  for (int k = 0; k < n; ++k)
+    if (!T[k]) fail(QS_ERR_ARG, "null tensor %d", k);
+  std::unique_ptr<qs_tensor> cur;
+  const QMeta *Bm = &T[n - 1]->meta;
+  const double *Bd = T[n - 1]->d;
+  bool cb = conj && conj[n - 1];
+  for (int k = n - 2; k >= 0; --k) {
+    const qs_tensor *A = T[k];
+    const bool ca = conj && conj[k];
+    if (A->meta.nblk == 0 || Bm->nblk == 0) {
+      auto E = std::make_unique<qs_tensor>();
+      E->ctx = ctx;
+      return E;
+    }
+    std::vector<int> ia, ib;
+    bool flip = false;
+    itag_pairs(A->meta, ca, *Bm, cb, ia, ib, flip);
+    const std::string sa = idx_string(ia, ca != flip), sb = idx_string(ib, cb);
+    auto C = contract_core(ctx, A->meta, A->d, *Bm, Bd, sa.c_str(), sb.c_str(), k == 0 ? perm : nullptr,
+                           k == 0 ? nperm : 0, opts, nullptr);
+    cur = std::move(C);
+    Bm = &cur->meta;
+    Bd = cur->d;
+    cb = false;
+  }
+  return cur;
+}
+
 // ======================================================================= C-ABI
 extern "C" {
 
@@ -591,6 +690,16 @@ qs_status qs_result_itags(const qs_result *C, char *buf, size_t len) {
 }
 
 void qs_tensor_free(qs_tensor *T) { delete T; }
+
+qs_status qs_contract_itags(qs_ctx *ctx, int32_t n, const qs_tensor *const *T, const int32_t *conj,
+                            const int32_t *perm, int32_t nperm, const qs_opts *opts, qs_tensor **C) {
+  QS_API_BEGIN
+  if (!ctx || !T || !C) fail(QS_ERR_ARG, "null argument");
+  *C = nullptr;
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  *C = contract_itags_core(&ctx->c, n, T, conj, perm, nperm, opts).release();
+  QS_API_END
+}
 
 qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char *ia, const qs_tensor *B,
                           const char *ib, const int32_t *perm, int32_t nperm, const qs_opts *opts,

@@ -21,7 +21,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _capi
-from ._capi import QSpaceView, Opts, Stats, check
+from ._capi import QSError, QSpaceView, Opts, Stats, check
 
 __all__ = ["QSpace", "Tensor", "Context", "contractQS", "permuteQS", "default_context",
            "upload", "contract_dev", "permute_dev"]
@@ -239,13 +239,19 @@ def _result_to_qspace(lib, res, info=None) -> QSpace:
     return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, bool(cx.value), info)
 
 
-def contractQS(A: QSpace, ia, B: QSpace, ib, perm=None, *, prec: str = "fp64", nslices: int = 0,
+def contractQS(A, ia=None, B: QSpace | None = None, ib=None, perm=None, *, prec: str = "fp64", nslices: int = 0,
                tol: float = 1e-12, ctx: Context | None = None, stats: dict | None = None) -> QSpace:
     """C = contractQS(A, ia, B, ib [,perm]) on the GPU (host buffers in/out).
 
     ``ia``/``ib``: '12*' style strings or 1-based sequences; ``perm`` 1-based.
     ``prec``: 'fp64' (plain drop-in) or 'split' (BF16 digits on tcgen05).
+
+    Cell form ``contractQS([X0, X1, '*', X2, ...] [, perm])``: contraction
+    over matching itags, right to left (Source/contractQS.cc:634-808); a '*'
+    after a QSpace is its conj option.
     """
+    if isinstance(A, (list, tuple)):
+        return contract_itags(A, ia, prec=prec, nslices=nslices, tol=tol, ctx=ctx)
     ctx = ctx or default_context()
     va, ka = A.pack()
     vb, kb = B.pack()
@@ -343,6 +349,41 @@ def contract_dev(A: Tensor, ia, B: Tensor, ib, perm=None, *, prec: str = "fp64",
     if stats is not None:
         stats.update(st.as_dict())
     return Tensor(ctx, h)
+
+
+def _cell_items(items):
+    """[X0, '*', X1, ...] -> [(X0, conj0), (X1, conj1), ...]"""
+    out = []
+    for x in items:
+        if isinstance(x, str):
+            if not out or x.strip() != "*":
+                raise QSError(1, f"invalid cell-contraction option {x!r}")
+            out[-1] = (out[-1][0], not out[-1][1])
+        else:
+            out.append((x, False))
+    return out
+
+
+def contract_itags(items, perm=None, *, prec: str = "fp64", nslices: int = 0, tol: float = 1e-12,
+                   ctx: Context | None = None):
+    """Cell contraction over matching itags (qs_contract_itags).  Items are
+    QSpace (host; result returned as QSpace) or Tensor (device; result
+    returned as Tensor), each optionally followed by '*'."""
+    pairs = _cell_items(items)
+    dev = all(isinstance(x, Tensor) for x, _ in pairs)
+    if not dev and any(isinstance(x, Tensor) for x, _ in pairs):
+        raise QSError(1, "cell contraction mixes host and device tensors")
+    ctx = pairs[0][0].ctx if dev else (ctx or default_context())
+    T = [x if dev else upload(x, ctx) for x, _ in pairs]
+    arr = (C.c_void_p * len(T))(*[t.h.value for t in T])
+    conj = np.array([1 if c else 0 for _, c in pairs], np.int32)
+    p, n = _perm_arg(perm)
+    o = make_opts(prec, nslices, tol)
+    h = C.c_void_p()
+    check(ctx.lib.qs_contract_itags(ctx.h, len(T), arr, conj.ctypes.data_as(_capi.c_int32_p), p, n,
+                                    C.byref(o), C.byref(h)))
+    R = Tensor(ctx, h)
+    return R if dev else R.download()
 
 
 def permute_dev(A: Tensor, perm, conj=False) -> Tensor:

@@ -5,8 +5,9 @@ against the fake MATLAB runtime (oracle/refbuild.py, oracle/ref.py).
     python -m oracle.refbuild contractQS permuteQS
     python tests/golden/make_golden.py
 
-Writes tests/golden/contract_golden.npz and permute_golden.npz: inputs,
-index/perm arguments, and the reference outputs (labels, block order, data).
+Writes tests/golden/contract_golden.npz, permute_golden.npz and
+cell_golden.npz (itag cell contractions): inputs, index/perm arguments, and
+the reference outputs (labels, block order, itags, data).
 The inputs are seeded synthetic tensors (qspace_gb300.workloads); the
 reference was built with QS_SKIP_MPFR (abelian cases need no CG data).
 """
@@ -79,6 +80,25 @@ def contract_cases():
     return out
 
 
+def cell_cases():
+    """Cell (itag) contractions: [(name, items, perm)], items QSpace dicts or '*'."""
+    out = []
+    for cx in (False, True):
+        rng = np.random.default_rng(4242 + cx)
+        t = [random_leg(rng, nsec=3, dmax=4, qdim=2) for _ in range(5)]
+        A = random_abelian(rng, [t[0], t[1], t[2]], complex_data=cx, itags=["a", "b", "c"]).to_dict()
+        B = random_abelian(rng, [t[2], t[3]], complex_data=cx, itags=["c*", "d"]).to_dict()
+        C = random_abelian(rng, [t[3], t[4]], complex_data=cx, itags=["d*", "e"]).to_dict()
+        s = f"{'z' if cx else 'r'}"
+        out += [(f"pair_{s}", [A, B], None), (f"pair_perm_{s}", [A, B], [3, 1, 2]),
+                (f"chain3_{s}", [A, B, C], None), (f"chain3_perm_{s}", [A, B, C], [2, 1]),
+                (f"conjA_{s}", [A, "*", B], None), (f"conjlast_{s}", [B, C, "*"], None),
+                (f"norm_{s}", [A, "*", A], None)]
+    M = mps_site_tensor(3, D=128, complex_data=True).to_dict()
+    out.append(("mps_rdm", [M, "*", M], None))
+    return out
+
+
 def main():
     if not ref.available("contractQS") or not ref.available("permuteQS"):
         sys.exit("build the reference oracle first: python -m oracle.refbuild contractQS permuteQS")
@@ -106,7 +126,22 @@ def main():
                 meta.append({"name": name, "perm": perm, "conj": conj})
     z["cases"] = np.array(json.dumps(meta))
     np.savez_compressed(os.path.join(HERE, "permute_golden.npz"), **z)
-    print("wrote", os.path.join(HERE, "contract_golden.npz"), os.path.join(HERE, "permute_golden.npz"))
+
+    z, meta = {}, []
+    for name, items, perm in cell_cases():
+        R = ref.contractQS_cell(items, perm)
+        spec = []
+        for k, x in enumerate(items):
+            if isinstance(x, str):
+                spec.append(x)
+            else:
+                pack(f"{name}_X{k}", x, z)
+                spec.append(f"X{k}")
+        pack(f"{name}_C", R, z)
+        meta.append({"name": name, "items": spec, "perm": perm})
+    z["cases"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "cell_golden.npz"), **z)
+    print("wrote contract_golden.npz, permute_golden.npz, cell_golden.npz in", HERE)
 
 
 if __name__ == "__main__":

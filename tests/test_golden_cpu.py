@@ -69,3 +69,17 @@ def test_oracle_vs_live_reference_fresh_inputs():
                 R, O = ref.contractQS(A, ia, B, ib, perm), orc.contract(A, ia, B, ib, perm)
             assert_qspace_close(O, R, 1e-14)
             assert O["info"].get("itags") == R["info"].get("itags")
+
+
+def _cell_items(z, c):
+    return [x if x == "*" else unpack(f"{c['name']}_{x}", z) for x in c["items"]]
+
+
+def test_oracle_matches_reference_cell_contractions():
+    z, cases = _cases("cell_golden.npz")
+    assert len(cases) >= 15
+    for c in cases:
+        R = unpack(f"{c['name']}_C", z)
+        O = orc.contract_cell(_cell_items(z, c), c["perm"])
+        assert_qspace_close(O, R, 1e-14)
+        assert (O["info"].get("itags") or None) == (R["info"].get("itags") or None), c["name"]

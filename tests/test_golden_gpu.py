@@ -40,3 +40,19 @@ def test_permuteQS_matches_reference(ctx):
         B = permuteQS(QSpace.from_dict(A), c["perm"], c["conj"], ctx=ctx)
         assert_qspace_close(B, R, 0.0)
         assert B.info.get("itags") == R["info"].get("itags"), n
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-14), ("split", 1e-12)])
+def test_cell_contraction_matches_reference(ctx, prec, tol):
+    from qspace_gb300 import contract_itags, upload
+    z, cases = _cases("cell_golden.npz")
+    for c in cases:
+        items = [x if x == "*" else QSpace.from_dict(unpack(f"{c['name']}_{x}", z)) for x in c["items"]]
+        R = unpack(f"{c['name']}_C", z)
+        C = contract_itags(items, c["perm"], prec=prec, ctx=ctx)
+        assert_qspace_close(C, R, tol)
+        assert (C.info.get("itags") or None) == (R["info"].get("itags") or None), c["name"]
+        # the same chain on device-resident tensors
+        dev = [x if x == "*" else upload(x, ctx) for x in items]
+        Cd = contract_itags(dev, c["perm"], prec=prec).download()
+        assert_qspace_close(Cd, R, tol)
