@@ -170,6 +170,18 @@ QS_EXPORT qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char 
                           const int32_t *perm, int32_t nperm,
                           const qs_opts *opts, qs_tensor **C, qs_stats *stats);
 
+/* A batch of device-resident contractions C[r] = contractQS(A[r], ia[r], B[r],
+ * ib[r] [,perm[r]]) whose block products all run in one grouped launch per
+ * result element type (no reference counterpart: the reference contracts
+ * one pair of QSpaces per call; the per-contraction semantics are those of
+ * qs_contract_dev).  On the split path each contraction keeps the digit
+ * plan it would get alone, so every result is bit-identical to the same
+ * call alone.  perm and nperm may be NULL; C receives n tensors. */
+QS_EXPORT qs_status qs_contract_batch(qs_ctx *ctx, int32_t n, const qs_tensor *const *A,
+                                      const char *const *ia, const qs_tensor *const *B,
+                                      const char *const *ib, const int32_t *const *perm,
+                                      const int32_t *nperm, const qs_opts *opts, qs_tensor **C);
+
 /* Cell contraction C = contractQS({X_0, X_1, ..., X_{n-1}} [,perm])
  * (Source/contractQS.cc:634-808, contractQS_itags) on device-resident
  * tensors: right to left, C = X_{n-1}, then C = X_k * C for k = n-2..0 over
@@ -327,7 +339,8 @@ QS_EXPORT qs_status qs_gs_reortho(qs_ctx *ctx, int64_t n, int64_t nv, const doub
 typedef struct qs_server qs_server;
 typedef struct {
   int32_t nslots;          /* concurrent requests on the device               */
-  int32_t pad_;
+  int32_t max_batch;       /* requests one slot runs in one grouped launch
+                              (continuous batching); 0 = 16                  */
   int64_t hbm_budget;      /* bytes of scratch+output the server may hold      */
 } qs_server_cfg;
 QS_EXPORT qs_status qs_server_create(qs_ctx *ctx, const qs_server_cfg *cfg, qs_server **out);

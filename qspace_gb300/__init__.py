@@ -6,8 +6,8 @@ split-precision BF16 tensor-core path; block eig/SVD and a serving loop.
 The numerical work runs in libqsgpu.so (CUDA for sm_103a) behind the C-ABI
 of include/qsgpu.h.
 """
-from .qspace import (QSpace, Tensor, Context, contractQS, contract_itags, permuteQS, default_context, upload,
+from .qspace import (QSpace, Tensor, Context, contractQS, contract_batch, contract_itags, permuteQS, default_context, upload,
                      contract_dev, permute_dev)
 
-__all__ = ["QSpace", "Tensor", "Context", "contractQS", "contract_itags", "permuteQS", "default_context",
+__all__ = ["QSpace", "Tensor", "Context", "contractQS", "contract_batch", "contract_itags", "permuteQS", "default_context",
            "upload", "contract_dev", "permute_dev"]

@@ -48,7 +48,7 @@ class PairList(C.Structure):
 
 
 class ServerCfg(C.Structure):
-    _fields_ = [("nslots", C.c_int32), ("pad_", C.c_int32), ("hbm_budget", C.c_int64)]
+    _fields_ = [("nslots", C.c_int32), ("max_batch", C.c_int32), ("hbm_budget", C.c_int64)]
 
 
 QS_PREC_FP64 = 0
@@ -100,6 +100,9 @@ SIGNATURES = {
                                C.POINTER(C.c_void_p)]),
     "qs_permute_dev": (C.c_int, [C.c_void_p, C.c_void_p, c_int32_p, C.c_int32, C.c_int32,
                                  C.POINTER(C.c_void_p)]),
+    "qs_contract_batch": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_char_p),
+                                    C.POINTER(C.c_void_p), C.POINTER(C.c_char_p), C.POINTER(c_int32_p), c_int32_p,
+                                    C.POINTER(Opts), C.POINTER(C.c_void_p)]),
     "qs_contract_itags": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), c_int32_p, c_int32_p,
                                     C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)]),
     "qs_grouped_gemm": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,

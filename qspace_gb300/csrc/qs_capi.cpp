@@ -200,161 +200,309 @@ static std::unique_ptr<qs_tensor> empty_tensor(Ctx *ctx, int rank, int qdim, boo
   return T;
 }
 
-// The device contraction driver shared by the host and device entry points.
-std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double *dA,
-                                                const QMeta &Bm, const double *dB, const char *ia,
-                                                const char *ib, const int32_t *perm, int32_t nperm,
-                                                const qs_opts *opts, qs_stats *stats) {
-  const int64_t launches0 = ctx->launches;
-  ContractPlan pl = plan_contract(Am, ia, Bm, ib, perm, nperm);
-  const bool cplx = pl.C.cplx;
-  if (stats) {
-    std::memset(stats, 0, sizeof *stats);
-    stats->flops = pl.flops;
-    stats->bytes = pl.bytes;
-    stats->npairs = (int64_t)pl.pairs.size();
-  }
+// ------------------------------------------------------ contraction driver
+// A contraction in flight: its plan, operands in the layout and element type
+// the plan wants, and its output arena before zero-block removal.
+struct Prepared {
+  ContractPlan pl;
+  bool cplx = false;
+  const double *a2 = nullptr, *b2 = nullptr;
+  double *dC = nullptr;
+  std::vector<void *> tmp;
+  std::unique_ptr<qs_tensor> done;  // set when no product is needed
+};
+
+// Plan on the host, then widen/permute the operands as the plan wants and
+// allocate the output (kernels on ctx->stream).
+static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, const QMeta &Bm,
+                    const double *dB, const char *ia, const char *ib, const int32_t *perm, int32_t nperm) {
+  w.pl = plan_contract(Am, ia, Bm, ib, perm, nperm);
+  ContractPlan &pl = w.pl;
+  const bool cplx = w.cplx = pl.C.cplx;
   if (pl.C.nblk == 0) {
     // no matching sectors: an empty QSpace that still carries the itags
-    auto T = empty_tensor(ctx, 0, Am.qdim, cplx);
-    for (int k = 0; k < (int)pl.C.itags.size(); ++k) T->meta.itags.push_back(pl.C.itags[pl.P.empty() ? k : pl.P[k]]);
-    return T;
+    w.done = empty_tensor(ctx, 0, Am.qdim, cplx);
+    for (int k = 0; k < (int)pl.C.itags.size(); ++k)
+      w.done->meta.itags.push_back(pl.C.itags[pl.P.empty() ? k : pl.P[k]]);
+    return;
   }
   const int es = cplx ? 2 : 1;
-
-  // Operands in the element type of the result, in the layout the plan wants.
-  std::vector<void *> tmp;
   auto prep = [&](const QMeta &m, const double *d, const OperandLayout &lay) -> const double * {
     const double *cur = d;
     if (cplx && !m.cplx) {
-      double *w = dev_alloc<double>(ctx, (size_t)m.nelem * 2);
-      tmp.push_back(w);
-      launch_widen(ctx, d, w, m.nelem);
-      cur = w;
+      double *x = dev_alloc<double>(ctx, (size_t)m.nelem * 2);
+      w.tmp.push_back(x);
+      launch_widen(ctx, d, x, m.nelem);
+      cur = x;
     }
     if (lay.permute) {
       double *o = dev_alloc<double>(ctx, (size_t)m.nelem * es);
-      tmp.push_back(o);
+      w.tmp.push_back(o);
       std::vector<PermDesc> pd = make_perm_descs(m, lay.perm, lay.conj, m.offs);
       run_permute(ctx, pd, cur, o, cplx);
       cur = o;
     }
     return cur;
   };
-  const double *a2 = prep(Am, dA, pl.la);
-  const double *b2 = prep(Bm, dB, pl.lb);
+  w.a2 = prep(Am, dA, pl.la);
+  w.b2 = prep(Bm, dB, pl.lb);
+  w.dC = dev_alloc<double>(ctx, (size_t)pl.C.nelem * es);
+}
 
-  double *dC = dev_alloc<double>(ctx, (size_t)pl.C.nelem * es);
+// All block products of a batch of prepared contractions of one element type
+// in one grouped launch.  The operands and outputs of different
+// contractions are separate arenas in the device's one address space:
+// their element offsets are taken relative to the lowest address of each
+// kind, so that one pair list addresses all of them.  forced_slices /
+// forced_bits (0: none) fix the split path's digit plan.
+static void run_products(Ctx *ctx, const std::vector<Prepared *> &batch, const qs_opts *opts, qs_stats *stats,
+                         int forced_slices = 0, int forced_bits = 0) {
+  if (batch.empty()) return;
+  const bool cplx = batch[0]->cplx;
+  const int64_t eb = cplx ? 16 : 8;
+  const double *baseA = batch[0]->a2, *baseB = batch[0]->b2;
+  double *baseC = batch[0]->dC;
+  for (Prepared *w : batch) {
+    if (w->cplx != cplx) fail(QS_ERR_INTERNAL, "batched products of mixed element types");
+    baseA = std::min(baseA, w->a2);
+    baseB = std::min(baseB, w->b2);
+    baseC = std::min(baseC, w->dC);
+  }
+  auto rel = [&](const void *p, const void *base) {
+    const int64_t d = (int64_t)((const char *)p - (const char *)base);
+    if (d % eb) fail(QS_ERR_INTERNAL, "misaligned arena in a batched launch");
+    return d / eb;
+  };
+  std::vector<PairDesc> pairs;
+  std::vector<int64_t> grp{0}, c_off;
+  std::vector<int32_t> bM, bN;
+  for (Prepared *w : batch) {
+    const ContractPlan &pl = w->pl;
+    const int64_t da = rel(w->a2, baseA), db = rel(w->b2, baseB), dc = rel(w->dC, baseC);
+    for (PairDesc d : pl.pairs) {
+      d.a_off += da;
+      d.b_off += db;
+      pairs.push_back(d);
+    }
+    for (size_t b = 0; b + 1 < pl.grp.size(); ++b) grp.push_back(grp.back() + (pl.grp[b + 1] - pl.grp[b]));
+    for (size_t b = 0; b < pl.blk_M.size(); ++b) {
+      bM.push_back(pl.blk_M[b]);
+      bN.push_back(pl.blk_N[b]);
+      c_off.push_back(pl.C.offs[b] + dc);
+    }
+  }
   const int prec = opts ? opts->prec : QS_PREC_FP64;
-  std::vector<int64_t> c_off = pl.C.offs;
   if (prec == QS_PREC_SPLIT) {
-    SplitResult sr = run_split(ctx, pl.pairs, pl.grp, pl.blk_M, pl.blk_N, c_off, a2, b2, dC, cplx,
-                               opts ? opts->nslices : 0, opts && opts->tol > 0 ? opts->tol : 1e-12);
+    SplitResult sr = run_split(ctx, pairs, grp, bM, bN, c_off, baseA, baseB, baseC, cplx,
+                               forced_slices ? forced_slices : (opts ? opts->nslices : 0),
+                               opts && opts->tol > 0 ? opts->tol : 1e-12, nullptr, forced_bits);
     if (stats) {
       stats->nslices = sr.nslices;
       stats->digit_bits = sr.bits;
       stats->err_bound = sr.err_bound;
     }
   } else if (prec == QS_PREC_FP64) {
-    std::vector<TileDesc> tiles =
-        make_tiles(pl.grp, pl.blk_M, pl.blk_N, c_off, gemm_f64_tile_m(), gemm_f64_tile_n());
-    PairDesc *dp = dev_upload(ctx, pl.pairs);
+    std::vector<TileDesc> tiles = make_tiles(grp, bM, bN, c_off, gemm_f64_tile_m(), gemm_f64_tile_n());
+    PairDesc *dp = dev_upload(ctx, pairs);
     TileDesc *dt = dev_upload(ctx, tiles);
-    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), a2, b2, dC, cplx ? 1 : 0);
+    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), baseA, baseB, baseC, cplx ? 1 : 0);
     dev_free(ctx, dp);
     dev_free(ctx, dt);
   } else {
     fail(QS_ERR_ARG, "unknown precision mode %d", prec);
   }
-  for (void *p : tmp) dev_free(ctx, p);
+  for (Prepared *w : batch) {
+    for (void *p : w->tmp) dev_free(ctx, p);
+    w->tmp.clear();
+  }
+}
 
-  // SkipZeroData: drop exactly-zero output blocks (with the rank-2 rule).
-  const int64_t nb = pl.C.nblk;
-  std::vector<int64_t> sizes(nb);
-  for (int64_t i = 0; i < nb; ++i) sizes[i] = pl.C.bsize(i);
-  int64_t *doff = dev_upload(ctx, pl.C.offs), *dsz = dev_upload(ctx, sizes);
+// SkipZeroData of every contraction of the batch (one test launch, one
+// synchronisation), then the final Permute(P) and the result tensors.
+static void finish(Ctx *ctx, const std::vector<Prepared *> &batch) {
+  if (batch.empty()) return;
+  std::vector<int64_t> offs, sizes;
+  std::vector<int64_t> first(batch.size() + 1, 0);
+  double *base = batch[0]->dC;
+  for (Prepared *w : batch) base = std::min(base, w->dC);
+  const int64_t eb = batch[0]->cplx ? 16 : 8;
+  for (size_t r = 0; r < batch.size(); ++r) {
+    const ContractPlan &pl = batch[r]->pl;
+    const int64_t dc = (int64_t)((const char *)batch[r]->dC - (const char *)base) / eb;
+    for (int64_t i = 0; i < pl.C.nblk; ++i) {
+      offs.push_back(pl.C.offs[i] + dc);
+      sizes.push_back(pl.C.bsize(i));
+    }
+    first[r + 1] = (int64_t)offs.size();
+  }
+  const int64_t nb = (int64_t)offs.size();
+  int64_t *doff = dev_upload(ctx, offs), *dsz = dev_upload(ctx, sizes);
   int *dflag = dev_alloc<int>(ctx, nb);
-  launch_block_nonzero(ctx, doff, dsz, nb, dC, cplx ? 1 : 0, dflag);
+  launch_block_nonzero(ctx, doff, dsz, nb, base, batch[0]->cplx ? 1 : 0, dflag);
   std::vector<int> flags(nb);
   int kerr = 0;
   QS_CUDA(cudaMemcpyAsync(flags.data(), dflag, nb * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QS_CUDA(cudaMemcpyAsync(&kerr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, doff);
+  dev_free(ctx, dsz);
+  dev_free(ctx, dflag);
   if (kerr) {
     QS_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     fail(QS_ERR_TIMEOUT, "a bounded device wait ran out (code %d)", kerr);
   }
-  dev_free(ctx, doff);
-  dev_free(ctx, dsz);
-  dev_free(ctx, dflag);
-  std::vector<int64_t> keep;
-  for (int64_t i = 0; i < nb; ++i)
-    if (flags[i]) keep.push_back(i);
-  if ((int64_t)keep.size() < nb && pl.rc == 2) {
-    std::vector<double> h((size_t)pl.C.nelem * es);
-    QS_CUDA(cudaMemcpyAsync(h.data(), dC, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    QS_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (rank2_keeps_zero_blocks(pl.C, h)) {
-      keep.resize(nb);
-      std::iota(keep.begin(), keep.end(), 0);
-    }
-  }
-
-  auto T = std::make_unique<qs_tensor>();
-  T->ctx = ctx;
-  QMeta &M = T->meta;
-  M.rank = pl.rc;
-  M.qdim = pl.C.qdim;
-  // output itags, permuted like the legs (QSpace::Permute)
-  if (!pl.C.itags.empty()) {
-    if (pl.P.empty()) M.itags = pl.C.itags;
-    else
-      for (int k = 0; k < pl.rc; ++k) M.itags.push_back(pl.C.itags[pl.P[k]]);
-  }
-  M.cplx = cplx;
-  M.nblk = (int64_t)keep.size();
-  const int r = pl.rc, qd = pl.C.qdim;
-  if (keep.empty()) {
-    dev_free(ctx, dC);
-    M.rank = 0;
-    if (stats) stats->launches = (int32_t)(ctx->launches - launches0);
-    return T;
-  }
-  if (pl.P.empty()) {
-    for (int64_t i : keep) {
-      M.q.insert(M.q.end(), pl.C.qrow(i), pl.C.qrow(i) + r * qd);
-      M.dims.insert(M.dims.end(), pl.C.drow(i), pl.C.drow(i) + r);
-      M.offs.push_back(pl.C.offs[i]);
-    }
-    M.nelem = pl.C.nelem;
-    T->d = dC;
-  } else {
-    // Permute(P) of labels and data (Source/QSpace.hh:2670-2719); the block
-    // order is not changed.
-    std::vector<int64_t> noffs;
-    int64_t ne = 0;
-    for (int64_t i : keep) {
-      for (int k = 0; k < r; ++k) {
-        const int32_t *src = pl.C.qrow(i) + pl.P[k] * qd;
-        M.q.insert(M.q.end(), src, src + qd);
-        M.dims.push_back(pl.C.drow(i)[pl.P[k]]);
+  for (size_t r = 0; r < batch.size(); ++r) {
+    Prepared &w = *batch[r];
+    const ContractPlan &pl = w.pl;
+    const bool cplx = w.cplx;
+    const int es = cplx ? 2 : 1;
+    const int64_t nbr = pl.C.nblk;
+    std::vector<int64_t> keep;
+    for (int64_t i = 0; i < nbr; ++i)
+      if (flags[first[r] + i]) keep.push_back(i);
+    if ((int64_t)keep.size() < nbr && pl.rc == 2) {
+      std::vector<double> h((size_t)pl.C.nelem * es);
+      QS_CUDA(cudaMemcpyAsync(h.data(), w.dC, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      QS_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (rank2_keeps_zero_blocks(pl.C, h)) {
+        keep.resize(nbr);
+        std::iota(keep.begin(), keep.end(), 0);
       }
-      noffs.push_back(ne);
-      ne += pl.C.bsize(i);
     }
-    M.offs = noffs;
-    M.nelem = ne;
-    double *dP = dev_alloc<double>(ctx, (size_t)ne * es);
-    std::vector<PermDesc> pd = make_perm_descs(pl.C, pl.P, false, noffs, &keep);
-    run_permute(ctx, pd, dC, dP, cplx);
-    dev_free(ctx, dC);
-    T->d = dP;
+    auto T = std::make_unique<qs_tensor>();
+    T->ctx = ctx;
+    QMeta &M = T->meta;
+    M.rank = pl.rc;
+    M.qdim = pl.C.qdim;
+    // output itags, permuted like the legs (QSpace::Permute)
+    if (!pl.C.itags.empty()) {
+      if (pl.P.empty()) M.itags = pl.C.itags;
+      else
+        for (int k = 0; k < pl.rc; ++k) M.itags.push_back(pl.C.itags[pl.P[k]]);
+    }
+    M.cplx = cplx;
+    M.nblk = (int64_t)keep.size();
+    const int rk = pl.rc, qd = pl.C.qdim;
+    if (keep.empty()) {
+      dev_free(ctx, w.dC);
+      w.dC = nullptr;
+      M.rank = 0;
+    } else if (pl.P.empty()) {
+      for (int64_t i : keep) {
+        M.q.insert(M.q.end(), pl.C.qrow(i), pl.C.qrow(i) + rk * qd);
+        M.dims.insert(M.dims.end(), pl.C.drow(i), pl.C.drow(i) + rk);
+        M.offs.push_back(pl.C.offs[i]);
+      }
+      M.nelem = pl.C.nelem;
+      T->d = w.dC;
+      w.dC = nullptr;
+    } else {
+      // Permute(P) of labels and data (Source/QSpace.hh:2670-2719); the block
+      // order is not changed.
+      std::vector<int64_t> noffs;
+      int64_t ne = 0;
+      for (int64_t i : keep) {
+        for (int k = 0; k < rk; ++k) {
+          const int32_t *src = pl.C.qrow(i) + pl.P[k] * qd;
+          M.q.insert(M.q.end(), src, src + qd);
+          M.dims.push_back(pl.C.drow(i)[pl.P[k]]);
+        }
+        noffs.push_back(ne);
+        ne += pl.C.bsize(i);
+      }
+      M.offs = noffs;
+      M.nelem = ne;
+      double *dP = dev_alloc<double>(ctx, (size_t)ne * es);
+      std::vector<PermDesc> pd = make_perm_descs(pl.C, pl.P, false, noffs, &keep);
+      run_permute(ctx, pd, w.dC, dP, cplx);
+      dev_free(ctx, w.dC);
+      w.dC = nullptr;
+      T->d = dP;
+    }
+    w.done = std::move(T);
+  }
+}
+
+static void release(Ctx *ctx, Prepared &w) {
+  for (void *p : w.tmp) dev_free(ctx, p);
+  w.tmp.clear();
+  if (w.dC) dev_free(ctx, w.dC);
+  w.dC = nullptr;
+}
+
+// The device contraction driver shared by the host and device entry points.
+std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double *dA,
+                                                const QMeta &Bm, const double *dB, const char *ia,
+                                                const char *ib, const int32_t *perm, int32_t nperm,
+                                                const qs_opts *opts, qs_stats *stats) {
+  const int64_t launches0 = ctx->launches;
+  Prepared w;
+  if (stats) std::memset(stats, 0, sizeof *stats);
+  try {
+    prepare(ctx, w, Am, dA, Bm, dB, ia, ib, perm, nperm);
+    if (stats) {
+      stats->flops = w.pl.flops;
+      stats->bytes = w.pl.bytes;
+      stats->npairs = (int64_t)w.pl.pairs.size();
+    }
+    if (!w.done) {
+      std::vector<Prepared *> one{&w};
+      run_products(ctx, one, opts, stats);
+      finish(ctx, one);
+    }
+  } catch (...) {
+    release(ctx, w);
+    throw;
   }
   if (stats) {
-    stats->nblk_out = M.nblk;
+    stats->nblk_out = w.done->meta.nblk;
     stats->launches = (int32_t)(ctx->launches - launches0);
   }
-  return T;
+  return std::move(w.done);
+}
+
+// A batch of contractions: the block products of all of them run in one
+// grouped launch per result element type and, on the split path, per digit
+// plan -- each contraction keeps the plan it would get alone, so every
+// result is bit-identical to the same contraction run alone.  out[r]
+// receives contraction r's result.
+void contract_batch_core(Ctx *ctx, int n, const QMeta *const *Am, const double *const *dA,
+                         const QMeta *const *Bm, const double *const *dB, const char *const *ia,
+                         const char *const *ib, const int32_t *const *perm, const int32_t *nperm,
+                         const qs_opts *opts, std::vector<std::unique_ptr<qs_tensor>> &out) {
+  std::vector<Prepared> ws(n);
+  try {
+    for (int r = 0; r < n; ++r)
+      prepare(ctx, ws[r], *Am[r], dA[r], *Bm[r], dB[r], ia[r], ib[r], perm ? perm[r] : nullptr,
+              nperm ? nperm[r] : 0);
+    const bool split = opts && opts->prec == QS_PREC_SPLIT;
+    std::vector<std::pair<int, int>> plan(n, {0, 0});  // (slices, bits)
+    if (split)
+      for (int r = 0; r < n; ++r)
+        if (!ws[r].done) {
+          const ContractPlan &pl = ws[r].pl;
+          const DigitPlan dp = choose_digits_for(pl.pairs, pl.grp, pl.blk_M, pl.blk_N, ws[r].cplx ? 2 : 1,
+                                                 opts->tol > 0 ? opts->tol : 1e-12, opts->nslices);
+          plan[r] = {dp.nslices, dp.bits};
+        }
+    std::vector<char> ran(n, 0);
+    for (int r = 0; r < n; ++r) {
+      if (ws[r].done || ran[r]) continue;
+      std::vector<Prepared *> batch;
+      for (int q = r; q < n; ++q)
+        if (!ws[q].done && !ran[q] && ws[q].cplx == ws[r].cplx && plan[q] == plan[r]) {
+          batch.push_back(&ws[q]);
+          ran[q] = 1;
+        }
+      run_products(ctx, batch, opts, nullptr, plan[r].first, plan[r].second);
+      finish(ctx, batch);
+    }
+  } catch (...) {
+    for (Prepared &w : ws) release(ctx, w);
+    throw;
+  }
+  out.clear();
+  for (Prepared &w : ws) out.push_back(std::move(w.done));
 }
 
 int64_t contract_footprint(const QMeta &Am, const QMeta &Bm, const char *ia, const char *ib,
@@ -690,6 +838,31 @@ qs_status qs_result_itags(const qs_result *C, char *buf, size_t len) {
 }
 
 void qs_tensor_free(qs_tensor *T) { delete T; }
+
+qs_status qs_contract_batch(qs_ctx *ctx, int32_t n, const qs_tensor *const *A, const char *const *ia,
+                            const qs_tensor *const *B, const char *const *ib, const int32_t *const *perm,
+                            const int32_t *nperm, const qs_opts *opts, qs_tensor **C) {
+  QS_API_BEGIN
+  if (!ctx || !A || !ia || !B || !ib || !C) fail(QS_ERR_ARG, "null argument");
+  if (n < 0) fail(QS_ERR_ARG, "negative batch size");
+  for (int r = 0; r < n; ++r) {
+    C[r] = nullptr;
+    if (!A[r] || !B[r] || !ia[r] || !ib[r]) fail(QS_ERR_ARG, "null operand %d", r);
+  }
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  std::vector<const QMeta *> am(n), bm(n);
+  std::vector<const double *> ad(n), bd(n);
+  for (int r = 0; r < n; ++r) {
+    am[r] = &A[r]->meta;
+    bm[r] = &B[r]->meta;
+    ad[r] = A[r]->d;
+    bd[r] = B[r]->d;
+  }
+  std::vector<std::unique_ptr<qs_tensor>> out;
+  contract_batch_core(&ctx->c, n, am.data(), ad.data(), bm.data(), bd.data(), ia, ib, perm, nperm, opts, out);
+  for (int r = 0; r < n; ++r) C[r] = out[r].release();
+  QS_API_END
+}
 
 qs_status qs_contract_itags(qs_ctx *ctx, int32_t n, const qs_tensor *const *T, const int32_t *conj,
                             const int32_t *perm, int32_t nperm, const qs_opts *opts, qs_tensor **C) {

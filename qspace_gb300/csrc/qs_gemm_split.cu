@@ -970,7 +970,7 @@ static double drain_units() {
 
 DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                             const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
-                            double tol, int forced_slices, int forced_bits = 0) {
+                            double tol, int forced_slices, int forced_bits) {
   if (!(tol > 0)) tol = 1e-12;
   // bits of precision wanted: the tolerance plus a margin for the growth of
   // the error with the summed depth relative to |C|.
@@ -1199,9 +1199,10 @@ static void launch_split(Ctx *ctx, const SplitWork &w, bool cplx, const SplitDev
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                       const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                       const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
-                      bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc) {
+                      bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
+                      int forced_bits) {
   SplitWork w;
-  SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w);
+  SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w, forced_bits);
   if (w.tiles.empty()) return res;
   // device buffers: one allocation for the digit arena (pooled scratch)
   SplitDev d;

@@ -29,6 +29,12 @@ std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double
                                          const double *dB, const char *ia, const char *ib,
                                          const int32_t *perm, int32_t nperm, const qs_opts *opts,
                                          qs_stats *stats);
+// A batch of contractions whose block products share one grouped launch per
+// element type (and digit plan); out[r] receives contraction r's result.
+void contract_batch_core(Ctx *ctx, int n, const QMeta *const *Am, const double *const *dA,
+                         const QMeta *const *Bm, const double *const *dB, const char *const *ia,
+                         const char *const *ib, const int32_t *const *perm, const int32_t *nperm,
+                         const qs_opts *opts, std::vector<std::unique_ptr<qs_tensor>> &out);
 // Device bytes a contraction will hold while it runs (output, operand
 // copies, digit arena): the admission footprint of the serving loop.
 int64_t contract_footprint(const QMeta &Am, const QMeta &Bm, const char *ia, const char *ib,

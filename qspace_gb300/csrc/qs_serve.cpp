@@ -8,9 +8,11 @@
 //  * nslots worker threads each own a stream, a scratch arena and an error
 //    word (a qs::Ctx).  A worker takes the head of the queue as soon as the
 //    request's device footprint fits into the HBM budget next to the
-//    requests already running, so requests that arrive while others are on
-//    the GPU are admitted as slots and memory free up, and their kernels
-//    overlap on the device.  A request larger than the whole budget is
+//    requests already running, together with up to max_batch - 1 further
+//    queued requests with the same options that also fit; the block
+//    products of the whole batch run in one grouped launch.  Requests that
+//    arrive while others are on the GPU are admitted as slots and memory
+//    free up, and their kernels overlap on the device.  A request larger than the whole budget is
 //    refused at submit time (QS_ERR_OOM).
 //  * Results are identical alone and in the mix: every kernel is
 //    deterministic (fixed reduction order) and requests share no buffers.
@@ -65,52 +67,123 @@ struct qs_server {
   int64_t budget = 0, in_use = 0;
   bool stop = false;
 
+  int max_batch = 16;
+
+  static bool same_opts(const Request &a, const Request &b) {
+    if (a.has_opts != b.has_opts) return false;
+    if (!a.has_opts) return true;
+    return a.opts.prec == b.opts.prec && a.opts.nslices == b.opts.nslices && a.opts.tol == b.opts.tol;
+  }
+
+  // Completes one request (under the lock).
+  void complete(Request &r, qs_status st, const std::string &msg, qs_tensor *C) {
+    in_use -= r.footprint;
+    r.latency_ms = std::chrono::duration<double, std::milli>(clk::now() - r.t_submit).count();
+    r.status = st;
+    r.err = msg;
+    r.C = C;
+    r.state = st == QS_OK ? Request::DONE : Request::FAILED;
+    if (r.ready) {
+      cudaEventDestroy(r.ready);
+      r.ready = nullptr;
+    }
+  }
+
   void worker(Ctx *slot) {
     cudaSetDevice(slot->device);
     for (;;) {
-      std::shared_ptr<Request> r;
+      std::vector<std::shared_ptr<Request>> batch;
       {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait(lk, [&] {
           return stop || (!queue.empty() && in_use + queue.front()->footprint <= budget);
         });
         if (stop) return;
-        r = queue.front();
+        batch.push_back(queue.front());
         queue.pop_front();
-        in_use += r->footprint;
-        r->state = Request::RUNNING;
+        in_use += batch[0]->footprint;
+        // continuous batching: queued requests with the same options that
+        // fit next to it join the launch
+        for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < max_batch;) {
+          if (same_opts(**it, *batch[0]) && in_use + (*it)->footprint <= budget) {
+            in_use += (*it)->footprint;
+            batch.push_back(*it);
+            it = queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+        for (auto &r : batch) r->state = Request::RUNNING;
       }
-      qs_status st = QS_OK;
-      std::string msg;
-      qs_tensor *C = nullptr;
+      const int n = (int)batch.size();
+      std::vector<qs_status> st(n, QS_OK);
+      std::vector<std::string> msg(n);
+      std::vector<qs_tensor *> C(n, nullptr);
+      auto run_alone = [&](int k) {
+        Request &r = *batch[k];
+        try {
+          auto T = contract_core(slot, r.A->meta, r.A->d, r.B->meta, r.B->d, r.ia.c_str(), r.ib.c_str(),
+                                 r.perm.empty() ? nullptr : r.perm.data(), (int32_t)r.perm.size(),
+                                 r.has_opts ? &r.opts : nullptr, nullptr);
+          QS_CUDA(cudaStreamSynchronize(slot->stream));
+          T->ctx = &parent->c;  // the caller frees the result on the parent context's stream
+          C[k] = T.release();
+        } catch (const Error &e) {
+          st[k] = e.code;
+          msg[k] = e.what();
+        } catch (const std::exception &e) {
+          st[k] = QS_ERR_INTERNAL;
+          msg[k] = e.what();
+        }
+      };
       try {
-        if (r->ready) QS_CUDA(cudaStreamWaitEvent(slot->stream, r->ready, 0));
-        auto T = contract_core(slot, r->A->meta, r->A->d, r->B->meta, r->B->d, r->ia.c_str(), r->ib.c_str(),
-                               r->perm.empty() ? nullptr : r->perm.data(), (int32_t)r->perm.size(),
-                               r->has_opts ? &r->opts : nullptr, nullptr);
-        QS_CUDA(cudaStreamSynchronize(slot->stream));
-        // the caller frees the result on the parent context's stream
-        T->ctx = &parent->c;
-        C = T.release();
+        for (auto &r : batch)
+          if (r->ready) QS_CUDA(cudaStreamWaitEvent(slot->stream, r->ready, 0));
+        if (n == 1) {
+          run_alone(0);
+        } else {
+          std::vector<const QMeta *> am(n), bm(n);
+          std::vector<const double *> ad(n), bd(n);
+          std::vector<const char *> ia(n), ib(n);
+          std::vector<const int32_t *> pp(n);
+          std::vector<int32_t> np(n);
+          for (int k = 0; k < n; ++k) {
+            const Request &r = *batch[k];
+            am[k] = &r.A->meta;
+            bm[k] = &r.B->meta;
+            ad[k] = r.A->d;
+            bd[k] = r.B->d;
+            ia[k] = r.ia.c_str();
+            ib[k] = r.ib.c_str();
+            pp[k] = r.perm.empty() ? nullptr : r.perm.data();
+            np[k] = (int32_t)r.perm.size();
+          }
+          std::vector<std::unique_ptr<qs_tensor>> out;
+          try {
+            contract_batch_core(slot, n, am.data(), ad.data(), bm.data(), bd.data(), ia.data(), ib.data(),
+                                pp.data(), np.data(), batch[0]->has_opts ? &batch[0]->opts : nullptr, out);
+            QS_CUDA(cudaStreamSynchronize(slot->stream));
+            for (int k = 0; k < n; ++k) {
+              out[k]->ctx = &parent->c;
+              C[k] = out[k].release();
+            }
+          } catch (...) {
+            // a failed batch: each request again on its own, so that every
+            // request gets its own status
+            cudaStreamSynchronize(slot->stream);
+            cudaGetLastError();
+            for (int k = 0; k < n; ++k) run_alone(k);
+          }
+        }
       } catch (const Error &e) {
-        st = e.code;
-        msg = e.what();
-      } catch (const std::exception &e) {
-        st = QS_ERR_INTERNAL;
-        msg = e.what();
+        for (int k = 0; k < n; ++k) {
+          st[k] = e.code;
+          msg[k] = e.what();
+        }
       }
       {
         std::lock_guard<std::mutex> lk(mu);
-        in_use -= r->footprint;
-        r->latency_ms = std::chrono::duration<double, std::milli>(clk::now() - r->t_submit).count();
-        r->status = st;
-        r->err = msg;
-        r->C = C;
-        r->state = st == QS_OK ? Request::DONE : Request::FAILED;
-        if (r->ready) {
-          cudaEventDestroy(r->ready);
-          r->ready = nullptr;
-        }
+        for (int k = 0; k < n; ++k) complete(*batch[k], st[k], msg[k], C[k]);
       }
       cv_done.notify_all();
       cv_work.notify_all();
@@ -129,6 +202,8 @@ qs_status qs_server_create(qs_ctx *ctx, const qs_server_cfg *cfg, qs_server **ou
   auto s = std::make_unique<qs_server>();
   s->parent = ctx;
   s->budget = cfg->hbm_budget;
+  if (cfg->max_batch < 0 || cfg->max_batch > 1024) fail(QS_ERR_ARG, "max_batch must be in 0..1024");
+  if (cfg->max_batch > 0) s->max_batch = cfg->max_batch;
   for (int i = 0; i < cfg->nslots; ++i) {
     auto c = std::make_unique<Ctx>();
     c->device = ctx->c.device;

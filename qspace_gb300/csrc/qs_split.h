@@ -25,13 +25,18 @@ struct DigitPlan {
   double err_bound;
 };
 DigitPlan choose_digits(int64_t kreal, double tol, int forced_slices);
+// The digit plan the split path picks for a grouped product (cm = 2 for
+// complex), optionally with the digit count and/or width forced.
+DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                            const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
+                            double tol, int forced_slices, int forced_bits = 0);
 
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs,
                       const std::vector<int64_t> &grp, const std::vector<int32_t> &blk_M,
                       const std::vector<int32_t> &blk_N, const std::vector<int64_t> &c_off,
                       const double *A, const double *B, double *C, bool cplx,
                       int forced_slices, double tol,
-                      const std::vector<int32_t> *blk_ldc = nullptr);
+                      const std::vector<int32_t> *blk_ldc = nullptr, int forced_bits = 0);
 
 // The same product with every device buffer carved from caller-provided
 // scratch (`cap` bytes, 256-byte aligned) instead of allocated; the bounded

@@ -191,6 +191,16 @@ def make_opts(prec: str = "fp64", nslices: int = 0, tol: float = 1e-12, flags: i
     return o
 
 
+def _perm_list(perm) -> list:
+    """1-based permutation as a list of ints ('312', '3,1,2' or a sequence)."""
+    if isinstance(perm, str):
+        s = perm.strip()
+        if any(c in s for c in ",; "):
+            return [int(x) for x in s.replace(",", " ").replace(";", " ").split()]
+        return [int(c) for c in s]
+    return [int(x) for x in np.atleast_1d(perm)]
+
+
 def _perm_arg(perm):
     if perm is None:
         return None, 0
@@ -349,6 +359,26 @@ def contract_dev(A: Tensor, ia, B: Tensor, ib, perm=None, *, prec: str = "fp64",
     if stats is not None:
         stats.update(st.as_dict())
     return Tensor(ctx, h)
+
+
+def contract_batch(jobs, *, prec: str = "fp64", nslices: int = 0, tol: float = 1e-12) -> list:
+    """Device-resident contractions [(A, ia, B, ib[, perm]), ...] whose block
+    products share one grouped launch (qs_contract_batch).  Returns Tensors."""
+    if not jobs:
+        return []
+    ctx = jobs[0][0].ctx
+    n = len(jobs)
+    A = (C.c_void_p * n)(*[j[0].h.value for j in jobs])
+    B = (C.c_void_p * n)(*[j[2].h.value for j in jobs])
+    ia = (C.c_char_p * n)(*[_idx_str(j[1]) for j in jobs])
+    ib = (C.c_char_p * n)(*[_idx_str(j[3]) for j in jobs])
+    perms = [np.asarray(_perm_list(j[4]) if len(j) > 4 and j[4] is not None else [], np.int32) for j in jobs]
+    P = (_capi.c_int32_p * n)(*[p.ctypes.data_as(_capi.c_int32_p) if p.size else None for p in perms])
+    NP = np.array([p.size for p in perms], np.int32)
+    out = (C.c_void_p * n)()
+    check(ctx.lib.qs_contract_batch(ctx.h, n, A, ia, B, ib, P, NP.ctypes.data_as(_capi.c_int32_p),
+                                    C.byref(make_opts(prec, nslices, tol)), out))
+    return [Tensor(ctx, C.c_void_p(out[r])) for r in range(n)]
 
 
 def _cell_items(items):

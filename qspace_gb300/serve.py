@@ -17,10 +17,12 @@ from .qspace import Context, Tensor, _idx_str, _perm_arg, default_context, make_
 
 
 class Server:
-    def __init__(self, nslots: int = 4, hbm_budget: int = 8 << 30, ctx: Context | None = None):
+    def __init__(self, nslots: int = 4, hbm_budget: int = 8 << 30, ctx: Context | None = None,
+                 max_batch: int = 0):
         self.ctx = ctx or default_context()
         cfg = ServerCfg()
         cfg.nslots = nslots
+        cfg.max_batch = max_batch
         cfg.hbm_budget = int(hbm_budget)
         h = C.c_void_p()
         check(self.ctx.lib.qs_server_create(self.ctx.h, C.byref(cfg), C.byref(h)))
