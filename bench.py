@@ -23,6 +23,7 @@ ranks' flops / max time over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -422,6 +423,54 @@ def main():
                 ts.append(time.perf_counter() - t0)
             rdm[pr + "_ms_p50"] = 1e3 * statistics.median(ts)
 
+    # ---- FP64 block eigendecompositions of one NRG step (SURVEY config 3,
+    # abelian stand-in): every symmetry block of a 39300-state Hamiltonian,
+    # 336 blocks of sizes 1..690, on the device; eig flops = sum (10/3) n^3
+    eig = None
+    if not a.no_extras:
+        from qspace_gb300.workloads import nrg_eig_blocks
+        blocks = nrg_eig_blocks(0)
+        n_ = np.array([b_.shape[0] for b_ in blocks], np.int64)
+        sz_ = n_ * n_
+        offs_ = np.concatenate([[0], np.cumsum(sz_)[:-1]]).astype(np.int64)
+        eoffs_ = np.concatenate([[0], np.cumsum(n_)[:-1]]).astype(np.int64)
+        Hh = np.concatenate([b_.reshape(-1, order="F") for b_ in blocks])
+        dH = torch.from_numpy(Hh).to("cuda")
+        dU = torch.empty_like(dH)
+        dE = torch.empty(int(n_.sum()), dtype=torch.float64, device="cuda")
+        p64 = lambda x: x.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
+
+        def eig_call():
+            r_ = ctx.lib.qs_eig_blocks(ctx.h, len(blocks), p64(n_), p64(offs_), p64(eoffs_),
+                                       C.c_void_p(dH.data_ptr()), C.c_void_p(dE.data_ptr()),
+                                       C.c_void_p(dU.data_ptr()), 0)
+            if r_:
+                raise RuntimeError(ctx.lib.qs_last_error().decode())
+
+        torch.cuda.synchronize()
+        eig_call()
+        ets = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            eig_call()
+            ets.append(time.perf_counter() - t0)
+        ems = 1e3 * statistics.median(ets)
+        eflops = float(np.sum(10.0 / 3.0 * n_.astype(float) ** 3))
+        Eh = dE.cpu().numpy()
+        big = int(np.argmax(n_))
+        ref_e = np.linalg.eigvalsh(blocks[big])
+        eerr = float(np.max(np.abs(Eh[eoffs_[big]:eoffs_[big] + n_[big]] - ref_e)) / np.max(np.abs(ref_e)))
+        eig = {"workload": "NRG step eig: 336 real symmetric blocks, 39300 states, sizes 1..690",
+               "ms": ems, "tflops": eflops / (ems * 1e-3) / 1e12, "max_rel_eig_err_largest_block": eerr}
+        if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+            out_ = subprocess.run([sys.executable, "-m", "oracle.cpu_baseline", "--eig", "--steps", "2",
+                                   "--max-seconds", "30"], cwd=ROOT, capture_output=True, text=True)
+            if out_.returncode == 0:
+                cb_ = json.loads(out_.stdout.strip().splitlines()[-1])
+                eig["cpu_baseline"] = {"ms": cb_["seconds_per_step"] * 1e3, "tflops": cb_["value"],
+                                       "cores": cb_["cores"], "kind": "port"}
+        del dH, dU, dE
+
     # ---- serving loop under Poisson load (split and plain), device-resident tensors
     serving = None
     if rank == 0 and not a.no_extras:
@@ -475,7 +524,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "slices": slices, "rdm_latency": rdm, "serving": serving,
+                "slices": slices, "rdm_latency": rdm, "eig": eig, "serving": serving,
                 "clocks": ck}
         print(json.dumps(line))
     if pg:

@@ -75,6 +75,7 @@ struct Ctx {
   void destroy_copy_streams();
   // cuSOLVER handle (created on first use)
   void *solver = nullptr;
+  void *solver_lanes = nullptr;  // extra solver streams for concurrent blocks
   // phase timing: events around operand preparation and the GEMM kernel
   bool timing = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

@@ -15,6 +15,10 @@
 //    v /= |v|; FP64 dot/axpy kernels (memory bound).
 #include <cusolverDn.h>
 
+#include <cstdlib>
+#include <exception>
+#include <thread>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -46,9 +50,45 @@ cusolverDnHandle_t solver_of(Ctx *ctx) {
   return h;
 }
 
+// Solver lanes: streams with their own cuSOLVER handles, driven from their
+// own host threads, so that the decompositions of independent symmetry
+// blocks run concurrently (the solver synchronises with its stream inside
+// each call, and one medium-size call keeps only part of the GPU busy).
+constexpr int NLANES = 8;
+struct SolverLanes {
+  cudaStream_t st[NLANES] = {};
+  cusolverDnHandle_t h[NLANES] = {};
+  cudaEvent_t ev[NLANES] = {};
+};
+
+static SolverLanes *lanes_of(Ctx *ctx) {
+  if (!ctx->solver_lanes) {
+    auto L = new SolverLanes;
+    ctx->solver_lanes = L;
+    for (int i = 0; i < NLANES; ++i) {
+      QS_CUDA(cudaStreamCreateWithFlags(&L->st[i], cudaStreamNonBlocking));
+      QS_SOLVER(cusolverDnCreate(&L->h[i]));
+      QS_SOLVER(cusolverDnSetStream(L->h[i], L->st[i]));
+      QS_CUDA(cudaEventCreateWithFlags(&L->ev[i], cudaEventDisableTiming));
+    }
+  }
+  return static_cast<SolverLanes *>(ctx->solver_lanes);
+}
+
 void destroy_solver(Ctx *ctx) {
   if (ctx->solver) cusolverDnDestroy(static_cast<cusolverDnHandle_t>(ctx->solver));
   ctx->solver = nullptr;
+  if (ctx->solver_lanes) {
+    auto L = static_cast<SolverLanes *>(ctx->solver_lanes);
+    for (int i = 0; i < NLANES; ++i) {
+      if (L->st[i]) cudaStreamSynchronize(L->st[i]);
+      if (L->h[i]) cusolverDnDestroy(L->h[i]);
+      if (L->ev[i]) cudaEventDestroy(L->ev[i]);
+      if (L->st[i]) cudaStreamDestroy(L->st[i]);
+    }
+    delete L;
+    ctx->solver_lanes = nullptr;
+  }
 }
 
 namespace {
@@ -239,32 +279,89 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
   }
   int *d_info = dev_alloc<int>(ctx, (size_t)std::max<int64_t>(nblk, 1));
   QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * std::max<int64_t>(nblk, 1), ctx->stream));
-  // large blocks: syevd
-  int64_t nmax = 0;
-  for (int64_t i : large) nmax = std::max(nmax, n[i]);
-  if (nmax > 0) {
-    int lwork = 0;
-    const int nm = (int)nmax;
-    if (cplx)
-      QS_SOLVER(cusolverDnZheevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm,
-                                            reinterpret_cast<cuDoubleComplex *>(U), nm, E, &lwork));
-    else
-      QS_SOLVER(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm, U, nm, E, &lwork));
-    // the workspace for the largest size bounds the smaller ones
-    double *work = dev_alloc<double>(ctx, (size_t)std::max(lwork, 1) * es);
+  // large blocks: syevd, spread over the solver lanes (largest first, each
+  // to the lane with the least work so far), concurrent with the batched
+  // Jacobi of the small blocks on the context stream
+  std::vector<double *> works;
+  std::vector<int> used;
+  SolverLanes *L = nullptr;
+  if (!large.empty()) {
+    L = lanes_of(ctx);
+    std::sort(large.begin(), large.end(), [&](int64_t x, int64_t y) { return n[x] > n[y]; });
+    // QS_EIG_LANES (1..8) overrides the number of concurrent lanes for tuning
+    const char *el = std::getenv("QS_EIG_LANES");
+    const int want = el ? std::max(1, std::min(NLANES, std::atoi(el))) : NLANES;
+    const int nl = (int)std::min<size_t>(want, large.size());
+    std::vector<std::vector<int64_t>> part(nl);
+    std::vector<double> load(nl, 0.0);
     for (int64_t i : large) {
-      const int ni = (int)n[i];
-      if (cplx)
-        QS_SOLVER(cusolverDnZheevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
-                                   reinterpret_cast<cuDoubleComplex *>(U) + offs[i], ni, E + eoffs[i],
-                                   reinterpret_cast<cuDoubleComplex *>(work), lwork, d_info + i));
-      else
-        QS_SOLVER(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni, U + offs[i] * es, ni,
-                                   E + eoffs[i], work, lwork, d_info + i));
-      ctx->launches++;
+      const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      part[l].push_back(i);
+      load[l] += double(n[i]) * n[i] * n[i];
     }
-    dev_free(ctx, work);
+    // workspaces (allocated on the context stream, before the fork)
+    std::vector<int> lwork(nl, 0);
+    for (int l = 0; l < nl; ++l) {
+      const int nm = (int)n[part[l][0]];  // the lane's largest block bounds its workspace
+      if (cplx)
+        QS_SOLVER(cusolverDnZheevd_bufferSize(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm,
+                                              reinterpret_cast<cuDoubleComplex *>(U), nm, E, &lwork[l]));
+      else
+        QS_SOLVER(cusolverDnDsyevd_bufferSize(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm, U, nm, E,
+                                              &lwork[l]));
+      works.push_back(dev_alloc<double>(ctx, (size_t)std::max(lwork[l], 1) * es));
+    }
+    cudaEvent_t fork;
+    QS_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    QS_CUDA(cudaEventRecord(fork, ctx->stream));
+    // one host thread per lane: the solver synchronises with its stream
+    // inside each call, so lanes driven from one thread would not overlap
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> errs(nl);
+    const int dev = ctx->device;
+    for (int l = 0; l < nl; ++l) {
+      QS_CUDA(cudaStreamWaitEvent(L->st[l], fork, 0));
+      used.push_back(l);
+      th.emplace_back([&, l]() {
+        try {
+          QS_CUDA(cudaSetDevice(dev));
+          for (int64_t i : part[l]) {
+            const int ni = (int)n[i];
+            if (cplx)
+              QS_SOLVER(cusolverDnZheevd(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
+                                         reinterpret_cast<cuDoubleComplex *>(U) + offs[i], ni, E + eoffs[i],
+                                         reinterpret_cast<cuDoubleComplex *>(works[l]), lwork[l], d_info + i));
+            else
+              QS_SOLVER(cusolverDnDsyevd(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
+                                         U + offs[i] * es, ni, E + eoffs[i], works[l], lwork[l], d_info + i));
+          }
+          QS_CUDA(cudaEventRecord(L->ev[l], L->st[l]));
+        } catch (...) {
+          errs[l] = std::current_exception();
+        }
+      });
+      ctx->launches += (int64_t)part[l].size();
+    }
+    for (auto &t : th) t.join();
+    cudaEventDestroy(fork);
+    for (auto &e : errs)
+      if (e) {
+        for (int l : used) cudaStreamSynchronize(L->st[l]);
+        used.clear();
+        for (double *w : works) dev_free(ctx, w);
+        works.clear();
+        std::rethrow_exception(e);
+      }
   }
+  // rejoins the lanes on the context stream (also on the error path, so that
+  // the workspaces are not released while a lane still uses them)
+  auto join = [&]() {
+    for (int l : used) cudaStreamWaitEvent(ctx->stream, L->ev[l], 0);
+    used.clear();
+    for (double *w : works) dev_free(ctx, w);
+    works.clear();
+  };
+  try {
   // small blocks: batched Jacobi on contiguous copies
   if (!small.empty()) {
     syevjInfo_t params;
@@ -326,6 +423,11 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
     }
     cusolverDnDestroySyevjInfo(params);
   }
+  } catch (...) {
+    join();
+    throw;
+  }
+  join();
   std::vector<int> info(std::max<int64_t>(nblk, 1));
   QS_CUDA(cudaMemcpyAsync(info.data(), d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QS_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -115,3 +115,20 @@ def random_leg(rng: np.random.Generator, nsec: int = 4, dmax: int = 5, qdim: int
     while len(labs) < nsec:
         labs.add(tuple(int(x) for x in rng.integers(-qmax, qmax + 1, size=qdim)))
     return [(lab, int(rng.integers(1, dmax + 1))) for lab in sorted(labs)]
+
+
+def nrg_eig_blocks(seed: int = 0, dmax: int = 700, sigma: float = 3.0):
+    """Real symmetric Hamiltonian blocks of one NRG step (abelian stand-in):
+    one block per (charge q in [-12, 12], 2Sz in -15..15 step 2) sector with
+    dimension round(dmax exp(-(q^2 + Sz^2) / (2 sigma^2))) -- 336 blocks of
+    uneven sizes 1..690, 39300 states -- entries N(0,1), symmetrised."""
+    rng = np.random.default_rng(seed)
+    blocks = []
+    for q in range(-12, 13):
+        for s2 in range(-15, 16, 2):
+            d = int(round(dmax * np.exp(-(q * q + (s2 / 2.0) ** 2) / (2 * sigma * sigma))))
+            if d < 1:
+                continue
+            x = rng.standard_normal((d, d))
+            blocks.append(np.asfortranarray(0.5 * (x + x.T)))
+    return blocks
