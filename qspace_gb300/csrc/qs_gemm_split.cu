@@ -63,15 +63,22 @@ namespace {
 
 constexpr int TMS = 128;          // output tile rows (MMA M)
 constexpr int TNS = 32;           // output tile cols (per digit group)
-constexpr int TKS = 32;           // K block per pipeline stage
+constexpr int TKS = 32;           // K block per pipeline stage (two MMA K steps)
+constexpr int KCM = TKS / 8;      // core matrices along K in a digit tile
 constexpr int A_DIGIT_BYTES = TMS * TKS * 2;  // 8 KB
 constexpr int B_DIGIT_BYTES = TNS * TKS * 2;  // 2 KB
+constexpr int MAX_STAGES = 8;
+// slicing threads per digit tile: one per (row, core matrix along K); a
+// complex task cuts one complex row into the two real rows of A~
+constexpr int SLICE_A_THREADS_R = TMS * KCM < 256 ? TMS * KCM : 256, SLICE_A_THREADS_C = TMS / 2 * KCM,
+              SLICE_B_THREADS = TNS * KCM;
 constexpr int EMPTY_EXP = -30000;
-constexpr int SMEM_HDR = 1024;
+constexpr int SMEM_HDR = 2048;   // barriers, TMEM slot, abort flag; tile-descriptor slots at 1024
 constexpr int SMEM_LIMIT = 227 * 1024;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;  // bounded mbarrier polls (seconds)
 constexpr int EPI_WARPS = 16;     // epilogue warps (4 per TMEM lane quarter)
 constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;
+constexpr int TILE_SLOTS = 1024;  // shared-memory offset of the epilogue warps' descriptor slots
 
 struct SplitPair {
   int64_t a_off, b_off;    // element offsets of op(A)/op(B) storage
@@ -87,7 +94,7 @@ struct SplitPair {
 };
 
 struct SplitTile {
-  int64_t c_off;           // double offset of the output block
+  int64_t c_off;           // double offset of the output block (first member: 8-byte aligned)
   int32_t p0, p1;
   int32_t mt, nt;
   int32_t Mr, N, ldc;
@@ -95,6 +102,8 @@ struct SplitTile {
   int32_t nchunk;          // drains of the accumulators
   int32_t rshift;          // bits dropped below the lowest group (int64 headroom)
 };
+constexpr int TILE_WORDS = (int)(sizeof(SplitTile) / 4);
+static_assert(sizeof(SplitTile) % 8 == 0 && TILE_WORDS <= 16, "tile descriptor fits one 64-byte slot");
 
 // ------------------------------------------------------------ bit helpers
 __device__ __forceinline__ int exp_key(double x) {
@@ -324,8 +333,8 @@ __global__ void fill_int_kernel(int *p, int64_t n, int v) {
 }
 
 // ------------------------------------------------------------ slicing
-// A~ digit tile (mt, kb): 128 rows x 32 k, core matrix (row group g, k core c)
-// at byte ((g*4 + c)*128), row r%8 at +16*(r%8), k%8 at +2*(k%8).
+// A~ digit tile (mt, kb): 128 rows x TKS k, core matrix (row group g, k core c)
+// at byte ((g*KCM + c)*128), row r%8 at +16*(r%8), k%8 at +2*(k%8).
 template <bool CPLX, int S, int B>
 __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb, const double *__restrict__ A,
                                              const int *__restrict__ E, uint8_t *__restrict__ tile) {
@@ -361,8 +370,8 @@ __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb,
         }
       }
       const int r0 = 2 * ml, r1 = r0 + 1;
-      uint8_t *d0 = tile + ((r0 >> 3) * 4 + q) * 128 + (r0 & 7) * 16;
-      uint8_t *d1 = tile + ((r1 >> 3) * 4 + q) * 128 + (r1 & 7) * 16;
+      uint8_t *d0 = tile + ((r0 >> 3) * KCM + q) * 128 + (r0 & 7) * 16;
+      uint8_t *d1 = tile + ((r1 >> 3) * KCM + q) * 128 + (r1 & 7) * 16;
 #pragma unroll
       for (int t = 0; t < S; ++t) {
         *reinterpret_cast<uint4 *>(d0 + t * A_DIGIT_BYTES) = make_uint4(p0[t][0], p0[t][1], p0[t][2], p0[t][3]);
@@ -390,7 +399,7 @@ __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb,
 #pragma unroll
         for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(dd[0][t], dd[1][t]);
       }
-      uint8_t *dst = tile + ((r >> 3) * 4 + q) * 128 + (r & 7) * 16;
+      uint8_t *dst = tile + ((r >> 3) * KCM + q) * 128 + (r & 7) * 16;
 #pragma unroll
       for (int t = 0; t < S; ++t)
         *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
@@ -414,7 +423,7 @@ slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tas
   }
 }
 
-// B~ digit tile (nt, kb): 32 columns x 32 k, the same core-matrix layout
+// B~ digit tile (nt, kb): 32 columns x TKS k, the same core-matrix layout
 // with the column index in the role of the row.
 template <bool CPLX, int S, int B>
 __device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb, const double *__restrict__ Bm,
@@ -454,7 +463,7 @@ __device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb,
 #pragma unroll
       for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(dd[0][t], dd[1][t]);
     }
-    uint8_t *dst = tile + ((c >> 3) * 4 + q) * 128 + (c & 7) * 16;
+    uint8_t *dst = tile + ((c >> 3) * KCM + q) * 128 + (c & 7) * 16;
 #pragma unroll
     for (int t = 0; t < S; ++t)
       *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
@@ -589,6 +598,10 @@ struct GroupWeight {
   int mh, ml, rs;
 };
 
+// V * 2^scale: one int64 -> FP64 conversion (round to nearest even) and an
+// exponent add.  Integer-only assemblies (64-bit or 32-bit words, exactly
+// rounded, measured on GB300) made the launch slower: on short tiles the
+// epilogue is the bottleneck and its cost follows its instruction count.
 __device__ __forceinline__ double fixed_to_double(long long V, int scale) {
   if (V == 0) return 0.0;
   const double d = __ll2double_rn(V);
@@ -619,10 +632,10 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
                   const int *__restrict__ F, double *__restrict__ C, int b, int nstages,
                   int kchunk, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem);       // [8]
-  uint64_t *empty = full + 8;                                 // [8]
-  uint64_t *acc_full = full + 16;                             // [2]
-  uint64_t *acc_empty = full + 18;                            // [2]
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);       // [MAX_STAGES]
+  uint64_t *empty = full + MAX_STAGES;                        // [MAX_STAGES]
+  uint64_t *acc_full = full + 2 * MAX_STAGES;                 // [2]
+  uint64_t *acc_empty = acc_full + 2;                         // [2]
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 512);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 516);
   uint8_t *stages = smem + SMEM_HDR;
@@ -708,7 +721,7 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       // shared-memory descriptors of stage 0; stage st adds st * STAGE_BYTES
       // to the start address field (addresses stay below 2^18, so the 14-bit
       // field never carries)
-      const uint64_t desc0 = make_desc(smem_u32(stages), 128, 512);
+      const uint64_t desc0 = make_desc(smem_u32(stages), 128, KCM * 128);
       bool ok = true;
       // before filling set u & 1 for use u >= 2, wait until use u - 2 is read
       auto acquire = [&](int uu) -> bool {
@@ -787,10 +800,22 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
     const int scale_b = -b * (S + 1);
     int u = 0;
     bool ok = true;
+    // The next tile's descriptor is fetched one tile ahead (one word per
+    // lane) and handed over through this warp's shared-memory slot, so that
+    // its global-load latency hides behind the current tile: short tiles are
+    // bound by the epilogue.
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + TILE_SLOTS + (warp - 2) * 64);
+    int ti = tile_of(0, cta, G);
+    uint32_t tw = (ti < ntiles && lane < TILE_WORDS) ? reinterpret_cast<const uint32_t *>(tiles + ti)[lane] : 0u;
     for (int r = 0; ok; ++r) {
-      const int ti = tile_of(r, cta, G);
       if (ti >= ntiles) break;
-      const SplitTile T = tiles[ti];
+      __syncwarp();  // every lane is done with the previous descriptor
+      if (lane < TILE_WORDS) tslot[lane] = tw;
+      __syncwarp();
+      // fields are read from the slot where used (no registers held)
+      const SplitTile &T = *reinterpret_cast<const SplitTile *>(tslot);
+      ti = tile_of(r + 1, cta, G);
+      tw = (ti < ntiles && lane < TILE_WORDS) ? reinterpret_cast<const uint32_t *>(tiles + ti)[lane] : 0u;
       const int i_glob = T.mt * TMS + q * 32 + lane;
       const bool rv = i_glob < T.Mr;
       // exponents of this thread's outputs, fetched now so that their load
@@ -885,7 +910,7 @@ template <int S>
 int pick_stages() {
   const size_t per = (size_t)S * (A_DIGIT_BYTES + B_DIGIT_BYTES);
   int n = (int)((SMEM_LIMIT - SMEM_HDR) / per);
-  return std::max(1, std::min(n, 4));
+  return std::max(1, std::min(n, MAX_STAGES));
 }
 
 template <int S>
@@ -907,14 +932,14 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d
     if (nrt) { exp_rows_kernel<true><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, dE); QS_LAUNCHED(ctx); }
     if (nct) { exp_cols_kernel<true><<<nct, 256, 0, st>>>(d_pairs, d_ct, B, dF); QS_LAUNCHED(ctx); }
     if (nxt) { exp_contig_kernel<true><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nat) { slice_a_kernel<true, S><<<nat, 256, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<true, S><<<nbt, 128, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nat) { slice_a_kernel<true, S><<<nat, SLICE_A_THREADS_C, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nbt) { slice_b_kernel<true, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
   } else {
     if (nrt) { exp_rows_kernel<false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, dE); QS_LAUNCHED(ctx); }
     if (nct) { exp_cols_kernel<false><<<nct, 256, 0, st>>>(d_pairs, d_ct, B, dF); QS_LAUNCHED(ctx); }
     if (nxt) { exp_contig_kernel<false><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nat) { slice_a_kernel<false, S><<<nat, 256, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<false, S><<<nbt, 128, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nat) { slice_a_kernel<false, S><<<nat, SLICE_A_THREADS_R, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nbt) { slice_b_kernel<false, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
   }
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);

@@ -4,9 +4,10 @@
 //
 //  * qs_eig_blocks  -- the OpenMP loop of QSpace::EigenSymmetric
 //    (Source/QSpace.cc:4789-4811) calling wbEigenS -> dsyevd / zheevd
-//    (Source/wbarray_blas.cc:501-660).  Blocks up to 32 rows go through one
-//    batched Jacobi call per distinct size (syevjBatched); larger blocks use
-//    the divide-and-conquer solver (syevd) on the context stream.
+//    (Source/wbarray_blas.cc:501-660).  Blocks up to 16 rows go through one
+//    batched Jacobi call per distinct size (syevjBatched); larger blocks
+//    through one batched solve per distinct size (XsyevBatched), spread over
+//    concurrent solver lanes.
 //  * qs_svd_blocks  -- SVD_Data::blockSVD (Source/mpsortho.cc:546-613) ->
 //    wbSVD -> dgesdd (Source/wbarray_blas.cc:995-1090); Jacobi SVD (gesvdj).
 //  * qs_mark_keep   -- markSet (Source/gathered.cc:1822-1990) on the host.
@@ -55,6 +56,18 @@ cusolverDnHandle_t solver_of(Ctx *ctx) {
 // blocks run concurrently (the solver synchronises with its stream inside
 // each call, and one medium-size call keeps only part of the GPU busy).
 constexpr int NLANES = 8;
+constexpr int64_t JACOBI_MAX = 16;     // largest block sent to the batched Jacobi solver
+
+// Estimated GB300 time (ms) of one solver call on nb real blocks of size n,
+// fitted to measured XsyevBatched times (one block: 2.2, 5.6, 7.9, 11.8,
+// 17.3, 22.7 ms at n = 64, 128, 256, 400, 550, 690; batches: a start-up
+// term ~ n^1.57 plus ~ n^2.5 per block beyond two).  Only its ratios
+// matter: it balances the work over the solver lanes.
+static double eig_unit_ms(int64_t n, int64_t nb) {
+  const double x = (double)n;
+  if (nb <= 1) return 0.5 + 0.032 * x;
+  return 0.00215 * std::pow(x, 1.565) + 2.7e-7 * std::pow(x, 2.5) * double(nb - 2);
+}
 struct SolverLanes {
   cudaStream_t st[NLANES] = {};
   cusolverDnHandle_t h[NLANES] = {};
@@ -269,48 +282,118 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
     dev_free(ctx, d_so);
     dev_free(ctx, d_sz);
   }
-  // group small blocks by size for batched Jacobi; others one by one
-  std::map<int64_t, std::vector<int64_t>> small;
-  std::vector<int64_t> large;
+  // blocks up to JACOBI_MAX rows: one batched Jacobi call per size on the
+  // context stream; larger blocks: one solver unit per distinct size (the
+  // symmetry sectors of an NRG/DMRG step repeat sizes, e.g. q and -q)
+  std::map<int64_t, std::vector<int64_t>> small, bysize;
   for (int64_t i = 0; i < nblk; ++i) {
     if (n[i] == 0) continue;
-    if (n[i] <= 32) small[n[i]].push_back(i);
-    else large.push_back(i);
+    if (n[i] <= JACOBI_MAX) small[n[i]].push_back(i);
+    else bysize[n[i]].push_back(i);
   }
-  int *d_info = dev_alloc<int>(ctx, (size_t)std::max<int64_t>(nblk, 1));
-  QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * std::max<int64_t>(nblk, 1), ctx->stream));
-  // large blocks: syevd, spread over the solver lanes (largest first, each
-  // to the lane with the least work so far), concurrent with the batched
-  // Jacobi of the small blocks on the context stream
-  std::vector<double *> works;
+  // units: (size, blocks); a unit is solved in place when its blocks follow
+  // one another in U and E, otherwise through a staging copy
+  struct Unit {
+    int ni;
+    int64_t first;     // index of its first block in `order` / the info array
+    int nb;
+    bool inplace;
+  };
+  std::vector<Unit> units;
+  std::vector<int64_t> order;
+  // One unit per size.  Splitting groups of large blocks into single-block
+  // solves (faster alone: 22.7 ms for one n = 690 block against 60 ms for a
+  // batch of two) was slower over a whole NRG step on eight lanes (218-233 ms
+  // against 189 ms): concurrent single solves contend for the GPU, while the
+  // batched algorithm's time per block keeps falling with the batch.
+  for (auto &kv : bysize) {
+    const int64_t ni = kv.first, bs = ni * ni;
+    const auto &g = kv.second;
+    Unit u{(int)ni, (int64_t)order.size(), (int)g.size(), true};
+    for (size_t j = 0; j < g.size(); ++j) {
+      if (offs[g[j]] != offs[g[0]] + (int64_t)j * bs || eoffs[g[j]] != eoffs[g[0]] + (int64_t)j * ni) u.inplace = false;
+      order.push_back(g[j]);
+    }
+    units.push_back(u);
+  }
+  const int64_t nlarge = (int64_t)order.size();
+  int *d_info = dev_alloc<int>(ctx, (size_t)std::max<int64_t>(nlarge, 1));
+  QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * std::max<int64_t>(nlarge, 1), ctx->stream));
+  // units spread over the solver lanes (largest first, each to the lane with
+  // the least work so far), concurrent with the Jacobi calls on the context
+  // stream
+  std::vector<void *> bufs;      // device buffers released after the join
   std::vector<int> used;
   SolverLanes *L = nullptr;
-  if (!large.empty()) {
+  if (!units.empty()) {
     L = lanes_of(ctx);
-    std::sort(large.begin(), large.end(), [&](int64_t x, int64_t y) { return n[x] > n[y]; });
-    // QS_EIG_LANES (1..8) overrides the number of concurrent lanes for tuning
+    std::vector<int> uo(units.size());
+    std::iota(uo.begin(), uo.end(), 0);
+    auto cost = [&](int u) { return eig_unit_ms(units[u].ni, units[u].nb); };
+    std::sort(uo.begin(), uo.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    // QS_EIG_LANES (1..8) overrides the number of concurrent lanes (eight
+    // measured best for an NRG step on GB300: 189 ms, four 252 ms, twelve or
+    // sixteen 237 ms)
     const char *el = std::getenv("QS_EIG_LANES");
     const int want = el ? std::max(1, std::min(NLANES, std::atoi(el))) : NLANES;
-    const int nl = (int)std::min<size_t>(want, large.size());
-    std::vector<std::vector<int64_t>> part(nl);
+    const int nl = (int)std::min<size_t>(want, units.size());
+    std::vector<std::vector<int>> part(nl);
     std::vector<double> load(nl, 0.0);
-    for (int64_t i : large) {
+    for (int u : uo) {
       const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-      part[l].push_back(i);
-      load[l] += double(n[i]) * n[i] * n[i];
+      part[l].push_back(u);
+      load[l] += cost(u);
     }
-    // workspaces (allocated on the context stream, before the fork)
-    std::vector<int> lwork(nl, 0);
+    // per lane: device workspace, host workspace and staging area, sized for
+    // its largest unit; gather/scatter tables for the staged units
+    std::vector<cusolverDnParams_t> prm(nl, nullptr);
+    std::vector<size_t> wdev(nl, 0), whost(nl, 0);
+    const cudaDataType dtA = cplx ? CUDA_C_64F : CUDA_R_64F;
+    std::vector<double *> work(nl, nullptr), stage(nl, nullptr), wstage(nl, nullptr);
+    std::vector<std::vector<char>> hwork(nl);
+    std::vector<int64_t> so, dof, sz, eo, ed, ez;  // per staged block: U/E offsets <-> staging offsets
+    std::vector<int64_t> tab(units.size(), -1);    // first table row of a staged unit
     for (int l = 0; l < nl; ++l) {
-      const int nm = (int)n[part[l][0]];  // the lane's largest block bounds its workspace
-      if (cplx)
-        QS_SOLVER(cusolverDnZheevd_bufferSize(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm,
-                                              reinterpret_cast<cuDoubleComplex *>(U), nm, E, &lwork[l]));
-      else
-        QS_SOLVER(cusolverDnDsyevd_bufferSize(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nm, U, nm, E,
-                                              &lwork[l]));
-      works.push_back(dev_alloc<double>(ctx, (size_t)std::max(lwork[l], 1) * es));
+      QS_SOLVER(cusolverDnCreateParams(&prm[l]));
+      int64_t sa = 0, se = 0;
+      for (int u : part[l]) {
+        Unit &un = units[u];
+        const int ni = un.ni;
+        size_t wd = 0, wh = 0;
+        QS_SOLVER(cusolverDnXsyevBatched_bufferSize(L->h[l], prm[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                                    ni, dtA, U, ni, CUDA_R_64F, E, dtA, &wd, &wh, un.nb));
+        wdev[l] = std::max(wdev[l], wd);
+        whost[l] = std::max(whost[l], wh);
+        if (!un.inplace) {
+          const int64_t bs = (int64_t)ni * ni;
+          tab[u] = (int64_t)so.size();
+          for (int j = 0; j < un.nb; ++j) {
+            const int64_t i = order[un.first + j];
+            so.push_back(offs[i]); dof.push_back(bs * j); sz.push_back(bs);
+            eo.push_back(eoffs[i]); ed.push_back((int64_t)ni * j); ez.push_back(ni);
+          }
+          sa = std::max(sa, bs * un.nb);
+          se = std::max(se, (int64_t)ni * un.nb);
+        }
+      }
+      work[l] = dev_alloc<double>(ctx, (wdev[l] + 7) / 8 + 1);
+      bufs.push_back(work[l]);
+      hwork[l].resize(whost[l] + 16);
+      if (sa) {
+        stage[l] = dev_alloc<double>(ctx, (size_t)sa * es);
+        wstage[l] = dev_alloc<double>(ctx, (size_t)se);
+        bufs.push_back(stage[l]);
+        bufs.push_back(wstage[l]);
+      }
     }
+    int64_t *d_tab = nullptr;
+    if (!so.empty()) {
+      std::vector<int64_t> t;
+      for (auto *v : {&so, &dof, &sz, &eo, &ed, &ez}) t.insert(t.end(), v->begin(), v->end());
+      d_tab = dev_upload(ctx, t);
+      bufs.push_back(d_tab);
+    }
+    const int64_t nt = (int64_t)so.size();
     cudaEvent_t fork;
     QS_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
     QS_CUDA(cudaEventRecord(fork, ctx->stream));
@@ -319,37 +402,58 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
     std::vector<std::thread> th;
     std::vector<std::exception_ptr> errs(nl);
     const int dev = ctx->device;
+    int64_t nlaunch = 0;
     for (int l = 0; l < nl; ++l) {
       QS_CUDA(cudaStreamWaitEvent(L->st[l], fork, 0));
       used.push_back(l);
+      for (int u : part[l]) nlaunch += units[u].inplace ? 1 : 4;
       th.emplace_back([&, l]() {
         try {
           QS_CUDA(cudaSetDevice(dev));
-          for (int64_t i : part[l]) {
-            const int ni = (int)n[i];
-            if (cplx)
-              QS_SOLVER(cusolverDnZheevd(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
-                                         reinterpret_cast<cuDoubleComplex *>(U) + offs[i], ni, E + eoffs[i],
-                                         reinterpret_cast<cuDoubleComplex *>(works[l]), lwork[l], d_info + i));
-            else
-              QS_SOLVER(cusolverDnDsyevd(L->h[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
-                                         U + offs[i] * es, ni, E + eoffs[i], works[l], lwork[l], d_info + i));
+          for (int u : part[l]) {
+            const Unit &un = units[u];
+            const int ni = un.ni;
+            int *info = d_info + un.first;
+            const int64_t i0 = order[un.first];
+            double *A = U + offs[i0] * es, *W = E + eoffs[i0];
+            const int64_t bs = (int64_t)ni * ni;
+            const int64_t *t = d_tab + (tab[u] < 0 ? 0 : tab[u]);
+            dim3 g((unsigned)std::min<int64_t>((bs * es + 255) / 256, 256), (unsigned)un.nb);
+            dim3 g2((unsigned)std::min<int64_t>((ni + 255) / 256, 4), (unsigned)un.nb);
+            if (!un.inplace) {
+              A = stage[l];
+              W = wstage[l];
+              copy_blocks_kernel<<<g, 256, 0, L->st[l]>>>(U, A, t, t + nt, t + 2 * nt, es);
+              QS_CUDA(cudaGetLastError());
+            }
+            QS_SOLVER(cusolverDnXsyevBatched(L->h[l], prm[l], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, ni,
+                                             dtA, A, ni, CUDA_R_64F, W, dtA, work[l], wdev[l],
+                                             hwork[l].data(), whost[l], info, un.nb));
+            if (!un.inplace) {
+              copy_blocks_kernel<<<g, 256, 0, L->st[l]>>>(A, U, t + nt, t, t + 2 * nt, es);
+              QS_CUDA(cudaGetLastError());
+              copy_blocks_kernel<<<g2, 256, 0, L->st[l]>>>(W, E, t + 4 * nt, t + 3 * nt, t + 5 * nt, 1);
+              QS_CUDA(cudaGetLastError());
+            }
           }
           QS_CUDA(cudaEventRecord(L->ev[l], L->st[l]));
         } catch (...) {
           errs[l] = std::current_exception();
         }
       });
-      ctx->launches += (int64_t)part[l].size();
     }
+    ctx->launches += nlaunch;
     for (auto &t : th) t.join();
     cudaEventDestroy(fork);
+    for (auto *p : prm)
+      if (p) cusolverDnDestroyParams(p);
     for (auto &e : errs)
       if (e) {
         for (int l : used) cudaStreamSynchronize(L->st[l]);
         used.clear();
-        for (double *w : works) dev_free(ctx, w);
-        works.clear();
+        for (void *p : bufs) dev_free(ctx, p);
+        bufs.clear();
+        dev_free(ctx, d_info);
         std::rethrow_exception(e);
       }
   }
@@ -358,8 +462,8 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
   auto join = [&]() {
     for (int l : used) cudaStreamWaitEvent(ctx->stream, L->ev[l], 0);
     used.clear();
-    for (double *w : works) dev_free(ctx, w);
-    works.clear();
+    for (void *p : bufs) dev_free(ctx, p);
+    bufs.clear();
   };
   try {
   // small blocks: batched Jacobi on contiguous copies
@@ -425,15 +529,17 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
   }
   } catch (...) {
     join();
+    dev_free(ctx, d_info);
     throw;
   }
   join();
-  std::vector<int> info(std::max<int64_t>(nblk, 1));
+  std::vector<int> info(std::max<int64_t>(nlarge, 1));
   QS_CUDA(cudaMemcpyAsync(info.data(), d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QS_CUDA(cudaStreamSynchronize(ctx->stream));
   dev_free(ctx, d_info);
-  for (int64_t i = 0; i < nblk; ++i)
-    if (info[i] != 0) fail(QS_ERR_NUMERIC, "eig: block %lld did not converge (info %d)", (long long)i, info[i]);
+  for (int64_t k = 0; k < nlarge; ++k)
+    if (info[k] != 0)
+      fail(QS_ERR_NUMERIC, "eig: block %lld did not converge (info %d)", (long long)order[k], info[k]);
 }
 
 // -------------------------------------------------------------- svd blocks

@@ -32,6 +32,24 @@ def test_eig_blocks_uneven_sizes(ctx, cplx):
         assert np.max(np.abs(H @ U - U * E[None, :])) <= 1e-11 * scale
 
 
+@pytest.mark.parametrize("cplx", [False, True])
+def test_eig_blocks_repeated_sizes(ctx, cplx):
+    """Blocks of one size solved together: scattered through the arena (staged
+    copies), adjacent (in place), next to blocks of the Jacobi range."""
+    rng = np.random.default_rng(8)
+    sizes = [40, 7, 40, 90, 40, 90, 16, 16, 17, 17, 120, 120, 120, 5, 40]
+    blocks = [_sym(rng, n, cplx) for n in sizes]
+    blocks[3] = blocks[3] * 1e-3          # scales differ within a size group
+    Es, Us = eig_blocks(blocks, ctx)
+    for H, E, U in zip(blocks, Es, Us):
+        ref = np.linalg.eigvalsh(H)
+        scale = max(1e-3, np.abs(ref).max())
+        assert np.max(np.abs(E - ref)) <= 1e-12 * scale
+        n = H.shape[0]
+        assert np.max(np.abs(U.conj().T @ U - np.eye(n))) <= 1e-12 * max(1, n)
+        assert np.max(np.abs(H @ U - U * E[None, :])) <= 1e-11 * scale
+
+
 def test_eigQS_truncation_matches_oracle(ctx):
     rng = np.random.default_rng(5)
     labels = np.arange(-3, 4, dtype=np.int32).reshape(-1, 1)
