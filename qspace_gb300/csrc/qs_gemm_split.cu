@@ -347,8 +347,10 @@ __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb,
     for (int w = threadIdx.x; w < (TMS / 2) * (TKS / 8); w += blockDim.x) {
       const int ml = w % (TMS / 2), q = w / (TMS / 2);
       const int m = mt * (TMS / 2) + ml;
-      const bool rv = m < P.M;
-      const int Ei = rv ? E[P.eoff + 2 * m] : 0;
+      // rows past the block only feed outputs the epilogue discards: not written
+      if (m >= P.M) continue;
+      const bool rv = true;
+      const int Ei = E[P.eoff + 2 * m];
       uint32_t p0[S][4], p1[S][4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -382,8 +384,9 @@ __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb,
     for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
       const int r = w % TMS, q = w / TMS;
       const int rr = mt * TMS + r;
-      const bool rv = rr < P.Mr;
-      const int Ei = rv ? E[P.eoff + rr] : 0;
+      if (rr >= P.Mr) continue;  // feeds discarded outputs only: not written
+      const bool rv = true;
+      const int Ei = E[P.eoff + rr];
       uint32_t pk[S][4];
 #pragma unroll
       for (int e = 0; e < 8; e += 2) {
@@ -432,8 +435,9 @@ __device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb,
   for (int w = threadIdx.x; w < TNS * (TKS / 8); w += blockDim.x) {
     const int c = w % TNS, q = w / TNS;
     const int n = nt * TNS + c;
-    const bool nv = n < P.N;
-    const int Fj = nv ? F[P.foff + n] : 0;
+    if (n >= P.N) continue;  // columns past the block feed discarded outputs only: not written
+    const bool nv = true;
+    const int Fj = F[P.foff + n];
     uint32_t pk[S][4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
