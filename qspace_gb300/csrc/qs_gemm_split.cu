@@ -91,6 +91,8 @@ struct SplitPair {
   int32_t e_afac;          // exponent added by the CG factor (|afac| < 2^e)
   int32_t fe, fneg;        // CG factor folded into A's digits: fm 2^fe, sign
   uint64_t fm;             // (fm = 0: factor 1)
+  int32_t swap;            // block computed as C^T = op(B)^T op(A)^T: the A role reads the B arena
+  int32_t pad_;
 };
 
 struct SplitTile {
@@ -101,6 +103,10 @@ struct SplitTile {
   int32_t eoff, foff;
   int32_t nchunk;          // drains of the accumulators
   int32_t rshift;          // bits dropped below the lowest group (int64 headroom)
+  // output address of tile row r, column j (doubles from c_off):
+  // (r >> rsplit) * rs + (r & rsplit) + j * ldc; rsplit = 1 for a complex
+  // block computed transposed (its rows interleave Re/Im of C's columns)
+  int32_t rs, rsplit;
 };
 constexpr int TILE_WORDS = (int)(sizeof(SplitTile) / 4);
 static_assert(sizeof(SplitTile) % 8 == 0 && TILE_WORDS <= 16, "tile descriptor fits one 64-byte slot");
@@ -199,27 +205,31 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 }
 
 // --------------------------------------------------------- exponent passes
-// Row exponents of op(A~) (per output block, max over its pairs).
-// A block of 256 threads covers rows [m0, m0 + min(256, M - m0)) and depths
-// [k0, k1): R threads per depth phase (R a power of two >= the row count),
-// 256 / R phases splitting the depth, so short blocks keep every thread
-// loading and neighbouring threads read neighbouring rows.  Deep operands
-// are split into several tasks along k (maxima combine atomically).
-template <bool CPLX>
+// Exponents of lines strided along k: rows of a plain op(A~) (ROLE_B =
+// false) or columns of a transposed op(B~) (ROLE_B = true); per output
+// block, max over its pairs.  A block of 256 threads covers lines
+// [m0, m0 + min(256, lines - m0)) and depths [k0, k1): R threads per depth
+// phase (R a power of two >= the line count), 256 / R phases splitting the
+// depth, so short blocks keep every thread loading and neighbouring threads
+// read neighbouring elements.  Deep operands are split into several tasks
+// along k (maxima combine atomically).
+template <bool CPLX, bool ROLE_B>
 __global__ void __launch_bounds__(256)
-exp_rows_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-                const double *__restrict__ A, int *__restrict__ E) {
+exp_lines_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
+                 const double *__restrict__ Aarena, const double *__restrict__ Barena, int *__restrict__ E,
+                 int *__restrict__ F) {
   __shared__ int keys[256];
   const int4 tk = tasks[blockIdx.x];  // (pair, m0, k0, k1)
   const SplitPair P = pairs[tk.x];
-  const int rows = min(P.M - tk.y, 256);
+  // a swapped pair's roles read the other arena
+  const double *__restrict__ A = (ROLE_B != (P.swap != 0)) ? Barena : Aarena;
+  const int rows = min((ROLE_B ? P.N : P.M) - tk.y, 256);
   int R = 1;
   while (R < rows) R <<= 1;
   const int KS = 256 / R;
   const int r = threadIdx.x % R, ph = threadIdx.x / R;
   const int m = tk.y + r;
-  const bool ta = P.trans & 1;
-  const int64_t sk = ta ? 1 : P.lda, base = P.a_off + (ta ? (int64_t)m * P.lda : (int64_t)m);
+  const int64_t sk = ROLE_B ? P.ldb : P.lda, base = (ROLE_B ? P.b_off : P.a_off) + (int64_t)m;
   int key = 0;
   if (r < rows) {
     int k = tk.z + ph;
@@ -253,6 +263,10 @@ exp_rows_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ ta
     for (int p = 1; p < KS; ++p) key = max(key, keys[p * R + r]);
   }
   if (r >= rows || !key) return;
+  if (ROLE_B) {
+    atomicMax(&F[P.foff + m], key - 1022);
+    return;
+  }
   const int e = key - 1022 + P.e_afac;
   if (CPLX) {
     atomicMax(&E[P.eoff + 2 * m], e);
@@ -260,29 +274,6 @@ exp_rows_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ ta
   } else {
     atomicMax(&E[P.eoff + m], e);
   }
-}
-
-// Column exponents of op(B~).
-template <bool CPLX>
-__global__ void __launch_bounds__(256)
-exp_cols_kernel(const SplitPair *__restrict__ pairs, const int2 *__restrict__ tasks,
-                const double *__restrict__ B, int *__restrict__ F) {
-  const int2 tk = tasks[blockIdx.x];
-  const SplitPair P = pairs[tk.x];
-  const int n = tk.y + threadIdx.x;
-  if (n >= P.N) return;
-  const bool tb = P.trans & 2;
-  int key = 0;
-  for (int k = 0; k < P.K; ++k) {
-    const int64_t idx = tb ? (int64_t)n + (int64_t)k * P.ldb : (int64_t)k + (int64_t)n * P.ldb;
-    if (CPLX) {
-      const double2 v = reinterpret_cast<const double2 *>(B)[P.b_off + idx];
-      key = max(key, max(exp_key(v.x), exp_key(v.y)));
-    } else {
-      key = max(key, exp_key(B[P.b_off + idx]));
-    }
-  }
-  if (key) atomicMax(&F[P.foff + n], key - 1022);
 }
 
 // Same maxima for lines stored contiguously along k (rows of a transposed
@@ -300,7 +291,7 @@ exp_contig_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ 
   const int line = tk.y + (threadIdx.x >> 5);
   const bool rowsA = tk.z == 0;
   if (line >= (rowsA ? P.M : P.N)) return;
-  const double *base = rowsA ? A : B;
+  const double *base = (rowsA != (P.swap != 0)) ? A : B;  // a swapped pair's roles read the other arena
   const int64_t off = rowsA ? P.a_off + (int64_t)line * P.lda : P.b_off + (int64_t)line * P.ldb;
   int key = 0;
   for (int k = lane; k < P.K; k += 32) {
@@ -413,10 +404,11 @@ __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb,
 template <bool CPLX, int S>
 __global__ void __launch_bounds__(256)
 slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-               const double *__restrict__ A, const int *__restrict__ E,
+               const double *__restrict__ Aarena, const double *__restrict__ Barena, const int *__restrict__ E,
                uint8_t *__restrict__ arena, int b) {
   const int4 tk = tasks[blockIdx.x];  // (pair, mt, kb, -)
   const SplitPair P = pairs[tk.x];
+  const double *__restrict__ A = P.swap ? Barena : Aarena;
   uint8_t *tile = arena + P.as_off + ((int64_t)(tk.y * P.KB + tk.z) * S) * A_DIGIT_BYTES;
   switch (b) {  // the host admits b = 5..8 only
     case 5: slice_a_tile<CPLX, S, 5>(P, tk.y, tk.z, A, E, tile); break;
@@ -477,10 +469,11 @@ __device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb,
 template <bool CPLX, int S>
 __global__ void __launch_bounds__(128)
 slice_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-               const double *__restrict__ Bm, const int *__restrict__ F,
+               const double *__restrict__ Aarena, const double *__restrict__ Barena, const int *__restrict__ F,
                uint8_t *__restrict__ arena, int b) {
   const int4 tk = tasks[blockIdx.x];
   const SplitPair P = pairs[tk.x];
+  const double *__restrict__ Bm = P.swap ? Aarena : Barena;
   uint8_t *tile = arena + P.bs_off + ((int64_t)(tk.y * P.KB + tk.z) * S) * B_DIGIT_BYTES;
   switch (b) {
     case 5: slice_b_tile<CPLX, S, 5>(P, tk.y, tk.z, Bm, F, tile); break;
@@ -884,7 +877,7 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       }
       if (!ok) break;
       if (rv) {
-        double *crow = C + T.c_off + (int64_t)i_glob;
+        double *crow = C + T.c_off + (int64_t)(i_glob >> T.rsplit) * T.rs + (i_glob & T.rsplit);
 #pragma unroll
         for (int jj = 0; jj < CW; ++jj) {
           const int j = j0 + jj;
@@ -919,7 +912,7 @@ int pick_stages() {
 
 template <int S>
 void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d_rt, int nrt,
-                    const int2 *d_ct, int nct, const int4 *d_xt, int nxt, const int4 *d_at, int nat,
+                    const int4 *d_ct, int nct, const int4 *d_xt, int nxt, const int4 *d_at, int nat,
                     const int4 *d_bt, int nbt,
                     const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
                     int *dE, int64_t nE, int *dF, int64_t nF, uint8_t *arena, int b, int kchunk,
@@ -933,17 +926,17 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d
   fill_int_kernel<<<fg, 256, 0, st>>>(dF, nF, EMPTY_EXP);
   QS_LAUNCHED(ctx);
   if (cplx) {
-    if (nrt) { exp_rows_kernel<true><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, dE); QS_LAUNCHED(ctx); }
-    if (nct) { exp_cols_kernel<true><<<nct, 256, 0, st>>>(d_pairs, d_ct, B, dF); QS_LAUNCHED(ctx); }
+    if (nrt) { exp_lines_kernel<true, false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, B, dE, dF); QS_LAUNCHED(ctx); }
+    if (nct) { exp_lines_kernel<true, true><<<nct, 256, 0, st>>>(d_pairs, d_ct, A, B, dE, dF); QS_LAUNCHED(ctx); }
     if (nxt) { exp_contig_kernel<true><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nat) { slice_a_kernel<true, S><<<nat, SLICE_A_THREADS_C, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<true, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nat) { slice_a_kernel<true, S><<<nat, SLICE_A_THREADS_C, 0, st>>>(d_pairs, d_at, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nbt) { slice_b_kernel<true, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
   } else {
-    if (nrt) { exp_rows_kernel<false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, dE); QS_LAUNCHED(ctx); }
-    if (nct) { exp_cols_kernel<false><<<nct, 256, 0, st>>>(d_pairs, d_ct, B, dF); QS_LAUNCHED(ctx); }
+    if (nrt) { exp_lines_kernel<false, false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, B, dE, dF); QS_LAUNCHED(ctx); }
+    if (nct) { exp_lines_kernel<false, true><<<nct, 256, 0, st>>>(d_pairs, d_ct, A, B, dE, dF); QS_LAUNCHED(ctx); }
     if (nxt) { exp_contig_kernel<false><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nat) { slice_a_kernel<false, S><<<nat, SLICE_A_THREADS_R, 0, st>>>(d_pairs, d_at, A, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<false, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nat) { slice_a_kernel<false, S><<<nat, SLICE_A_THREADS_R, 0, st>>>(d_pairs, d_at, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nbt) { slice_b_kernel<false, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
   }
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);
@@ -1049,7 +1042,7 @@ struct SplitWork {
   int64_t nE = 0, nF = 0, arena = 0;
   std::vector<SplitPair> sp;
   std::vector<int4> rt;
-  std::vector<int2> ct;
+  std::vector<int4> ct;  // strided columns of op(B~): (pair, n0, k0, k1)
   std::vector<int4> xt, at, bt;
   std::vector<SplitTile> tiles;
 };
@@ -1058,7 +1051,7 @@ struct SplitWork {
 struct SplitDev {
   SplitPair *pairs = nullptr;
   int4 *rt = nullptr;
-  int2 *ct = nullptr;
+  int4 *ct = nullptr;
   int4 *xt = nullptr, *at = nullptr, *bt = nullptr;
   SplitTile *tiles = nullptr;
   int *E = nullptr, *F = nullptr;
@@ -1068,13 +1061,58 @@ struct SplitDev {
 // Host half of the split path: digit plan, per-pair digit geometry and arena
 // offsets, and the device work lists (exponent lines, slicing tiles, output
 // tiles in launch order).
-static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
-                              const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+// Orientation of each output block: computed as C^T = op(B)^T op(A)^T when
+// that is estimated at least 3 % cheaper.  The estimate per k-block of the
+// block's pairs, in bytes of slicing traffic: 26900 per 128 x 32 output tile
+// (GEMM), plus the digit bytes the slicing writes for the A role (128-row
+// tiles of the 2x2 real form, 48 KB at six digits) and for the B role
+// (32-column tiles, 12 KB, weighted 0.86) -- fitted to GB300 timings of the
+// split GEMM (5.65 ns per tile and k-block) and of the slicing kernels (0.21 and
+// 0.18 ps per byte).  Turning a wide block gives the 128-row tiles the larger
+// side but also the duplicated real form to the larger operand.  A swapped
+// pair exchanges the roles and storage of its operands: A' = op(B)^T reads
+// B's storage (transposed unless op(B) was), B' = op(A)^T reads A's, with the
+// conjugation flags exchanged; the tiles store C^T transposed.
+static std::vector<uint8_t> orient_blocks(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                                          std::vector<int32_t> &bM, std::vector<int32_t> &bN, int cm,
+                                          std::vector<PairDesc> &tp) {
+  const int64_t nb = (int64_t)bM.size();
+  std::vector<uint8_t> swp(nb, 0);
+  bool any = false;
+  auto cost = [&](int64_t m, int64_t n) {
+    const double mt = double((m * cm + TMS - 1) / TMS), nt = double((n + TNS - 1) / TNS);
+    return 26900.0 * mt * nt + 49152.0 * mt + 10530.0 * nt;
+  };
+  for (int64_t g = 0; g < nb; ++g)
+    if (cost(bN[g], bM[g]) < 0.97 * cost(bM[g], bN[g])) swp[g] = 1, any = true;
+  if (!any) return swp;
+  tp = pairs;
+  for (int64_t g = 0; g < nb; ++g) {
+    if (!swp[g]) continue;
+    std::swap(bM[g], bN[g]);
+    for (int64_t p = grp[g]; p < grp[g + 1]; ++p) {
+      PairDesc &d = tp[p];
+      const int t = d.trans;
+      std::swap(d.M, d.N);
+      std::swap(d.a_off, d.b_off);
+      std::swap(d.lda, d.ldb);
+      d.trans = ((t & 2) ? 0 : 1) | ((t & 1) ? 0 : 2) | ((t & 8) ? 4 : 0) | ((t & 4) ? 8 : 0);
+    }
+  }
+  return swp;
+}
+
+static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::vector<int64_t> &grp,
+                              const std::vector<int32_t> &blk_M_in, const std::vector<int32_t> &blk_N_in,
                               const std::vector<int64_t> &c_off, bool cplx, int forced_slices, double tol,
                               const std::vector<int32_t> *blk_ldc, SplitWork &w, int forced_bits = 0) {
   SplitResult res;
-  const int64_t nb = (int64_t)blk_M.size();
+  const int64_t nb = (int64_t)blk_M_in.size();
   const int cm = cplx ? 2 : 1;
+  std::vector<int32_t> blk_M = blk_M_in, blk_N = blk_N_in;
+  std::vector<PairDesc> swapped_pairs;
+  const std::vector<uint8_t> swp = orient_blocks(pairs_in, grp, blk_M, blk_N, cm, swapped_pairs);
+  const std::vector<PairDesc> &pairs = swapped_pairs.empty() ? pairs_in : swapped_pairs;
   DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices, forced_bits);
   const int S = dp.nslices, b = dp.bits;
   const int kchunk = kchunk_of(b, S);
@@ -1101,7 +1139,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
   int64_t &arena = w.arena;
   arena = 0;
   std::vector<int4> &rt = w.rt;
-  std::vector<int2> &ct = w.ct;
+  std::vector<int4> &ct = w.ct;
   std::vector<int4> &xt = w.xt;
   std::vector<int4> &at = w.at, &bt = w.bt;
   std::vector<SplitTile> &tiles = w.tiles;
@@ -1133,6 +1171,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
       int e = 0;
       if (d.afac != 1.0 && d.afac != 0.0) std::frexp(d.afac, &e);
       s.e_afac = e;
+      s.swap = swp[g];
       s.as_off = arena;
       arena += (int64_t)s.MT * s.KB * S * A_DIGIT_BYTES;
       s.bs_off = arena;
@@ -1146,7 +1185,8 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
         for (int m0 = 0; m0 < d.M; m0 += 256)
           for (int k0 = 0; k0 < d.K; k0 += 256) rt.push_back(make_int4((int)p, m0, k0, std::min(d.K, k0 + 256)));
       if (d.trans & 2)
-        for (int n0 = 0; n0 < d.N; n0 += 256) ct.push_back(make_int2((int)p, n0));
+        for (int n0 = 0; n0 < d.N; n0 += 256)
+          for (int k0 = 0; k0 < d.K; k0 += 256) ct.push_back(make_int4((int)p, n0, k0, std::min(d.K, k0 + 256)));
       else
         for (int n0 = 0; n0 < d.N; n0 += 8) xt.push_back(make_int4((int)p, n0, 1, 0));
       for (int mt = 0; mt < s.MT; ++mt)
@@ -1176,7 +1216,21 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs, const std::vec
         t.nt = nt;
         t.Mr = blk_M[g] * cm;
         t.N = blk_N[g];
-        t.ldc = blk_ldc ? (*blk_ldc)[g] * cm : std::max(t.Mr, 1);
+        // column stride of C in its elements, in the caller's orientation
+        const int64_t ldc0 = blk_ldc ? (*blk_ldc)[g] : std::max(blk_M_in[g], 1);
+        if (!swp[g]) {
+          t.ldc = (int32_t)(ldc0 * cm);
+          t.rs = 1;
+          t.rsplit = 0;
+        } else if (cm == 1) {
+          t.ldc = 1;
+          t.rs = (int32_t)ldc0;
+          t.rsplit = 0;
+        } else {
+          t.ldc = 2;
+          t.rs = (int32_t)(2 * ldc0);
+          t.rsplit = 1;
+        }
         t.eoff = (int32_t)eoff[g];
         t.foff = (int32_t)foff[g];
         t.nchunk = nchunk;
@@ -1273,7 +1327,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
     return o;
   };
   const size_t o_pairs = take(w.sp.size() * sizeof(SplitPair));
-  const size_t o_rt = take(w.rt.size() * sizeof(int4)), o_ct = take(w.ct.size() * sizeof(int2));
+  const size_t o_rt = take(w.rt.size() * sizeof(int4)), o_ct = take(w.ct.size() * sizeof(int4));
   const size_t o_xt = take(w.xt.size() * sizeof(int4)), o_at = take(w.at.size() * sizeof(int4));
   const size_t o_bt = take(w.bt.size() * sizeof(int4));
   const size_t o_tiles = take(w.tiles.size() * sizeof(SplitTile));
@@ -1285,7 +1339,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
   SplitDev d;
   d.pairs = reinterpret_cast<SplitPair *>(scratch + o_pairs);
   d.rt = reinterpret_cast<int4 *>(scratch + o_rt);
-  d.ct = reinterpret_cast<int2 *>(scratch + o_ct);
+  d.ct = reinterpret_cast<int4 *>(scratch + o_ct);
   d.xt = reinterpret_cast<int4 *>(scratch + o_xt);
   d.at = reinterpret_cast<int4 *>(scratch + o_at);
   d.bt = reinterpret_cast<int4 *>(scratch + o_bt);
@@ -1298,7 +1352,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
   };
   put(d.pairs, w.sp.data(), w.sp.size() * sizeof(SplitPair));
   put(d.rt, w.rt.data(), w.rt.size() * sizeof(int4));
-  put(d.ct, w.ct.data(), w.ct.size() * sizeof(int2));
+  put(d.ct, w.ct.data(), w.ct.size() * sizeof(int4));
   put(d.xt, w.xt.data(), w.xt.size() * sizeof(int4));
   put(d.at, w.at.data(), w.at.size() * sizeof(int4));
   put(d.bt, w.bt.data(), w.bt.size() * sizeof(int4));
