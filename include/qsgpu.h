@@ -164,6 +164,26 @@ QS_EXPORT qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t 
 QS_EXPORT const double *qs_tensor_data(const qs_tensor *T);
 QS_EXPORT qs_status qs_tensor_itags(const qs_tensor *T, char *buf, size_t len);
 QS_EXPORT void qs_tensor_free(qs_tensor *T);
+
+/* ---------------------------------------------------------- wire container
+ * A QSpace as one flat binary container (no counterpart in binary form: the
+ * reference's container is the MATLAB struct {Q, data, info} of
+ * Source/QSpace.hh:3005-3100, kept in .mat files).  Little-endian; a 128-byte
+ * header ("QSPW", format version 1, complex flag, rank, qdim, nblk, data
+ * extent, section offsets) followed by 64-byte aligned sections: labels
+ * (int32, block-major as in qs_qspace_view), dims (int64), offsets (int64),
+ * data (FP64 or interleaved complex128), itags ("a,b*,c" + NUL).  Abelian
+ * QSpaces only (no info.cgr section).  Every offset and length is validated
+ * before a view points into a buffer; a malformed container is QS_ERR_ARG. */
+QS_EXPORT qs_status qs_wire_size(const qs_qspace_view *A, int64_t *bytes);
+QS_EXPORT qs_status qs_wire_pack(const qs_qspace_view *A, void *buf, int64_t bytes);
+/* Zero copy: *A points into buf (8-byte aligned) and is valid as long as it. */
+QS_EXPORT qs_status qs_wire_view(const void *buf, int64_t bytes, qs_qspace_view *A);
+/* Device tensors straight from / into a container: one host->device copy of
+ * its data section, or one device->host copy into it. */
+QS_EXPORT qs_status qs_tensor_from_wire(qs_ctx *ctx, const void *buf, int64_t bytes, qs_tensor **out);
+QS_EXPORT qs_status qs_tensor_wire_size(const qs_tensor *T, int64_t *bytes);
+QS_EXPORT qs_status qs_tensor_to_wire(qs_ctx *ctx, const qs_tensor *T, void *buf, int64_t bytes);
 /* Same contraction as qs_contractQS with device-resident operands and result. */
 QS_EXPORT qs_status qs_contract_dev(qs_ctx *ctx, const qs_tensor *A, const char *ia,
                           const qs_tensor *B, const char *ib,

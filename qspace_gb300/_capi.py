@@ -93,6 +93,12 @@ SIGNATURES = {
                                      c_double_p]),
     "qs_tensor_data": (C.c_void_p, [C.c_void_p]),
     "qs_tensor_free": (_V, [C.c_void_p]),
+    "qs_wire_size": (C.c_int, [C.POINTER(QSpaceView), C.POINTER(C.c_int64)]),
+    "qs_wire_pack": (C.c_int, [C.POINTER(QSpaceView), C.c_void_p, C.c_int64]),
+    "qs_wire_view": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(QSpaceView)]),
+    "qs_tensor_from_wire": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
+    "qs_tensor_wire_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "qs_tensor_to_wire": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
     "qs_contract_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_char_p, C.c_void_p, C.c_char_p,
                                   c_int32_p, C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p),
                                   C.POINTER(Stats)]),

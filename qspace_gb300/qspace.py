@@ -24,7 +24,7 @@ from . import _capi
 from ._capi import QSError, QSpaceView, Opts, Stats, check
 
 __all__ = ["QSpace", "Tensor", "Context", "contractQS", "permuteQS", "default_context",
-           "upload", "contract_dev", "permute_dev"]
+           "upload", "contract_dev", "permute_dev", "to_wire", "from_wire", "upload_wire"]
 
 
 # --------------------------------------------------------------------- QSpace
@@ -76,7 +76,7 @@ class QSpace:
         n, r = self.nblk, self.rank
         qd = self.qdim
         cplx = self.is_complex
-        if n:
+        if n and r:
             q = np.stack([np.asarray(x, dtype=np.int32).reshape(n, qd) for x in self.Q], axis=1)
             q = np.ascontiguousarray(q.reshape(n, r * qd), dtype=np.int32)
         else:
@@ -325,6 +325,15 @@ class Tensor:
             info["itags"] = tb.value.decode().split(",")
         return QSpace.unpack(rank, qdim, q[:n * rank * qdim], dims[:n * rank], offs[:n], data, cx, info)
 
+    def to_wire(self) -> np.ndarray:
+        """The tensor as a wire container (qs_tensor_to_wire: its device data
+        copied once, straight into the container's data section)."""
+        n = C.c_int64()
+        check(self.ctx.lib.qs_tensor_wire_size(self.h, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        check(self.ctx.lib.qs_tensor_to_wire(self.ctx.h, self.h, buf.ctypes.data_as(C.c_void_p), n.value))
+        return buf
+
     def free(self):
         if self.h:
             self.ctx.lib.qs_tensor_free(self.h)
@@ -335,6 +344,64 @@ class Tensor:
             self.free()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------ wire container
+def to_wire(A: QSpace) -> np.ndarray:
+    """Pack a QSpace into one flat binary container (qs_wire_pack); returns a
+    uint8 array (64-byte aligned) that can be written, sent or memory-mapped."""
+    lib = _capi.load()
+    v, keep = A.pack()
+    n = C.c_int64()
+    check(lib.qs_wire_size(C.byref(v), C.byref(n)))
+    buf = np.empty(n.value, np.uint8)
+    check(lib.qs_wire_pack(C.byref(v), buf.ctypes.data_as(C.c_void_p), n.value))
+    del keep
+    return buf
+
+
+def _aligned(buf) -> np.ndarray:
+    a = np.frombuffer(buf, np.uint8)
+    if a.ctypes.data % 8:
+        a = a.copy()   # the container's sections are read in place: 8-byte alignment
+    return a
+
+
+def from_wire(buf) -> QSpace:
+    """Read a container without copying its data: the blocks of the returned
+    QSpace are read-only numpy views into ``buf`` (qs_wire_view validates
+    the container first)."""
+    lib = _capi.load()
+    a = _aligned(buf)
+    v = QSpaceView()
+    check(lib.qs_wire_view(a.ctypes.data_as(C.c_void_p), a.size, C.byref(v)))
+    base = a.ctypes.data
+    n, r, qd = v.nblk, v.rank, v.qdim
+
+    def at(ptr, dtype, count):
+        off = C.cast(ptr, C.c_void_p).value - base if count else 0
+        return np.frombuffer(a, dtype, count, off) if count else np.zeros(0, dtype)
+
+    q = at(v.q, np.int32, n * r * qd)
+    dims = at(v.dims, np.int64, n * r)
+    offs = at(v.offs, np.int64, n)
+    ext = int(max((offs[i] + int(np.prod(dims[i * r:(i + 1) * r])) for i in range(n)), default=0)) if n else 0
+    data = at(v.data, np.float64, ext * (2 if v.is_complex else 1))
+    info = {"itags": v.itags.decode().split(",")} if v.itags else {}
+    if n == 0:
+        return QSpace([np.zeros((0, qd), np.int32) for _ in range(r)], [], info)
+    return QSpace.unpack(r, qd, q, dims, offs, data, bool(v.is_complex), info)
+
+
+def upload_wire(buf, ctx: Context | None = None, info: dict | None = None) -> Tensor:
+    """Device tensor straight from a container (one host->device copy of
+    its data section; qs_tensor_from_wire)."""
+    ctx = ctx or default_context()
+    a = _aligned(buf)
+    h = C.c_void_p()
+    check(ctx.lib.qs_tensor_from_wire(ctx.h, a.ctypes.data_as(C.c_void_p), a.size, C.byref(h)))
+    ctx.sync()
+    return Tensor(ctx, h, info)
 
 
 def upload(A: QSpace, ctx: Context | None = None) -> Tensor:
