@@ -160,6 +160,9 @@ QS_EXPORT qs_status qs_tensor_info(const qs_tensor *T, int32_t *rank, int32_t *q
                          int64_t *nblk, int64_t *nelem, int32_t *is_complex);
 QS_EXPORT qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q,
                              int64_t *dims, int64_t *offs, double *data);
+/* Labels, dims and element offsets of a device tensor (host copies of its
+ * metadata only; any pointer may be NULL). */
+QS_EXPORT qs_status qs_tensor_meta(const qs_tensor *T, int32_t *q, int64_t *dims, int64_t *offs);
 /* Device pointer of the block data (for callers that keep data on device). */
 QS_EXPORT const double *qs_tensor_data(const qs_tensor *T);
 QS_EXPORT qs_status qs_tensor_itags(const qs_tensor *T, char *buf, size_t len);
@@ -331,6 +334,18 @@ QS_EXPORT qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E
                        const double *qdim_w, int64_t nkeep, double etrunc,
                        double deps, uint8_t *keep, int64_t *nkeep_out,
                        double *etrunc_out);
+
+/* eigQS on a device-resident block-diagonal rank-2 QSpace H (EigenSymmetric,
+ * Source/QSpace.cc:4673-4939, with markSet): block eig on the device, the
+ * global truncation (as qs_mark_keep) from the eigenvalues, and the kept /
+ * discarded eigenvectors as new device tensors *AK / *AD (legs: H's first
+ * leg and the eigenstate index, labels of H's block; blocks without kept
+ * resp. discarded states are omitted).  Optional host outputs: E (sum of the
+ * block sizes) = ascending eigenvalues per block in H's block order, keep =
+ * 0/1 per eigenvalue, the kept count and the truncation energy. */
+QS_EXPORT qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc,
+                       double deps, qs_tensor **AK, qs_tensor **AD, double *E,
+                       uint8_t *keep, int64_t *nkeep_out, double *etrunc_out);
 
 /* -------------------------------------------------------- svdQS blocks
  * Thin SVD of every block (SVD_Data::blockSVD, Source/mpsortho.cc:546-613 ->

@@ -814,6 +814,16 @@ qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q, int64_
   QS_API_END
 }
 
+qs_status qs_tensor_meta(const qs_tensor *T, int32_t *q, int64_t *dims, int64_t *offs) {
+  QS_API_BEGIN
+  if (!T) fail(QS_ERR_ARG, "null tensor");
+  const QMeta &m = T->meta;
+  if (q && !m.q.empty()) std::memcpy(q, m.q.data(), m.q.size() * 4);
+  if (dims && !m.dims.empty()) std::memcpy(dims, m.dims.data(), m.dims.size() * 8);
+  if (offs && !m.offs.empty()) std::memcpy(offs, m.offs.data(), m.offs.size() * 8);
+  QS_API_END
+}
+
 const double *qs_tensor_data(const qs_tensor *T) { return T ? T->d : nullptr; }
 
 static void copy_tags(const std::vector<std::string> &t, char *buf, size_t len) {

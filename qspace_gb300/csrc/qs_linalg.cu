@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "qs_internal.h"
+#include "qs_objects.h"
 
 namespace qs {
 
@@ -639,6 +640,113 @@ qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E, const do
   if (nblk < 0 || (nblk > 0 && (!n || !E || !keep))) fail(QS_ERR_ARG, "null argument");
   if (qdim_w) fail(QS_ERR_UNSUPPORTED, "multiplet weights: markSet counts every multiplet once; pass NULL");
   mark_keep_host(nblk, n, E, nkeep, etrunc, deps, keep, nkeep_out, etrunc_out);
+  QS_API_END
+}
+
+// eigQS on a device-resident block-diagonal rank-2 QSpace (EigenSymmetric,
+// Source/QSpace.cc:4673-4939, with markSet, Source/gathered.cc:1822-2040):
+// block eig on the device, the global truncation on the host from the
+// eigenvalues alone (a few bytes per state), and the kept / discarded
+// eigenvectors gathered into device tensors AK / AD without leaving the
+// device.  Every block's kept states are its lowest ones (markSet keeps a
+// prefix of the ascending global order), i.e. its first k columns.
+qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc, double deps, qs_tensor **AK,
+                       qs_tensor **AD, double *E, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
+  QS_API_BEGIN
+  if (!ctx || !H || !AK || !AD) fail(QS_ERR_ARG, "null argument");
+  Ctx *c = &ctx->c;
+  QS_CUDA(cudaSetDevice(c->device));
+  const QMeta &m = H->meta;
+  if (m.rank != 2) fail(QS_ERR_SHAPE, "eigQS: rank-2 QSpace required (got rank %d)", m.rank);
+  const int64_t nb = m.nblk;
+  std::vector<int64_t> n(nb), eoffs(nb);
+  int64_t ntot = 0;
+  for (int64_t i = 0; i < nb; ++i) {
+    const int64_t *d = m.drow(i);
+    if (d[0] != d[1]) fail(QS_ERR_SHAPE, "eigQS: block %lld is %lld x %lld, not square", (long long)i, (long long)d[0], (long long)d[1]);
+    const int32_t *q = m.qrow(i);
+    for (int j = 0; j < m.qdim; ++j)
+      if (q[j] != q[m.qdim + j]) fail(QS_ERR_LABEL, "eigQS: block %lld is not on the diagonal", (long long)i);
+    n[i] = d[0];
+    eoffs[i] = ntot;
+    ntot += d[0];
+  }
+  const int es = m.cplx ? 2 : 1;
+  double *U = dev_alloc<double>(c, (size_t)std::max<int64_t>(m.nelem, 1) * es);
+  double *dE = dev_alloc<double>(c, (size_t)std::max<int64_t>(ntot, 1));
+  std::vector<double> hE((size_t)std::max<int64_t>(ntot, 1));
+  std::vector<uint8_t> hk((size_t)std::max<int64_t>(ntot, 1));
+  int64_t nk = 0;
+  double et = 0;
+  try {
+    eig_blocks(c, nb, n.data(), m.offs.data(), eoffs.data(), H->d, dE, U, m.cplx);
+    if (ntot) QS_CUDA(cudaMemcpyAsync(hE.data(), dE, ntot * 8, cudaMemcpyDeviceToHost, c->stream));
+    QS_CUDA(cudaStreamSynchronize(c->stream));
+    mark_keep_host(nb, n.data(), hE.data(), nkeep, etrunc, deps, hk.data(), &nk, &et);
+    // kept / discarded parts of each block
+    std::vector<int64_t> k(nb);
+    for (int64_t i = 0; i < nb; ++i) {
+      int64_t j = 0;
+      while (j < n[i] && hk[eoffs[i] + j]) ++j;
+      k[i] = j;
+      for (int64_t t = j; t < n[i]; ++t)
+        if (hk[eoffs[i] + t]) fail(QS_ERR_INTERNAL, "eigQS: kept states of block %lld are not its lowest", (long long)i);
+    }
+    auto part = [&](bool kept) {
+      auto T = std::make_unique<qs_tensor>();
+      T->ctx = c;
+      QMeta &o = T->meta;
+      o.rank = 2;
+      o.qdim = m.qdim;
+      o.cplx = m.cplx;
+      o.itags = m.itags;
+      std::vector<int64_t> so, dof, sz;
+      int64_t off = 0;
+      for (int64_t i = 0; i < nb; ++i) {
+        const int64_t cols = kept ? k[i] : n[i] - k[i];
+        if (cols == 0) continue;
+        const int32_t *q = m.qrow(i);
+        o.q.insert(o.q.end(), q, q + 2 * m.qdim);
+        o.dims.push_back(n[i]);
+        o.dims.push_back(cols);
+        o.offs.push_back(off);
+        so.push_back(m.offs[i] + (kept ? 0 : n[i] * k[i]));  // first or remaining columns
+        dof.push_back(off);
+        sz.push_back(n[i] * cols);
+        off += n[i] * cols;
+      }
+      o.nblk = (int64_t)o.offs.size();
+      o.nelem = off;
+      T->d = dev_alloc<double>(c, (size_t)std::max<int64_t>(off, 1) * es);
+      if (o.nblk) {
+        int64_t mx = 1;
+        for (int64_t v : sz) mx = std::max(mx, v);
+        int64_t *d_so = dev_upload(c, so), *d_do = dev_upload(c, dof), *d_sz = dev_upload(c, sz);
+        if (o.nblk > 65535) fail(QS_ERR_SHAPE, "eigQS: too many blocks in one call");
+        dim3 g((unsigned)std::min<int64_t>((mx * es + 255) / 256, 1024), (unsigned)o.nblk);
+        copy_blocks_kernel<<<g, 256, 0, c->stream>>>(U, T->d, d_so, d_do, d_sz, es);
+        QS_LAUNCHED(c);
+        dev_free(c, d_so);
+        dev_free(c, d_do);
+        dev_free(c, d_sz);
+      }
+      return T;
+    };
+    std::unique_ptr<qs_tensor> tk = part(true), td = part(false);
+    dev_free(c, U);
+    dev_free(c, dE);
+    U = dE = nullptr;
+    if (E && ntot) std::memcpy(E, hE.data(), ntot * 8);
+    if (keep && ntot) std::memcpy(keep, hk.data(), ntot);
+    if (nkeep_out) *nkeep_out = nk;
+    if (etrunc_out) *etrunc_out = et;
+    *AK = tk.release();
+    *AD = td.release();
+  } catch (...) {
+    if (U) dev_free(c, U);
+    if (dE) dev_free(c, dE);
+    throw;
+  }
   QS_API_END
 }
 

@@ -145,3 +145,31 @@ def gs_reortho(V: np.ndarray, v: np.ndarray, ctx: Context | None = None):
                                 C.byref(nrm)))
     ctx.sync()
     return dv.cpu().numpy(), nrm.value
+
+
+def eigQS_dev(H, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0):
+    """eigQS of a device tensor (qs_eigQS_dev): the eigenvectors stay on the
+    device.  Returns (Etot, I) with Etot the ascending eigenvalues of all
+    blocks, I['AK'] / I['AD'] device Tensors of the kept / discarded
+    eigenvectors, I['E'] the per-block eigenvalues (H's block order),
+    I['keep'] their 0/1 flags, I['NK'] the kept count, I['Etrunc']."""
+    from .qspace import Tensor
+    ctx = H.ctx
+    rank, qdim, nblk, nelem, cx = H.meta()
+    if rank != 2:
+        raise ValueError("eigQS_dev: rank-2 tensor required")
+    dims = np.empty(max(nblk * 2, 1), np.int64)
+    check(ctx.lib.qs_tensor_meta(H.h, None, dims.ctypes.data_as(_capi.c_int64_p), None))
+    ntot = int(dims[:2 * nblk:2].sum()) if nblk else 0
+    E = np.zeros(max(ntot, 1), np.float64)
+    keep = np.zeros(max(ntot, 1), np.uint8)
+    ak, ad = C.c_void_p(), C.c_void_p()
+    nk, et = C.c_int64(), C.c_double()
+    check(ctx.lib.qs_eigQS_dev(ctx.h, H.h, int(Nkeep), float(Etrunc), float(deps), C.byref(ak), C.byref(ad),
+                               E.ctypes.data_as(_capi.c_double_p), keep.ctypes.data_as(C.POINTER(C.c_uint8)),
+                               C.byref(nk), C.byref(et)))
+    E, keep = E[:ntot], keep[:ntot].astype(bool)
+    parts = {"AK": Tensor(ctx, ak, H.info), "AD": Tensor(ctx, ad, H.info), "E": E, "keep": keep,
+             "NK": nk.value, "Etrunc": et.value}
+    return np.sort(E), parts
+

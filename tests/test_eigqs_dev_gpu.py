@@ -1,0 +1,81 @@
+"""eigQS on a device-resident QSpace (qs_eigQS_dev): the same eigenvectors
+and truncation as the host-side eigQS (bit for bit: same kernels on the same
+blocks), the oracle's markSet restatement for the kept set (Nkeep, Etrunc and
+degeneracy averaging), kept states = the lowest of each block, and AK, AD
+orthonormal with AK^H H AK diagonal."""
+import numpy as np
+import pytest
+
+from oracle import qs_oracle as orc
+from qspace_gb300 import QSpace, upload
+from qspace_gb300.linalg import eigQS, eigQS_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _herm(rng, n, cplx):
+    a = rng.standard_normal((n, n))
+    if cplx:
+        a = a + 1j * rng.standard_normal((n, n))
+    return (a + a.conj().T) / 2
+
+
+def _H(seed, cplx, sizes):
+    rng = np.random.default_rng(seed)
+    labels = np.array([[q, s] for q, s in zip(range(-len(sizes) // 2, len(sizes)), [1, -1] * len(sizes))][:len(sizes)],
+                      np.int32)
+    data = [_herm(rng, n, cplx) for n in sizes]
+    return QSpace([labels.copy(), labels.copy()], data, {"itags": ["K", "K*"]})
+
+
+def _blocks(Q: QSpace):
+    return {tuple(np.asarray(Q.Q[0][i]).ravel()): np.asarray(d) for i, d in enumerate(Q.data)}
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("nkeep,etrunc,deps", [(-1, 0.0, 0.0), (25, 0.0, 0.0), (60, 0.0, 1e-3), (200, 1.5, 0.0)])
+def test_eigqs_dev_matches_host_and_oracle(ctx, cplx, nkeep, etrunc, deps):
+    sizes = [1, 7, 40, 40, 17, 64, 3, 33, 40, 120]
+    H = _H(11, cplx, sizes)
+    T = upload(H, ctx)
+    Etot, I = eigQS_dev(T, Nkeep=nkeep, Etrunc=etrunc, deps=deps)
+    Eh, Ih = eigQS(H, Nkeep=nkeep, Etrunc=etrunc, deps=deps, ctx=ctx)
+    assert np.array_equal(Etot, Eh) and I["NK"] == Ih["NK"]
+    ref_E = [np.linalg.eigvalsh(d) for d in H.data]
+    keep_ref, nk_ref = orc.mark_keep(ref_E, nkeep, etrunc, deps)
+    assert I["NK"] == nk_ref
+    AK, AD = I["AK"].download(), I["AD"].download()
+    for part, host in ((AK, Ih["AK"]), (AD, Ih["AD"])):
+        a, b = _blocks(part), _blocks(host)
+        assert a.keys() == b.keys()
+        for k in a:
+            assert np.asarray(a[k]).tobytes(order="F") == np.asarray(b[k]).tobytes(order="F")
+    # kept = the lowest states of each block; vectors orthonormal, H diagonal on them
+    o = 0
+    ak, ad = _blocks(AK), _blocks(AD)
+    for i, (d, e) in enumerate(zip(H.data, ref_E)):
+        key = tuple(np.asarray(H.Q[0][i]).ravel())
+        n = d.shape[0]
+        flags = I["keep"][o:o + n]
+        k = int(flags.sum())
+        assert np.all(flags[:k]) and not np.any(flags[k:])
+        assert k == int(np.sum(keep_ref[i]))
+        U = np.hstack([x for x in (ak.get(key), ad.get(key)) if x is not None])
+        assert U.shape == (n, n)
+        assert np.max(np.abs(U.conj().T @ U - np.eye(n))) <= 1e-12 * n
+        D = U.conj().T @ d @ U
+        assert np.max(np.abs(D - np.diag(np.diag(D)))) <= 1e-11 * max(1.0, np.abs(e).max())
+        assert np.max(np.abs(np.diag(D).real - I["E"][o:o + n])) <= 1e-11 * max(1.0, np.abs(e).max())
+        o += n
+    assert AK.info.get("itags") == ["K", "K*"]
+    for t in (T, I["AK"], I["AD"]):
+        t.free()
+
+
+def test_eigqs_dev_rejects_off_diagonal(ctx):
+    from qspace_gb300._capi import QSError
+    H = QSpace([np.array([[0], [1]], np.int32), np.array([[1], [0]], np.int32)], [np.eye(2), np.eye(2)])
+    T = upload(H, ctx)
+    with pytest.raises(QSError) as e:
+        eigQS_dev(T)
+    assert e.value.code == 3
