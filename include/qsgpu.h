@@ -160,6 +160,13 @@ QS_EXPORT qs_status qs_tensor_info(const qs_tensor *T, int32_t *rank, int32_t *q
                          int64_t *nblk, int64_t *nelem, int32_t *is_complex);
 QS_EXPORT qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q,
                              int64_t *dims, int64_t *offs, double *data);
+/* C = A + bfac * B for device tensors (plusQS, Source/plusQS.cc:11-45 with
+ * QSpace::plus_plain, Source/QSpace.cc:3593-3700): blocks of the union of both
+ * label sets in lexicographic label order, each the sum of the blocks present
+ * (dims must agree), then SkipZeroData (rank-2 exemption as in contractQS).
+ * Real + complex gives complex.  Abelian QSpaces. */
+QS_EXPORT qs_status qs_plus_dev(qs_ctx *ctx, const qs_tensor *A, const qs_tensor *B, double bfac,
+                      qs_tensor **C);
 /* Labels, dims and element offsets of a device tensor (host copies of its
  * metadata only; any pointer may be NULL). */
 QS_EXPORT qs_status qs_tensor_meta(const qs_tensor *T, int32_t *q, int64_t *dims, int64_t *offs);

@@ -29,7 +29,7 @@ import numpy as np
 
 __all__ = [
     "parse_ctr_idx", "contract", "permute", "block_dims", "rank_of",
-    "flops_of_contract", "skip_zero_blocks", "lexsort_rows",
+    "flops_of_contract", "skip_zero_blocks", "lexsort_rows", "plus",
 ]
 
 
@@ -495,6 +495,53 @@ def permute(A: dict, perm, conj: bool = False) -> dict:
     if conj:
         data = [np.conj(d) for d in data]
     return {"Q": Q, "data": data, "info": dict(A.get("info") or {})}
+
+
+def plus(A: dict, B: dict, bfac: float = 1.0) -> dict:
+    """Restates plusQS for abelian QSpaces (Source/plusQS.cc:11-45 ->
+    QSpace::plus_plain, Source/QSpace.cc:3593-3700; getQOverlapU :3520-):
+    the label records of A then B are concatenated and grouped (groupRecs:
+    lexicographic order, a record at most once per operand); each output
+    block is A's block + bfac * B's block (either alone when the other has
+    none), then SkipZeroData."""
+    na, nb = nblk_of(A), nblk_of(B)
+    if na == 0 and nb == 0:
+        return {"Q": [], "data": [], "info": dict(A.get("info") or B.get("info") or {})}
+    r = rank_of(A) if na else rank_of(B)
+    rows, src = [], []
+    for X, tag, n in ((A, 0, na), (B, 1, nb)):
+        if n:
+            rows.append(qrows(X, list(range(r))))
+            src += [(tag, i) for i in range(n)]
+    R = np.concatenate(rows, axis=0)
+    P = lexsort_rows(R)
+    cplx = any(np.iscomplexobj(d) for X in (A, B) for d in X["data"])
+    dt = np.complex128 if cplx else np.float64
+    outQ, data = [], []
+    k = 0
+    while k < len(P):
+        e = k + 1
+        while e < len(P) and np.array_equal(R[P[e]], R[P[k]]):
+            e += 1
+        if e - k > 2 or (e - k == 2 and src[P[k]][0] == src[P[k + 1]][0]):
+            raise ValueError("plus: non-unique block labels")
+        acc = None
+        for j in range(k, e):
+            tag, i = src[P[j]]
+            X = B if tag else A
+            blk = np.asarray(X["data"][i], dt).reshape(block_dims(X, i), order="F") * (bfac if tag else 1.0)
+            acc = blk if acc is None else acc + blk
+        outQ.append(R[P[k]])
+        data.append(acc)
+        k = e
+    Rq = np.asarray(outQ)
+    qd = Rq.shape[1] // r
+    Q = [Rq[:, l * qd:(l + 1) * qd].astype(np.int32) for l in range(r)]
+    Q, data = skip_zero_blocks(Q, data)
+    info = dict(A.get("info") or {}) or dict(B.get("info") or {})
+    if not data:
+        return {"Q": [], "data": [], "info": info}
+    return {"Q": Q, "data": data, "info": info}
 
 
 def flops_of_contract(A: dict, ia, B: dict, ib) -> int:

@@ -814,6 +814,133 @@ qs_status qs_tensor_download(qs_ctx *ctx, const qs_tensor *T, int32_t *q, int64_
   QS_API_END
 }
 
+// C = A + bfac B for device tensors (plusQS, Source/plusQS.cc:11-45 ->
+// QSpace::plus_plain, Source/QSpace.cc:3593-3700): blocks of the union of both
+// label sets in lexicographic order of their label records (getQOverlapU:
+// cat + groupRecs), each the sum of the blocks present, then SkipZeroData
+// with its rank-2 exemption.  Abelian QSpaces; an empty operand contributes
+// nothing; itags from the operand that has them (both: they must agree).
+static std::unique_ptr<qs_tensor> plus_core(Ctx *ctx, const qs_tensor *A, const qs_tensor *B, double bfac) {
+  const QMeta &a = A->meta, &b = B->meta;
+  const bool ea = a.nblk == 0, eb = b.nblk == 0;
+  if (!ea && !eb && (a.rank != b.rank || a.qdim != b.qdim))
+    fail(QS_ERR_SHAPE, "plusQS: QSpace mismatch (QDIM=%d/%d; r=%d/%d)", a.qdim, b.qdim, a.rank, b.rank);
+  std::vector<std::string> tags = a.itags;
+  if (tags.empty()) tags = b.itags;
+  else if (!b.itags.empty() && b.itags != a.itags)
+    fail(QS_ERR_LABEL, "plusQS: inconsistent itags %s <> %s", join_itags(a.itags).c_str(), join_itags(b.itags).c_str());
+  const int rank = ea ? b.rank : a.rank, qd = ea ? b.qdim : a.qdim, w = rank * qd;
+  const bool cplx = a.cplx || b.cplx;
+  const int es = cplx ? 2 : 1;
+  // union of the label records (A's first), sorted, equal records grouped
+  struct Rec { const int32_t *q; int src; int64_t i; };
+  std::vector<Rec> all;
+  for (int64_t i = 0; i < a.nblk; ++i) all.push_back({a.qrow(i), 0, i});
+  for (int64_t i = 0; i < b.nblk; ++i) all.push_back({b.qrow(i), 1, i});
+  std::stable_sort(all.begin(), all.end(), [&](const Rec &x, const Rec &y) { return rec_compare(x.q, y.q, w) < 0; });
+  auto T = std::make_unique<qs_tensor>();
+  T->ctx = ctx;
+  QMeta &M = T->meta;
+  M.rank = rank;
+  M.qdim = qd;
+  M.cplx = cplx;
+  M.itags = tags;
+  std::vector<int64_t> sa, da, za, sb, db, zb;
+  int64_t off = 0, mxa = 1, mxb = 1;
+  for (size_t k = 0; k < all.size();) {
+    size_t e = k + 1;
+    while (e < all.size() && rec_compare(all[e].q, all[k].q, w) == 0) ++e;
+    if (e - k > 2 || (e - k == 2 && all[k].src == all[k + 1].src))
+      fail(QS_ERR_LABEL, "plusQS: non-unique block labels");
+    const QMeta &m0 = all[k].src ? b : a;
+    const int64_t *d0 = m0.drow(all[k].i);
+    if (e - k == 2) {
+      const QMeta &m1 = all[k + 1].src ? b : a;
+      const int64_t *d1 = m1.drow(all[k + 1].i);
+      for (int r = 0; r < rank; ++r)
+        if (d0[r] != d1[r]) fail(QS_ERR_SHAPE, "plusQS: block dims differ on leg %d (%lld/%lld)", r + 1, (long long)d0[r], (long long)d1[r]);
+    }
+    M.q.insert(M.q.end(), all[k].q, all[k].q + w);
+    M.dims.insert(M.dims.end(), d0, d0 + rank);
+    M.offs.push_back(off);
+    const int64_t sz = m0.bsize(all[k].i);
+    for (size_t j = k; j < e; ++j) {
+      const QMeta &mj = all[j].src ? b : a;
+      (all[j].src ? sb : sa).push_back(mj.offs[all[j].i]);
+      (all[j].src ? db : da).push_back(off);
+      (all[j].src ? zb : za).push_back(sz);
+      (all[j].src ? mxb : mxa) = std::max(all[j].src ? mxb : mxa, sz);
+    }
+    off += sz;
+    k = e;
+  }
+  M.nblk = (int64_t)M.offs.size();
+  M.nelem = off;
+  T->d = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(off, 1) * es);
+  QS_CUDA(cudaMemsetAsync(T->d, 0, (size_t)std::max<int64_t>(off, 1) * es * 8, ctx->stream));
+  auto add = [&](const std::vector<int64_t> &so, const std::vector<int64_t> &dof, const std::vector<int64_t> &sz,
+                 int64_t mx, const qs_tensor *X, double f) {
+    if (so.empty()) return;
+    int64_t *d1 = dev_upload(ctx, so), *d2 = dev_upload(ctx, dof), *d3 = dev_upload(ctx, sz);
+    for (int64_t c0 = 0; c0 < (int64_t)so.size(); c0 += 65535)
+      launch_block_axpy(ctx, d1 + c0, d2 + c0, d3 + c0, std::min<int64_t>(65535, (int64_t)so.size() - c0), mx, X->d,
+                        T->d, f, X->meta.cplx ? 2 : 1, es);
+    dev_free(ctx, d1);
+    dev_free(ctx, d2);
+    dev_free(ctx, d3);
+  };
+  add(sa, da, za, mxa, A, 1.0);
+  add(sb, db, zb, mxb, B, bfac);
+  if (M.nblk == 0) return T;
+  // SkipZeroData
+  std::vector<int64_t> sizes(M.nblk);
+  for (int64_t i = 0; i < M.nblk; ++i) sizes[i] = M.bsize(i);
+  int64_t *doff = dev_upload(ctx, M.offs), *dsz = dev_upload(ctx, sizes);
+  int *dflag = dev_alloc<int>(ctx, M.nblk);
+  launch_block_nonzero(ctx, doff, dsz, M.nblk, T->d, cplx ? 1 : 0, dflag);
+  std::vector<int> flags(M.nblk);
+  QS_CUDA(cudaMemcpyAsync(flags.data(), dflag, M.nblk * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, doff);
+  dev_free(ctx, dsz);
+  dev_free(ctx, dflag);
+  std::vector<int64_t> keep;
+  for (int64_t i = 0; i < M.nblk; ++i)
+    if (flags[i]) keep.push_back(i);
+  if ((int64_t)keep.size() < M.nblk && rank == 2) {
+    std::vector<double> h((size_t)M.nelem * es);
+    QS_CUDA(cudaMemcpyAsync(h.data(), T->d, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QS_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (rank2_keeps_zero_blocks(M, h)) {
+      keep.resize(M.nblk);
+      std::iota(keep.begin(), keep.end(), 0);
+    }
+  }
+  if ((int64_t)keep.size() < M.nblk) {
+    QMeta K = M;
+    K.q.clear();
+    K.dims.clear();
+    K.offs.clear();
+    for (int64_t i : keep) {
+      K.q.insert(K.q.end(), M.qrow(i), M.qrow(i) + w);
+      K.dims.insert(K.dims.end(), M.drow(i), M.drow(i) + rank);
+      K.offs.push_back(M.offs[i]);
+    }
+    K.nblk = (int64_t)keep.size();
+    if (K.nblk == 0) K.rank = 0;  // all zero: an empty QSpace (as the contraction's)
+    M = K;
+  }
+  return T;
+}
+
+qs_status qs_plus_dev(qs_ctx *ctx, const qs_tensor *A, const qs_tensor *B, double bfac, qs_tensor **C) {
+  QS_API_BEGIN
+  if (!ctx || !A || !B || !C) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  *C = plus_core(&ctx->c, A, B, bfac).release();
+  QS_API_END
+}
+
 qs_status qs_tensor_meta(const qs_tensor *T, int32_t *q, int64_t *dims, int64_t *offs) {
   QS_API_BEGIN
   if (!T) fail(QS_ERR_ARG, "null tensor");

@@ -141,6 +141,10 @@ void launch_block_nonzero(Ctx *ctx, const int64_t *d_offs, const int64_t *d_size
                           int64_t nblk, const double *data, int is_complex,
                           int *d_flags);
 void launch_widen(Ctx *ctx, const double *in, double *out, int64_t n);
+// dst block b += f * src block b (element offsets / sizes; es = 1 real, 2
+// complex; a real source into a complex destination adds to the real parts)
+void launch_block_axpy(Ctx *ctx, const int64_t *d_soff, const int64_t *d_doff, const int64_t *d_size, int64_t nb,
+                       int64_t max_size, const double *src, double *dst, double f, int es_src, int es_dst);
 // copies `bytes` from mapped page-locked host memory to device memory with a kernel
 void launch_stage_copy(Ctx *ctx, const void *src, void *dst, size_t bytes);
 

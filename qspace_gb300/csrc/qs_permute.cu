@@ -74,6 +74,32 @@ void launch_widen(Ctx *ctx, const double *in, double *out, int64_t n) {
   QS_LAUNCHED(ctx);
 }
 
+// dst block b += f * src block b over block lists (element offsets and
+// sizes); a real source added into a complex destination lands on the real
+// parts.  Blocks of one launch must not share destination elements.
+__global__ void block_axpy_kernel(const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
+                                  const int64_t *__restrict__ size, const double *__restrict__ src,
+                                  double *__restrict__ dst, double f, int es_src, int es_dst) {
+  const int64_t b = blockIdx.y;
+  const int64_t n = size[b];
+  const double *s = src + soff[b] * es_src;
+  double *d = dst + doff[b] * es_dst;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * es_src; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = es_src == es_dst ? i : i * es_dst;  // real into complex: every other double
+    d[e] = fma(f, s[i], d[e]);
+  }
+}
+
+void launch_block_axpy(Ctx *ctx, const int64_t *d_soff, const int64_t *d_doff, const int64_t *d_size, int64_t nb,
+                       int64_t max_size, const double *src, double *dst, double f, int es_src, int es_dst) {
+  if (nb <= 0) return;
+  if (nb > 65535) fail(QS_ERR_SHAPE, "block_axpy: %lld blocks in one launch", (long long)nb);
+  const unsigned gx = (unsigned)std::min<int64_t>((std::max<int64_t>(max_size, 1) * es_src + 255) / 256, 1024);
+  block_axpy_kernel<<<dim3(gx, (unsigned)nb), 256, 0, ctx->stream>>>(d_soff, d_doff, d_size, src, dst, f, es_src,
+                                                                      es_dst);
+  QS_LAUNCHED(ctx);
+}
+
 // Per-block nonzero test (SkipZeroData with eps = 0, Source/QSpace.cc:
 // 3201-3269): flags[b] = 1 when any element of block b differs from zero.
 __global__ void block_nonzero_kernel(const int64_t *__restrict__ offs,

@@ -24,7 +24,7 @@ from . import _capi
 from ._capi import QSError, QSpaceView, Opts, Stats, check
 
 __all__ = ["QSpace", "Tensor", "Context", "contractQS", "permuteQS", "default_context",
-           "upload", "contract_dev", "permute_dev", "to_wire", "from_wire", "upload_wire"]
+           "upload", "contract_dev", "permute_dev", "to_wire", "from_wire", "upload_wire", "plus_dev", "plusQS"]
 
 
 # --------------------------------------------------------------------- QSpace
@@ -426,6 +426,29 @@ def contract_dev(A: Tensor, ia, B: Tensor, ib, perm=None, *, prec: str = "fp64",
     if stats is not None:
         stats.update(st.as_dict())
     return Tensor(ctx, h)
+
+
+def plus_dev(A: Tensor, B: Tensor, bfac: float = 1.0) -> Tensor:
+    """plusQS of device tensors: A + bfac * B (qs_plus_dev)."""
+    ctx = A.ctx
+    h = C.c_void_p()
+    check(ctx.lib.qs_plus_dev(ctx.h, A.h, B.h, float(bfac), C.byref(h)))
+    return Tensor(ctx, h)
+
+
+def plusQS(A: QSpace, B: QSpace, bfac: float = 1.0, ctx: Context | None = None) -> QSpace:
+    """plusQS(A, B [,bfac]) with host QSpaces (through the device)."""
+    ctx = ctx or default_context()
+    ta, tb = upload(A, ctx), upload(B, ctx)
+    try:
+        tc = plus_dev(ta, tb, bfac)
+        try:
+            return tc.download()
+        finally:
+            tc.free()
+    finally:
+        ta.free()
+        tb.free()
 
 
 def contract_batch(jobs, *, prec: str = "fp64", nslices: int = 0, tol: float = 1e-12) -> list:
