@@ -1,0 +1,195 @@
+"""One Wilson-chain NRG iteration on device-resident QSpaces.
+
+The iteration of NRGWilsonQS (Source/NRGWilsonQS.cc: the loop around
+:740-900 with nrgBuildH4_cg, :1197-1300) for a spinful fermion chain with
+abelian U(1) charge x U(1) spin symmetry (labels (q, 2Sz); a site holds
+|0> (-1,0), |up> (0,1), |dn> (0,-1), |updn> (1,0), q counting electrons
+relative to half filling):
+
+  H_{N+1} = sqrt(Lambda) H_N + t_N sum_s (f_{N,s}^+ f_{N+1,s} + h.c.)
+
+1. A4(K, s, n): the product basis of the kept space K and the new site s,
+   one identity slice per (sector of K, site state) inside the combined
+   sector n = K + s (initIdentityCG for abelian symmetries).
+2. H4 = A4^+ (sqrt(Lambda) HK x 1) A4 + t sum_s [A4^+ (F_s^+ Z x c_s) A4 + h.c.]
+   with the kept-space annihilator F_s of the last site and the fermionic
+   sign Z = (-1)^N of the kept states (carried by A4Z = Z A4): contractQS and
+   plusQS on the device.  The first term is diagonal in the product basis
+   (sqrt(Lambda) E_K on each slice of A4) and is laid out on the host: as a
+   contraction its exactly-zero blocks (a zero-energy sector) would be
+   dropped by SkipZeroData.
+3. eigQS of H4 with the global truncation (markSet): the eigenvectors stay
+   on the device.
+4. The new A-tensor A(K, s, k) = A4 AK and the annihilator of the new site in
+   the new kept basis, F'_s = A^+ (Z x c_s) A.
+
+Everything but the label bookkeeping of A4 (host-built, uploaded) and the
+eigenvalues (a few bytes per state, needed on the host for the truncation)
+stays on the device.  The driver is written against a small backend
+interface (``DeviceBackend`` here); any object with the same methods that
+works on host QSpace dicts runs the same iteration on the CPU.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .qspace import QSpace
+
+SITE_LABELS = [(-1, 0), (0, 1), (0, -1), (1, 0)]   # |0>, |up>, |dn>, |updn>
+
+
+def site_ops() -> dict:
+    """Annihilators of one site as rank-2 QSpaces (out, in) with 1x1 blocks;
+    |updn> = c_up^+ c_dn^+ |0>, so c_dn |updn> = -|up>."""
+    L = SITE_LABELS
+    def op(entries):
+        Q0 = np.array([L[o] for o, _, _ in entries], np.int32)
+        Q1 = np.array([L[i] for _, i, _ in entries], np.int32)
+        return QSpace([Q0, Q1], [np.array([[v]], np.float64) for _, _, v in entries], {})
+    return {"up": op([(0, 1, 1.0), (2, 3, 1.0)]), "dn": op([(0, 2, 1.0), (1, 3, -1.0)])}
+
+
+def parity(label, nsites: int) -> int:
+    """(-1)^N of a sector: N = q + nsites electrons."""
+    return -1 if (int(label[0]) + nsites) % 2 else 1
+
+
+@dataclass
+class KeptSpace:
+    """The kept space after an iteration: sectors (label -> ascending
+    eigenvalues of its kept states) and the last site's annihilators F_s in
+    that basis (backend tensors)."""
+    nsites: int
+    E: dict                        # label tuple -> np.ndarray of energies
+    F: dict = field(default_factory=dict)
+    A: object = None               # A-tensor (K, s, k) of the last iteration (backend tensor)
+    nkept: int = 0
+    ntotal: int = 0                # states before truncation
+    Eall: np.ndarray = None        # all energies of the iteration, ascending
+
+
+def initial_space(backend, eps: float = 0.0, U: float = 0.0) -> KeptSpace:
+    """Site 0 alone: H_0 = eps n + U n_up n_dn, F_s = c_s."""
+    E = {}
+    for lab, n_up, n_dn in zip(SITE_LABELS, (0, 1, 0, 1), (0, 0, 1, 1)):
+        E[lab] = np.array([eps * (n_up + n_dn) + U * n_up * n_dn])
+    ops = site_ops()
+    return KeptSpace(1, E, {s: backend.put(c) for s, c in ops.items()}, nkept=4, ntotal=4)
+
+
+def _fusion(K: KeptSpace):
+    """A4 and A4Z = Z_K A4 (host QSpaces), and the combined sectors."""
+    sectors = sorted(K.E)
+    off, D = {}, {}
+    for s in SITE_LABELS:
+        for qk in sectors:
+            qn = (qk[0] + s[0], qk[1] + s[1])
+            off[(qk, s)] = D.get(qn, 0)
+            D[qn] = D.get(qn, 0) + len(K.E[qk])
+    Q = [[], [], []]
+    data, dataz = [], []
+    for s in SITE_LABELS:
+        for qk in sectors:
+            qn = (qk[0] + s[0], qk[1] + s[1])
+            d = len(K.E[qk])
+            blk = np.zeros((d, 1, D[qn]))
+            blk[:, 0, off[(qk, s)]:off[(qk, s)] + d] = np.eye(d)
+            Q[0].append(qk)
+            Q[1].append(s)
+            Q[2].append(qn)
+            data.append(blk)
+            dataz.append(parity(qk, K.nsites) * blk)
+    Qa = [np.array(x, np.int32) for x in Q]
+    return QSpace(Qa, data, {}), QSpace([q.copy() for q in Qa], dataz, {}), D, off
+
+
+def _diag_product(K: KeptSpace, D: dict, off: dict, f: float) -> QSpace:
+    """f (E_K x 1) in the product basis: one diagonal block per combined
+    sector, E_K placed on the slice of each (K sector, site state)."""
+    diag = {qn: np.zeros(d) for qn, d in D.items()}
+    for (qk, s), o in off.items():
+        qn = (qk[0] + s[0], qk[1] + s[1])
+        diag[qn][o:o + len(K.E[qk])] = f * K.E[qk]
+    labs = sorted(diag)
+    Q = np.array(labs, np.int32)
+    return QSpace([Q, Q.copy()], [np.diag(diag[l]) for l in labs], {})
+
+
+def step(K: KeptSpace, backend, t: float, Lambda: float, nkeep: int = -1, deps: float = 0.0) -> KeptSpace:
+    """One iteration: H_{N+1} from the kept space K, its eigen-decomposition
+    and truncation to nkeep states (markSet; deps > 0 keeps near-degenerate
+    levels together), the new kept space."""
+    A4, A4Z, D, off = _fusion(K)
+    a4, a4z = backend.put(A4), backend.put(A4Z)
+    c = {s: backend.put(q) for s, q in site_ops().items()}
+    H = backend.put(_diag_product(K, D, off, math.sqrt(Lambda)))
+    for s in ("up", "dn"):
+        Fd = backend.permute(K.F[s], [2, 1], conj=True)            # f_{N,s}^+ in K
+        X1 = backend.contract(Fd, "2", a4z, "1")                   # (K', s, n), Z on K
+        X2 = backend.contract(c[s], "2", X1, "2")                  # (s', K', n)
+        T = backend.contract(a4, "12*", X2, "21")                  # (n', n)
+        # T + T^+ first: every partial sum stays hermitian, so SkipZeroData's
+        # rank-2 exemption keeps zero-energy sectors of H
+        H = backend.plus(H, backend.plus(T, backend.permute(T, [2, 1], conj=True), 1.0), t)
+    labels, E, keep, AK = backend.eig(H, nkeep, deps)
+    Anew = backend.contract(a4, "3", AK, "1")                      # (K, s, k)
+    AnewZ = backend.contract(a4z, "3", AK, "1")
+    F = {}
+    for s in ("up", "dn"):
+        X = backend.contract(c[s], "2", AnewZ, "2")                # (s', K, k)
+        F[s] = backend.contract(Anew, "12*", X, "21")              # (k', k)
+    Ek = {}
+    for lab, e, k in zip(labels, E, keep):
+        if np.any(k):
+            Ek[lab] = e[k]
+    return KeptSpace(K.nsites + 1, Ek, F, Anew, nkept=int(sum(int(np.sum(k)) for k in keep)),
+                     ntotal=int(sum(len(e) for e in E)), Eall=np.sort(np.concatenate(E)))
+
+
+class DeviceBackend:
+    """The iteration's operations on device tensors (qs_contract_dev,
+    qs_permute_dev, qs_plus_dev, qs_eigQS_dev)."""
+
+    def __init__(self, ctx=None, prec: str = "fp64"):
+        from .qspace import default_context
+        self.ctx = ctx or default_context()
+        self.prec = prec
+
+    def put(self, A: QSpace):
+        from .qspace import upload
+        return upload(A, self.ctx)
+
+    def contract(self, A, ia, B, ib):
+        from .qspace import contract_dev
+        return contract_dev(A, ia, B, ib, prec=self.prec)
+
+    def permute(self, A, perm, conj=False):
+        from .qspace import permute_dev
+        return permute_dev(A, perm, conj)
+
+    def plus(self, A, B, f):
+        from .qspace import plus_dev
+        return plus_dev(A, B, f)
+
+    def eig(self, H, nkeep, deps=0.0):
+        """(labels of H's blocks, per-block ascending energies, per-block
+        kept flags, device tensor of the kept eigenvectors)."""
+        from . import _capi
+        from .linalg import eigQS_dev
+        _, I = eigQS_dev(H, Nkeep=nkeep, deps=deps)
+        rank, qdim, nblk, _, _ = H.meta()
+        q = np.empty(max(nblk * rank * qdim, 1), np.int32)
+        dims = np.empty(max(nblk * rank, 1), np.int64)
+        _capi.check(self.ctx.lib.qs_tensor_meta(H.h, q.ctypes.data_as(_capi.c_int32_p),
+                                                dims.ctypes.data_as(_capi.c_int64_p), None))
+        q = q[:nblk * rank * qdim].reshape(nblk, rank, qdim)
+        n = dims[:nblk * rank:rank]
+        o = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+        labels = [tuple(int(x) for x in q[i, 0]) for i in range(nblk)]
+        E = [I["E"][o[i]:o[i] + n[i]] for i in range(nblk)]
+        keep = [I["keep"][o[i]:o[i] + n[i]] for i in range(nblk)]
+        I["AD"].free()
+        return labels, E, keep, I["AK"]
