@@ -434,9 +434,10 @@ def main():
                 ts.append(time.perf_counter() - t0)
             rdm[pr + "_ms_p50"] = 1e3 * statistics.median(ts)
 
-    # ---- FP64 block eigendecompositions of one NRG step (SURVEY config 3,
-    # abelian stand-in): every symmetry block of a 39300-state Hamiltonian,
-    # 336 blocks of sizes 1..690, on the device; eig flops = sum (10/3) n^3
+    # ---- FP64 block eigendecompositions of one NRG step (abelian U(1)xU(1)
+    # stand-in for the SU(2)xU(1) Wilson chain): every symmetry block of a
+    # 39300-state Hamiltonian, 336 blocks of sizes 1..690, on the device;
+    # eig flops = sum (10/3) n^3
     eig = None
     if not a.no_extras:
         from qspace_gb300.workloads import nrg_eig_blocks
@@ -481,6 +482,36 @@ def main():
                 eig["cpu_baseline"] = {"ms": cb_["seconds_per_step"] * 1e3, "tflops": cb_["value"],
                                        "cores": cb_["cores"], "kind": "port"}
         del dH, dU, dE
+
+    # ---- whole Wilson-chain NRG iterations resident on the device: product
+    # basis, hopping terms by contractions, plusQS, eigQS with truncation to
+    # 4096 kept states (16k product states), new A-tensor and site operators
+    nrg = None
+    if not a.no_extras:
+        from qspace_gb300.nrg import DeviceBackend, initial_space, step as nrg_step
+        Lam_, nk_ = 2.5, 4096
+        nrg = {"workload": "Wilson-chain NRG iteration, spinful U(1)xU(1) chain, Nkeep 4096 (16k product states), "
+                           "Lambda 2.5; ms per iteration at full size, median of 3"}
+        for pr_ in ("split", "fp64"):
+            be_ = DeviceBackend(ctx, pr_)
+            K_ = initial_space(be_, -0.2, 0.6)
+            its = []
+            for it_ in range(10):
+                ctx.sync()
+                t0 = time.perf_counter()
+                K_ = nrg_step(K_, be_, 1.0, Lam_, nkeep=nk_, deps=1e-8)
+                ctx.sync()
+                its.append(time.perf_counter() - t0)
+            nrg[pr_ + "_ms"] = 1e3 * statistics.median(its[-3:])
+            nrg["kept"], nrg["product_states"] = K_.nkept, K_.ntotal
+            del K_, be_
+        if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+            out_ = subprocess.run([sys.executable, "-m", "oracle.cpu_baseline", "--nrg", "--max-seconds", "60"],
+                                  cwd=ROOT, capture_output=True, text=True)
+            if out_.returncode == 0:
+                cb_ = json.loads(out_.stdout.strip().splitlines()[-1])
+                nrg["cpu_baseline"] = {"ms": cb_["seconds_per_step"] * 1e3, "cores": cb_["cores"], "kind": "port",
+                                       "sample": cb_["sample"]}
 
     # ---- serving loop under Poisson load (split and plain), device-resident tensors
     serving = None
@@ -535,7 +566,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "slices": slices, "rdm_latency": rdm, "eig": eig, "serving": serving,
+                "slices": slices, "rdm_latency": rdm, "eig": eig, "nrg": nrg, "serving": serving,
                 "clocks": ck}
         print(json.dumps(line))
     if pg:

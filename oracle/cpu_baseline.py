@@ -78,6 +78,31 @@ def main_eig(a):
                       "sample": f"all {len(blocks)} blocks ({sum(b.shape[0] for b in blocks)} states) per step"}))
 
 
+def main_nrg(a):
+    """Wilson-chain NRG iterations (the same step and parameters as the
+    bench's device row: Nkeep 4096, Lambda 2.5, eps -0.2, U 0.6, t 1,
+    deps 1e-8) with the oracle backend: numpy block operations and LAPACK
+    eigh through OpenBLAS on all host cores.  Reports the median of the last
+    three of ten iterations (the kept space is full from the seventh on)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    from oracle.nrg_port import OracleBackend
+    from qspace_gb300.nrg import initial_space, step
+    be = OracleBackend()
+    K = initial_space(be, -0.2, 0.6)
+    ts = []
+    t_all = time.perf_counter()
+    for _ in range(10):
+        t0 = time.perf_counter()
+        K = step(K, be, 1.0, 2.5, nkeep=4096, deps=1e-8)
+        ts.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > a.max_seconds:
+            break
+    t = float(np.median(ts[-3:]))
+    print(json.dumps({"unit": "ms", "cores": a.threads, "seconds_per_step": t, "steps": len(ts),
+                      "sample": f"{len(ts)} iterations, median of the last 3 ({K.nkept} kept, {K.ntotal} product states)"}))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--npairs", type=int, default=2000)
@@ -87,9 +112,12 @@ def main(argv=None):
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--max-seconds", type=float, default=60.0)
     ap.add_argument("--eig", action="store_true", help="block eigendecompositions instead of block products")
+    ap.add_argument("--nrg", action="store_true", help="Wilson-chain NRG iterations instead of block products")
     a = ap.parse_args(argv)
     if a.eig:
         return main_eig(a)
+    if a.nrg:
+        return main_nrg(a)
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     sys.path.insert(0, root)
     from qspace_gb300.workloads import grouped_pairs
