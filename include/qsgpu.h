@@ -354,6 +354,17 @@ QS_EXPORT qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep,
                        double deps, qs_tensor **AK, qs_tensor **AD, double *E,
                        uint8_t *keep, int64_t *nkeep_out, double *etrunc_out);
 
+/* The truncation of svdQS (SVD_Data::dmrgTruncate, Source/mpsortho.cc:
+ * 616-700, markSet in descending order): given the singular values of every
+ * block (k[i] values of block i back to back in S, host arrays), marks the
+ * kept ones: those above stol (at least Nkmin of the largest when stol would
+ * drop more), at most Nkeep (< 0: no limit).  Returns the kept count, the
+ * discarded and the total weight (sums of S^2), and sfac, the factor that
+ * rescales the kept values to the full norm. */
+QS_EXPORT qs_status qs_svd_keep(int64_t nblk, const int64_t *k, const double *S, int64_t nkeep,
+                      int64_t nkmin, double stol, uint8_t *keep, int64_t *nkeep_out,
+                      double *s2t_out, double *s2tot_out, double *sfac_out);
+
 /* -------------------------------------------------------- svdQS blocks
  * Thin SVD of every block (SVD_Data::blockSVD, Source/mpsortho.cc:546-613 ->
  * wbSVD -> dgesdd, Source/wbarray_blas.cc:995-1090).  Block i is m[i] x n[i]

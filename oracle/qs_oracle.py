@@ -29,7 +29,7 @@ import numpy as np
 
 __all__ = [
     "parse_ctr_idx", "contract", "permute", "block_dims", "rank_of",
-    "flops_of_contract", "skip_zero_blocks", "lexsort_rows", "plus",
+    "flops_of_contract", "skip_zero_blocks", "lexsort_rows", "plus", "svd_keep",
 ]
 
 
@@ -623,6 +623,55 @@ def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float 
         l = imax
     keep[P[:min(l, N)]] = True
     return out()
+
+
+def svd_keep(S_blocks: list, nkeep: int = -1, nkmin: int = 0, stol: float = 0.0):
+    """Restates the truncation of svdQS: SVD_Data::dmrgTruncate
+    (Source/mpsortho.cc:616-700) with markSet in descending mode
+    (Source/gathered.cc:1822-1880, 1964-1972, 2037-2090; eps = b = 0).  All
+    singular values sorted ascending (stable); with stol > 0 the cut l is the
+    highest index with S[l] <= stol below N - Nkmin; the kept states are those
+    above the cut, at most Nkeep; the kept values are then rescaled by
+    sfac = sqrt(sum S^2 / (sum S^2 - discarded S^2)).  Returns (per-block
+    keep flags, number kept, discarded weight s2t, total weight, sfac)."""
+    sizes = [len(x) for x in S_blocks]
+    E0 = np.concatenate([np.asarray(x, float) for x in S_blocks]) if S_blocks else np.zeros(0)
+    N = len(E0)
+    keep = np.zeros(N, bool)
+    nkmin = max(0, int(nkmin))
+    if N:
+        P = np.argsort(E0, kind="stable")
+        E = E0[P]
+        nk = N if nkeep < 0 else int(nkeep)
+        if nk == 0:
+            pass
+        elif nk >= N and stol <= 0:
+            keep[:] = True
+        else:
+            nk = min(nk, N)
+            if stol > 0:
+                lx = N - nkmin if nkmin < N else 0
+                l = None
+                for j in range(N - 1, -1, -1):
+                    if E[j] <= stol and j < lx:
+                        l = j
+                        break
+                if l is None:
+                    l = N - 1 - nk if N > nk else None
+                elif N - 1 - l > nk:
+                    l = N - 1 - nk
+            else:
+                l = N - 1 - nk
+            if l is None or l < 0:
+                keep[:] = True
+            elif l < N - 1:
+                keep[P[l + 1:]] = True
+    s2 = E0 ** 2
+    snorm2 = float(s2.sum())
+    s2t = float(s2[~keep].sum())
+    sfac = float(np.sqrt(snorm2 / (snorm2 - s2t))) if 0 < s2t < snorm2 else 1.0
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(int)
+    return [keep[offs[i]:offs[i + 1]] for i in range(len(sizes))], int(keep.sum()), s2t, snorm2, sfac
 
 
 def gs_reortho(V: np.ndarray, v: np.ndarray):

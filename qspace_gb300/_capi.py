@@ -94,6 +94,9 @@ SIGNATURES = {
     "qs_tensor_data": (C.c_void_p, [C.c_void_p]),
     "qs_tensor_free": (_V, [C.c_void_p]),
     "qs_tensor_meta": (C.c_int, [C.c_void_p, c_int32_p, c_int64_p, c_int64_p]),
+    "qs_svd_keep": (C.c_int, [C.c_int64, c_int64_p, c_double_p, C.c_int64, C.c_int64, C.c_double,
+                              C.POINTER(C.c_uint8), C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                              C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "qs_plus_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.POINTER(C.c_void_p)]),
     "qs_eigQS_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.POINTER(C.c_void_p),
                                C.POINTER(C.c_void_p), c_double_p, C.POINTER(C.c_uint8), C.POINTER(C.c_int64),

@@ -261,6 +261,64 @@ void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nke
   if (etrunc_out) *etrunc_out = (l < N) ? s[l] - s[0] : 0.0;
 }
 
+// ------------------------------------------------------- svd truncation
+// The truncation of svdQS: SVD_Data::dmrgTruncate (Source/mpsortho.cc:
+// 616-700) with markSet in descending mode (Source/gathered.cc:1822-1880,
+// 1964-1972, 2037-2090; no degeneracy averaging, no gap search).  All
+// singular values are sorted ascending (stable); with stol > 0 the cut is the
+// highest index l < N - Nkmin with S[l] <= stol; the states above the cut are
+// kept, at most Nkeep of them (Nkeep < 0: all); the kept values are rescaled
+// by sfac = sqrt(sum S^2 / (sum S^2 - discarded S^2)) so that the norm is
+// preserved.
+void svd_keep_host(int64_t nblk, const int64_t *k, const double *S, int64_t nkeep, int64_t nkmin, double stol,
+                   uint8_t *keep, int64_t *nkeep_out, double *s2t_out, double *s2tot_out, double *sfac_out) {
+  int64_t N = 0;
+  for (int64_t i = 0; i < nblk; ++i) N += k[i];
+  std::fill(keep, keep + N, 0);
+  if (nkmin < 0) nkmin = 0;
+  if (N > 0) {
+    std::vector<int64_t> P(N);
+    std::iota(P.begin(), P.end(), 0);
+    std::stable_sort(P.begin(), P.end(), [&](int64_t a, int64_t b) { return S[a] < S[b]; });
+    int64_t nk = nkeep < 0 ? N : nkeep;
+    if (nk == 0) {
+    } else if (nk >= N && stol <= 0) {
+      std::fill(keep, keep + N, 1);
+    } else {
+      nk = std::min(nk, N);
+      int64_t l;               // cut: keep sorted indices l+1 .. N-1
+      bool all = false;
+      if (stol > 0) {
+        const int64_t lx = nkmin < N ? N - nkmin : 0;
+        int64_t j = N - 1;
+        for (; j >= 0; --j)
+          if (S[P[j]] <= stol && j < lx) break;
+        if (j < 0) {           // every value above stol (or protected by Nkmin)
+          if (N > nk) l = N - 1 - nk;
+          else all = true, l = -1;
+        } else {
+          l = (N - 1 - j > nk) ? N - 1 - nk : j;
+        }
+      } else {
+        l = N - 1 - nk;
+      }
+      if (all || l < 0) std::fill(keep, keep + N, 1);
+      else
+        for (int64_t i = l + 1; i < N; ++i) keep[P[i]] = 1;
+    }
+  }
+  double tot = 0, t2 = 0;
+  int64_t nkept = 0;
+  for (int64_t i = 0; i < N; ++i) {
+    tot += S[i] * S[i];
+    if (keep[i]) ++nkept; else t2 += S[i] * S[i];
+  }
+  if (nkeep_out) *nkeep_out = nkept;
+  if (s2t_out) *s2t_out = t2;
+  if (s2tot_out) *s2tot_out = tot;
+  if (sfac_out) *sfac_out = (t2 > 0 && t2 < tot) ? std::sqrt(tot / (tot - t2)) : 1.0;
+}
+
 // -------------------------------------------------------------- eig blocks
 void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, const int64_t *eoffs,
                 const double *H, double *E, double *U, bool cplx) {
@@ -747,6 +805,16 @@ qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double et
     if (dE) dev_free(c, dE);
     throw;
   }
+  QS_API_END
+}
+
+qs_status qs_svd_keep(int64_t nblk, const int64_t *k, const double *S, int64_t nkeep, int64_t nkmin, double stol,
+                      uint8_t *keep, int64_t *nkeep_out, double *s2t_out, double *s2tot_out, double *sfac_out) {
+  QS_API_BEGIN
+  if (nblk < 0 || (nblk > 0 && (!k || !S || !keep))) fail(QS_ERR_ARG, "null argument");
+  for (int64_t i = 0; i < nblk; ++i)
+    if (k[i] < 0) fail(QS_ERR_ARG, "negative singular value count");
+  svd_keep_host(nblk, k, S, nkeep, nkmin, stol, keep, nkeep_out, s2t_out, s2tot_out, sfac_out);
   QS_API_END
 }
 

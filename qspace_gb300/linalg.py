@@ -103,6 +103,23 @@ def eigQS(H: QSpace, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0, ct
     return Etot, parts
 
 
+def svd_keep(S_blocks: list, nkeep: int = -1, nkmin: int = 0, stol: float = 0.0):
+    """The truncation of svdQS on the host (qs_svd_keep): per-block keep
+    flags, kept count, discarded and total weight, and the rescale factor
+    sfac of the kept singular values."""
+    lib = _capi.load()
+    k = np.array([len(s) for s in S_blocks], np.int64)
+    S = np.concatenate([np.asarray(s, np.float64) for s in S_blocks]) if S_blocks else np.zeros(0)
+    keep = np.zeros(max(len(S), 1), np.uint8)
+    nk, s2t, tot, sfac = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
+    check(lib.qs_svd_keep(len(k), _ptr(k), S.ctypes.data_as(_capi.c_double_p), int(nkeep), int(nkmin), float(stol),
+                          keep.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(nk), C.byref(s2t), C.byref(tot),
+                          C.byref(sfac)))
+    offs = np.concatenate([[0], np.cumsum(k)]).astype(np.int64)
+    return ([keep[offs[i]:offs[i + 1]].astype(bool) for i in range(len(k))], nk.value, s2t.value, tot.value,
+            sfac.value)
+
+
 def svd_blocks(blocks: list, ctx: Context | None = None):
     """Thin SVD of real blocks on the GPU: returns lists U, S, Vt."""
     import torch
