@@ -569,7 +569,9 @@ def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float 
     (Source/gathered.cc:1822-2040) with eigQS's option handling
     (Source/eigQS.cc:55-100): deps > 0 averages near-degenerate levels and
     moves the cut to the largest weighted gap near Nkeep (b=-1, dmax=-1).
-    Returns (list of bool arrays, Nkeep)."""
+    Returns (list of bool arrays, number kept).  (The reference's NK output
+    is that number except with Etrunc > 0 and deps = 0, where markSet leaves
+    it at min(Nkeep, N): only its gap-search branch rewrites Nkeep.)"""
     sizes = [len(e) for e in E_blocks]
     E = np.concatenate([np.asarray(e, float) for e in E_blocks]) if E_blocks else np.zeros(0)
     N = len(E)

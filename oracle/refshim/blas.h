@@ -35,9 +35,9 @@ void scipy_zgeev_64_(FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P,
                      FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P);
 void scipy_dgetrf_64_(FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P);
 void scipy_dgetri_64_(FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P);
-}
 long long scipy_ilaenv_64_(FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P, FAKEMX_P,
                            unsigned long, unsigned long);
+}
 #define FAKEMX_PTR_STYLE(name)                                                 \
   template <class A, class... T>                                               \
   inline void name##_(A *a0, T *...r) {                                        \

@@ -187,6 +187,8 @@ __global__ void scale_kernel(double *__restrict__ v, int64_t n, const double *__
 // levels (relative to the spectral width) and moves the cut to the largest
 // weighted gap near Nkeep (b = -1, dmax = -1); otherwise the Nkeep lowest
 // levels are kept, or those below E_min + Etrunc when Etrunc > 0.
+// *nkeep_out is the number kept (the reference's NK output differs only with
+// Etrunc > 0 and deps = 0, where markSet leaves it at min(Nkeep, N)).
 void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nkeep_in, double etrunc,
                     double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
   int64_t N = 0;
