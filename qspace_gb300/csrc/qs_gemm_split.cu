@@ -570,6 +570,14 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Recombination without the FP64 pipe.  The S accumulators hold exact
@@ -591,9 +599,6 @@ __device__ __forceinline__ unsigned long long mad_wide(int a, int m, unsigned lo
 // word, 0 <= sh <= 30 adds acc * 2^sh to the low 64-bit word, sh < 0 adds
 // acc / 2^-sh rounded.  All words wrap; V itself fits in int64, so
 // V = hi * 2^32 + lo (mod 2^64) is exact.
-struct GroupWeight {
-  int mh, ml, rs;
-};
 
 // V * 2^scale: one int64 -> FP64 conversion (round to nearest even) and an
 // exponent add.  Integer-only assemblies (64-bit or 32-bit words, exactly
@@ -606,6 +611,38 @@ __device__ __forceinline__ double fixed_to_double(long long V, int scale) {
   const int e = (int)((bits >> 52) & 0x7ff) + scale;
   if (e <= 0 || e >= 2047) return ldexp(d, scale);
   return __longlong_as_double(bits + ((long long)scale << 52));
+}
+
+// Folds accumulator groups G0..G0+NG-1 of one set (this thread's TMEM lane,
+// 8 columns from cbase) into the fixed-point words: group g enters with shift
+// sh = b(S-1-g) - rsh, >= 32 into the high word Vh, 0..30 into the low word
+// Vl (the host keeps sh off 31), < 0 rounded down by -sh bits; exactly one
+// form applies to a group (uniform branch).
+template <int S, int G0, int NG>
+__device__ __forceinline__ void fold_groups(uint32_t set_base, int cbase, int b, int rsh,
+                                            unsigned long long (&Vl)[8], unsigned int (&Vh)[8]) {
+  float acc[NG][8];
+#pragma unroll
+  for (int g = 0; g < NG; ++g) tmem_ld8(set_base + (uint32_t)((G0 + g) * TNS + cbase), acc[g]);
+  tmem_wait_ld();
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    const int sh = b * (S - 1 - (G0 + g)) - rsh;
+    if (sh >= 32) {
+      const unsigned m = 1u << (sh - 32);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) Vh[c] += (unsigned int)__float2int_rn(acc[g][c]) * m;
+    } else if (sh >= 0) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) Vl[c] = mad_wide(__float2int_rn(acc[g][c]), 1 << sh, Vl[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int a = __float2int_rn(acc[g][c]);
+        Vl[c] = mad_wide((a + (1 << (-sh - 1))) >> -sh, 1, Vl[c]);
+      }
+    }
+  }
 }
 
 // Chunking rule shared by the host and the MMA issuer: a new chunk starts
@@ -735,8 +772,16 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
         int depth = 0;
         bool fresh = true;
         if (!acquire(u)) { ok = false; break; }
-        for (int p = T.p0; p < T.p1 && ok; ++p) {
-          const int KB = pairs[p].KB, Kr = pairs[p].Kr;
+        // the sizes of the next pair are loaded one pair ahead, so that the
+        // global-load latency stays off the issue path
+        const int p1 = T.p1;
+        int KBn = pairs[T.p0].KB, Krn = pairs[T.p0].Kr;
+        for (int p = T.p0; p < p1 && ok; ++p) {
+          const int KB = KBn, Kr = Krn;
+          if (p + 1 < p1) {
+            KBn = pairs[p + 1].KB;
+            Krn = pairs[p + 1].Kr;
+          }
           for (int kb = 0; kb < KB; ++kb, ++it) {
             const int dk = max(kblock_depth(Kr, kb), 0);
             if (!fresh && depth + dk > kchunk) {
@@ -792,6 +837,7 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
     // all quarters for CW consecutive columns of the tile.
     const int q = warp & 3;
     constexpr int CW = TNS * 4 / EPI_WARPS;
+    static_assert(CW == 8, "the drain reads 8 columns per thread and group");
     const int cbase = ((warp - 2) >> 2) * CW;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
     const int scale_b = -b * (S + 1);
@@ -815,21 +861,13 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       tw = (ti < ntiles && lane < TILE_WORDS) ? reinterpret_cast<const uint32_t *>(tiles + ti)[lane] : 0u;
       const int i_glob = T.mt * TMS + q * 32 + lane;
       const bool rv = i_glob < T.Mr;
-      // exponents of this thread's outputs, fetched now so that their load
-      // latency hides behind the accumulation
+      // the row exponent is fetched now so that its load latency hides behind
+      // the accumulation; the column exponents (broadcast loads) are read at
+      // the stores, which keeps the drain's registers below the 96 a thread
+      // of this launch has
       const int j0 = T.nt * TNS + cbase;
       const int Ei = rv ? E[T.eoff + i_glob] : 0;
-      int Fj[CW];
-#pragma unroll
-      for (int jj = 0; jj < CW; ++jj) Fj[jj] = (rv && j0 + jj < T.N) ? F[T.foff + j0 + jj] : 0;
-      GroupWeight gw[S];
-#pragma unroll
-      for (int g = 0; g < S; ++g) {
-        const int sh = b * (S - 1 - g) - T.rshift;
-        gw[g].mh = sh >= 32 ? (1 << (sh - 32)) : 0;
-        gw[g].ml = (sh >= 0 && sh <= 30) ? (1 << sh) : 0;
-        gw[g].rs = sh < 0 ? -sh : 0;
-      }
+      const int rsh = T.rshift;
       unsigned long long Vl[CW];
       unsigned int Vh[CW];
 #pragma unroll
@@ -845,31 +883,13 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
         if (!w) { ok = false; break; }
         tc_fence_after();
         const uint32_t set_base = lane_base + (uint32_t)((u & 1) * SET_COLS);
-#pragma unroll
-        for (int c4 = 0; c4 < CW; c4 += 4) {
-          float acc[S][4];
-#pragma unroll
-          for (int g = 0; g < S; ++g) tmem_ld4(set_base + (uint32_t)(g * TNS + cbase + c4), acc[g]);
-          tmem_wait_ld();
-#pragma unroll
-          for (int g = 0; g < S; ++g) {
-            const GroupWeight w = gw[g];
-            // exactly one of the three forms applies to a group (uniform branch)
-            if (w.mh != 0) {
-#pragma unroll
-              for (int cc = 0; cc < 4; ++cc)
-                Vh[c4 + cc] += (unsigned int)__float2int_rn(acc[g][cc]) * (unsigned int)w.mh;
-            } else if (w.rs == 0) {
-#pragma unroll
-              for (int cc = 0; cc < 4; ++cc) Vl[c4 + cc] = mad_wide(__float2int_rn(acc[g][cc]), w.ml, Vl[c4 + cc]);
-            } else {
-#pragma unroll
-              for (int cc = 0; cc < 4; ++cc) {
-                const int a = __float2int_rn(acc[g][cc]);
-                Vl[c4 + cc] = mad_wide((a + (1 << (w.rs - 1))) >> w.rs, 1, Vl[c4 + cc]);
-              }
-            }
-          }
+        // the groups' columns are in flight together (one wait per batch of up
+        // to six): the drain is bound by TMEM load latency otherwise
+        if constexpr (S <= 6) {
+          fold_groups<S, 0, S>(set_base, cbase, b, rsh, Vl, Vh);
+        } else {
+          fold_groups<S, 0, 4>(set_base, cbase, b, rsh, Vl, Vh);
+          fold_groups<S, 4, S - 4>(set_base, cbase, b, rsh, Vl, Vh);
         }
         tc_fence_before();
         __syncwarp();
@@ -883,7 +903,7 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
           const int j = j0 + jj;
           if (j < T.N) {
             const long long V = (long long)(((unsigned long long)Vh[jj] << 32) + Vl[jj]);
-            crow[(int64_t)j * T.ldc] = fixed_to_double(V, Ei + Fj[jj] + T.rshift + scale_b);
+            crow[(int64_t)j * T.ldc] = fixed_to_double(V, Ei + F[T.foff + j] + rsh + scale_b);
           }
         }
       }

@@ -248,11 +248,15 @@ static void grouped_host(Ctx *c, const qs_pair_list *pl, const double *A, int64_
   SplitResult sr;
   try {
     c->ensure_copy_streams();
-    QS_CUDA(cudaMemsetAsync(dC, 0, (size_t)c_elems * eb, c->stream));
-    cudaEvent_t ready = event();  // allocations and the zero fill are done
+    // the copies in wait only for the allocations; the zero fill of C runs
+    // meanwhile on the context stream, ahead of every product
+    cudaEvent_t ready = event();
     QS_CUDA(cudaEventRecord(ready, c->stream));
     QS_CUDA(cudaStreamWaitEvent(c->h2d, ready, 0));
-    QS_CUDA(cudaStreamWaitEvent(c->d2h, ready, 0));
+    QS_CUDA(cudaMemsetAsync(dC, 0, (size_t)c_elems * eb, c->stream));
+    cudaEvent_t filled = event();
+    QS_CUDA(cudaEventRecord(filled, c->stream));
+    QS_CUDA(cudaStreamWaitEvent(c->d2h, filled, 0));
     // all copies in are queued first: the copy stream never waits for the
     // host to plan a chunk
     int64_t wa = 0, wb = 0, wc = 0;
