@@ -319,6 +319,36 @@ QS_EXPORT qs_status qs_grouped_gemm_split_static(qs_ctx *ctx, const qs_pair_list
                                                  const double *A, const double *B, double *C,
                                                  const qs_opts *opts, qs_stats *stats);
 
+/* ------------------------------------------- device CG / X-symbol factors
+ * The reference looks every block pair's X-symbol up in a host hash map
+ * (X3Map gXS, Source/clebsch.hh:3911-4245), filled on first use by
+ * X3Map::contractCGR (Source/clebsch_aux.cc:4073-4330) and consulted inside
+ * the pair loop (Source/QSpace_aux.cc:27-355).  A qs_xcache is that store on
+ * the device: the caller derives a 128-bit key (two uint64 words) from the
+ * (CGT_a, ica, CGT_b, icb) tuple of a factor, puts the factors once, and the
+ * keyed grouped product resolves every pair's factor on the device, so
+ * repeated contractions pass keys only.  The key (2^64-1, 2^64-1) is
+ * reserved.  A table holds up to `capacity` entries; a put beyond that is
+ * refused with QS_ERR_OOM and leaves the table unchanged.  Puts synchronise
+ * with the context's stream (they belong to warm-up). */
+typedef struct qs_xcache qs_xcache;
+QS_EXPORT qs_status qs_xcache_create(qs_ctx *ctx, int64_t capacity, qs_xcache **out);
+QS_EXPORT void qs_xcache_destroy(qs_xcache *cache);
+/* Inserts or overwrites n factors; keys holds 2n words. */
+QS_EXPORT qs_status qs_xcache_put(qs_xcache *cache, int64_t n, const uint64_t *keys, const double *vals);
+/* Looks n keys up on the device (host arrays in and out); found[i] = 0
+ * marks a missing key, whose vals[i] is 0. */
+QS_EXPORT qs_status qs_xcache_get(qs_xcache *cache, int64_t n, const uint64_t *keys, double *vals,
+                                  int32_t *found);
+QS_EXPORT qs_status qs_xcache_count(const qs_xcache *cache, int64_t *n);
+/* qs_grouped_gemm with the factor of pair p looked up under the key
+ * fkeys[2p], fkeys[2p+1] (host array); pairs->afac is ignored and may be
+ * NULL.  The call waits for its products.  A key missing from the table
+ * fails it with QS_ERR_ARG; the products of that pair then used factor 0. */
+QS_EXPORT qs_status qs_grouped_gemm_keyed(qs_ctx *ctx, const qs_pair_list *pairs, const uint64_t *fkeys,
+                                          const qs_xcache *cache, const double *A, const double *B,
+                                          double *C, const qs_opts *opts, qs_stats *stats);
+
 /* ------------------------------------------------------- eigQS blocks
  * Hermitian eigendecomposition of every symmetry block on the device in FP64
  * (the OpenMP loop of QSpace::EigenSymmetric, Source/QSpace.cc:4789-4811,

@@ -127,6 +127,13 @@ SIGNATURES = {
     "qs_grouped_plan_destroy": (None, [C.c_void_p]),
     "qs_grouped_gemm_split_static": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
+    "qs_xcache_create": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
+    "qs_xcache_destroy": (None, [C.c_void_p]),
+    "qs_xcache_put": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "qs_xcache_get": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qs_xcache_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "qs_grouped_gemm_keyed": (C.c_int, [C.c_void_p, C.POINTER(PairList), C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.POINTER(Opts), C.POINTER(Stats)]),
     "qs_grouped_gemm_host": (C.c_int, [C.c_void_p, C.POINTER(PairList), c_double_p, C.c_int64,
                                        c_double_p, C.c_int64, c_double_p, C.c_int64,
                                        C.POINTER(Opts), C.POINTER(Stats)]),

@@ -9,6 +9,7 @@
 #include <numeric>
 
 #include "qs_internal.h"
+#include "qs_xcache.h"
 #include "qs_objects.h"
 #include "qs_plan.h"
 #include "qs_split.h"
@@ -689,6 +690,7 @@ qs_status qs_ctx_create(int device, qs_ctx **out) {
 void qs_ctx_destroy(qs_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->c.device);
+  xcache_orphan_all(&ctx->c);
   if (ctx->c.scratch) cudaFreeAsync(ctx->c.scratch, ctx->c.stream);
   destroy_solver(&ctx->c);
   cudaStreamSynchronize(ctx->c.stream);

@@ -56,6 +56,7 @@
 
 #include "qs_internal.h"
 #include "qs_split.h"
+#include "qs_xcache.h"
 
 namespace qs {
 
@@ -971,6 +972,25 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d
 
 }  // namespace
 
+namespace {
+// A pair's CG factor from the device table, folded like the host does for a
+// given factor (make_factor, frexp exponent); a missing key gives factor 0
+// and raises the source's flag.
+__global__ void resolve_split_factors_kernel(SplitPair *__restrict__ sp, int64_t n, FactorSource fs) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double x = 0.0;
+    if (!xview_find(fs.tab, fs.keys[2 * i], fs.keys[2 * i + 1], &x)) atomicExch(fs.missing, 1);
+    const Factor f = make_factor(x);
+    sp[i].fm = f.fm;
+    sp[i].fe = f.fe;
+    sp[i].fneg = f.neg ? 1 : 0;
+    int e = 0;
+    if (x != 1.0 && x != 0.0) frexp(x, &e);
+    sp[i].e_afac = e;
+  }
+}
+}  // namespace
+
 // ---------------------------------------------------------------- host side
 // Largest summed (real) depth that keeps every accumulator group exact:
 // |sum_{t+u=g} d_t d'_u| <= 2^(2b) (1 + max(0, g-1)/4) per term.
@@ -1303,7 +1323,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
                       const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                       const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                       bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
-                      int forced_bits) {
+                      int forced_bits, const FactorSource *fs) {
   SplitWork w;
   SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w, forced_bits);
   if (w.tiles.empty()) return res;
@@ -1319,6 +1339,12 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   d.tiles = dev_upload(ctx, w.tiles);
   d.E = dev_alloc<int>(ctx, (size_t)w.nE);
   d.F = dev_alloc<int>(ctx, (size_t)w.nF);
+  if (fs && !w.sp.empty()) {
+    const int64_t n = (int64_t)w.sp.size();
+    resolve_split_factors_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+        d.pairs, n, *fs);
+    QS_LAUNCHED(ctx);
+  }
   launch_split(ctx, w, cplx, d, A, B, C, ctx->d_err);
   dev_free(ctx, d.pairs);
   dev_free(ctx, d.rt);

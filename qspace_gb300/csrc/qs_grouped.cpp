@@ -12,13 +12,7 @@
 #include "qs_plan.h"
 #include "qs_split.h"
 #include "qs_grouped.h"
-
-namespace qs {
-void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
-                 const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
-                 int64_t c_elems, uint8_t *static_scratch = nullptr, size_t static_cap = 0,
-                 int *static_err = nullptr);
-}
+#include "qs_xcache.h"
 
 using namespace qs;
 
@@ -105,8 +99,17 @@ GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elem
 // that scratch instead of allocating.
 static void grouped_exec(Ctx *ctx, const GroupedPlan &g, size_t b0, size_t b1, const double *A,
                          const double *B, double *C, const qs_opts *opts, SplitResult *sr_out,
-                         uint8_t *static_scratch, size_t static_cap, int *static_err) {
+                         uint8_t *static_scratch, size_t static_cap, int *static_err,
+                         const FactorSource *fs_all = nullptr) {
   if (b1 <= b0) return;
+  // the keys of this range's pairs
+  FactorSource fs_sub{};
+  const FactorSource *fs = nullptr;
+  if (fs_all) {
+    fs_sub = *fs_all;
+    fs_sub.keys += 2 * g.grp[b0];
+    fs = &fs_sub;
+  }
   const bool whole = b0 == 0 && b1 == g.bM.size();
   std::vector<PairDesc> sub_pairs;
   std::vector<int64_t> sub_grp, sub_coff;
@@ -129,10 +132,11 @@ static void grouped_exec(Ctx *ctx, const GroupedPlan &g, size_t b0, size_t b1, c
   if (prec == QS_PREC_SPLIT) {
     const int ns = opts ? opts->nslices : 0;
     const double tol = opts && opts->tol > 0 ? opts->tol : 1e-12;
+    if (static_scratch && fs) fail(QS_ERR_ARG, "the static-scratch entry point takes its factors from the pair list");
     SplitResult sr = static_scratch
                          ? run_split_static(ctx, pairs, grp, bM, bN, coff, A, B, C, g.cplx, ns, tol, &bldc,
                                             static_scratch, static_cap, static_err)
-                         : run_split(ctx, pairs, grp, bM, bN, coff, A, B, C, g.cplx, ns, tol, &bldc);
+                         : run_split(ctx, pairs, grp, bM, bN, coff, A, B, C, g.cplx, ns, tol, &bldc, 0, fs);
     if (sr_out && sr.err_bound >= sr_out->err_bound) *sr_out = sr;
   } else if (static_scratch) {
     fail(QS_ERR_ARG, "the static-scratch entry point runs the split path only");
@@ -140,6 +144,7 @@ static void grouped_exec(Ctx *ctx, const GroupedPlan &g, size_t b0, size_t b1, c
     std::vector<TileDesc> tiles = make_tiles(grp, bM, bN, coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &bldc);
     PairDesc *dp = dev_upload(ctx, pairs);
     TileDesc *dt = dev_upload(ctx, tiles);
+    if (fs) launch_resolve_pairdesc(ctx, dp, (int64_t)pairs.size(), *fs);
     launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), A, B, C, g.cplx ? 1 : 0);
     dev_free(ctx, dp);
     dev_free(ctx, dt);
@@ -165,13 +170,14 @@ static void fill_stats(qs_stats *stats, const GroupedPlan &g, const SplitResult 
 // of it.
 void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
                  const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
-                 int64_t c_elems, uint8_t *static_scratch, size_t static_cap, int *static_err) {
+                 int64_t c_elems, uint8_t *static_scratch, size_t static_cap, int *static_err,
+                 const FactorSource *fs) {
   if (stats) std::memset(stats, 0, sizeof *stats);
   GroupedPlan g = grouped_plan(pl, a_elems, b_elems, c_elems);
   if (g.pairs.empty()) return;
   const int64_t launches0 = ctx->launches;
   SplitResult sr;
-  grouped_exec(ctx, g, 0, g.bM.size(), A, B, C, opts, &sr, static_scratch, static_cap, static_err);
+  grouped_exec(ctx, g, 0, g.bM.size(), A, B, C, opts, &sr, static_scratch, static_cap, static_err, fs);
   fill_stats(stats, g, sr, ctx->launches - launches0);
 }
 

@@ -25,4 +25,13 @@ struct GroupedPlan {
 // access is checked against them.
 GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elems, int64_t c_elems);
 
+struct FactorSource;
+// Validates the pair list, then launches the FP64 or the split path on all of
+// it.  With `fs` every pair's factor is looked up on the device (the pair
+// list's afac is ignored).
+void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
+                 const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
+                 int64_t c_elems, uint8_t *static_scratch = nullptr, size_t static_cap = 0,
+                 int *static_err = nullptr, const FactorSource *fs = nullptr);
+
 }  // namespace qs

@@ -47,6 +47,9 @@ void set_last_error(const std::string &msg);
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // factor tables made on this context: their device memory is released
+  // with the context, so a table destroyed later touches no freed context
+  std::vector<qs_xcache *> tables;
   int num_sms = 0;
   int64_t launches = 0;
   // device error word for bounded waits inside kernels (0 = ok)

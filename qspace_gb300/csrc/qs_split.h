@@ -31,12 +31,16 @@ DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vecto
                             const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
                             double tol, int forced_slices, int forced_bits = 0);
 
+struct FactorSource;
+// With `fs` every pair's CG factor is looked up on the device before it is
+// folded into the digits (the pairs' afac is ignored).
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs,
                       const std::vector<int64_t> &grp, const std::vector<int32_t> &blk_M,
                       const std::vector<int32_t> &blk_N, const std::vector<int64_t> &c_off,
                       const double *A, const double *B, double *C, bool cplx,
                       int forced_slices, double tol,
-                      const std::vector<int32_t> *blk_ldc = nullptr, int forced_bits = 0);
+                      const std::vector<int32_t> *blk_ldc = nullptr, int forced_bits = 0,
+                      const FactorSource *fs = nullptr);
 
 // The same product with every device buffer carved from caller-provided
 // scratch (`cap` bytes, 256-byte aligned) instead of allocated; the bounded

@@ -4,13 +4,8 @@
 // lives in one file-scope array per device and process; nothing is allocated.
 #include <mutex>
 
+#include "qs_grouped.h"
 #include "qs_internal.h"
-
-namespace qs {
-void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
-                 const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
-                 int64_t c_elems, uint8_t *static_scratch, size_t static_cap, int *static_err);
-}
 
 using namespace qs;
 

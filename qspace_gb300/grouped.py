@@ -162,6 +162,22 @@ class DeviceBatch:
         if stats is not None:
             stats.update(st.as_dict())
 
+    def run_keyed(self, fkeys: np.ndarray, table: "FactorTable", prec="fp64", nslices=0, tol=1e-12,
+                  stats: dict | None = None):
+        """The batch with pair p's factor looked up on the device under the
+        128-bit key fkeys[p] (uint64 array of shape (npairs, 2))."""
+        k = np.ascontiguousarray(fkeys, dtype=np.uint64).reshape(-1, 2)
+        if len(k) != self.pl.npairs:
+            raise ValueError("one key per pair")
+        o = make_opts(prec, nslices, tol)
+        st = Stats()
+        check(self.ctx.lib.qs_grouped_gemm_keyed(self.ctx.h, C.byref(self.pl), k.ctypes.data_as(C.c_void_p),
+                                                 table.h, C.c_void_p(self.dA.data_ptr()),
+                                                 C.c_void_p(self.dB.data_ptr()), C.c_void_p(self.dC.data_ptr()),
+                                                 C.byref(o), C.byref(st)))
+        if stats is not None:
+            stats.update(st.as_dict())
+
     def plan(self, prec="split", nslices=0, tol=1e-12, autotune=False, graph=True) -> "GroupedPlan":
         return GroupedPlan(self.pk, prec, nslices, tol, autotune, graph, self.ctx)
 
@@ -213,3 +229,52 @@ def run_device(w: dict, prec="fp64", nslices=0, tol=1e-12, ctx=None, stats=None)
     db = DeviceBatch(pk, ctx)
     db.run(prec, nslices, tol, stats)
     return db.result()
+
+
+class FactorTable:
+    """Device-resident CG / X-symbol factors keyed by 128-bit keys
+    (qs_xcache_*): the device form of the reference's X-symbol store (X3Map,
+    Source/clebsch.hh:3911-4245).  Keys are uint64 arrays of shape (n, 2)."""
+
+    def __init__(self, capacity: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        check(self.ctx.lib.qs_xcache_create(self.ctx.h, int(capacity), C.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def _keys(keys) -> np.ndarray:
+        return np.ascontiguousarray(keys, dtype=np.uint64).reshape(-1, 2)
+
+    def put(self, keys, vals):
+        k = self._keys(keys)
+        v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+        if len(v) != len(k):
+            raise ValueError("one value per key")
+        check(self.ctx.lib.qs_xcache_put(self.h, len(k), k.ctypes.data_as(C.c_void_p),
+                                         v.ctypes.data_as(C.c_void_p)))
+
+    def get(self, keys):
+        """(values, found) looked up on the device."""
+        k = self._keys(keys)
+        v = np.zeros(len(k), np.float64)
+        f = np.zeros(len(k), np.int32)
+        check(self.ctx.lib.qs_xcache_get(self.h, len(k), k.ctypes.data_as(C.c_void_p),
+                                         v.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p)))
+        return v, f.astype(bool)
+
+    def __len__(self) -> int:
+        n = C.c_int64()
+        check(self.ctx.lib.qs_xcache_count(self.h, C.byref(n)))
+        return int(n.value)
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.qs_xcache_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
