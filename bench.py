@@ -158,22 +158,30 @@ GEMM_DRAM_WRITE_PER_OUTPUT_BYTE = 177.814784e6 / 231684512
 
 def split_arena_bytes(pk, S: int) -> float:
     """Bytes of the BF16 digit arena of the batch: 128 x 32 A tiles and 32 x 32
-    B tiles of the real form (2M x 2K and 2K x N per complex pair), S digits,
-    after the planner's choice of orientation per output block (a block is
-    computed as C^T when that is estimated 3 % cheaper; the estimate weighs
-    output tiles against digit bytes, as in the library).  One pair per output
-    block, as in this workload."""
+    B tiles of the real form (2M x 2K and 2K x N per complex pair with A
+    duplicated, M x 2K and 2K x 2N with B duplicated), S digits, after the
+    planner's choice of layout per output block (plain, C^T, and for complex
+    data which operand is duplicated; another layout than the plain one when
+    it is estimated 3 % cheaper; the estimate weighs output tiles against
+    digit bytes, as in the library).  One pair per output block, as in this
+    workload."""
     import numpy as np
     cm = 2 if pk.cplx else 1
     M, N, K = (x.astype(np.int64) for x in (pk.M, pk.N, pk.K))
 
-    def cost(m, n):
-        mt, nt = (cm * m + 127) // 128, (n + 31) // 32
+    def cost(rows, cols):
+        mt, nt = (rows + 127) // 128, (cols + 31) // 32
         return 26900.0 * mt * nt + 49152.0 * mt + 10530.0 * nt
 
-    swap = cost(N, M) < 0.97 * cost(M, N)
-    Ma, Nb = np.where(swap, N, M), np.where(swap, M, N)
-    MT, NT = (cm * Ma + 127) // 128, (Nb + 31) // 32
+    # layouts: (A-role real rows, B-role real columns) -- A duplicated, plain
+    # or transposed, and for complex data B duplicated, plain or transposed
+    lay = [(cm * M, N), (cm * N, M)] + ([(M, 2 * N), (N, 2 * M)] if cm == 2 else [])
+    c = np.stack([cost(r, k) for r, k in lay])
+    best = np.argmin(c, axis=0)
+    best = np.where(c[best, np.arange(len(M))] < 0.97 * c[0], best, 0)
+    rows = np.choose(best, [r for r, _ in lay])
+    cols = np.choose(best, [k for _, k in lay])
+    MT, NT = (rows + 127) // 128, (cols + 31) // 32
     KB = np.maximum(1, (cm * K + 31) // 32)
     return float(np.sum(MT * KB * S * 8192 + NT * KB * S * 2048))
 

@@ -93,6 +93,13 @@ struct SplitPair {
   int32_t fe, fneg;        // CG factor folded into A's digits: fm 2^fe, sign
   uint64_t fm;             // (fm = 0: factor 1)
   int32_t swap;            // block computed as C^T = op(B)^T op(A)^T: the A role reads the B arena
+  // Real form of a complex block.  dupb = 0: A~ (2M x 2K) rows 2m, 2m+1 =
+  // (Re, -Im), (Im, Re) of row m of op(A), B~ (2K x N) rows 2k, 2k+1 = (Re, Im)
+  // of op(B), C~ (2M x N) rows = (Re, Im) of C.  dupb = 1: A' (M x 2K) columns
+  // 2k, 2k+1 = (Re, Im) of op(A), B' (2K x 2N) columns 2n = (Re; -Im) and
+  // 2n+1 = (Im; Re) of column n of op(B), C' (M x 2N) columns = (Re, Im) of C.
+  int32_t dupb;
+  int32_t Nr;              // real columns of op(B~)
   int32_t pad_;
 };
 
@@ -105,9 +112,12 @@ struct SplitTile {
   int32_t nchunk;          // drains of the accumulators
   int32_t rshift;          // bits dropped below the lowest group (int64 headroom)
   // output address of tile row r, column j (doubles from c_off):
-  // (r >> rsplit) * rs + (r & rsplit) + j * ldc; rsplit = 1 for a complex
-  // block computed transposed (its rows interleave Re/Im of C's columns)
-  int32_t rs, rsplit;
+  // (r >> rsplit) * rs + (r & rsplit) + (j >> csplit) * ldc + (j & csplit),
+  // splits = rsplit | csplit << 1; rsplit = 1 for a complex block computed
+  // transposed in the A-duplicated form (its rows interleave Re/Im of C's
+  // columns), csplit = 1 for one in the B-duplicated form, not transposed
+  // (its columns interleave Re/Im of C's columns)
+  int32_t rs, splits;
 };
 constexpr int TILE_WORDS = (int)(sizeof(SplitTile) / 4);
 static_assert(sizeof(SplitTile) % 8 == 0 && TILE_WORDS <= 16, "tile descriptor fits one 64-byte slot");
@@ -206,6 +216,24 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 }
 
 // --------------------------------------------------------- exponent passes
+// Records the exponent key of one line (row m of op(A) or column m of op(B),
+// max over Re and Im for complex data) for every real line it becomes: rows
+// 2m, 2m+1 of A~ (A-duplicated form) or columns 2m, 2m+1 of B' (B-duplicated
+// form), else the one line m.  Row exponents include the CG factor's.
+template <bool CPLX>
+__device__ __forceinline__ void put_line_exp(const SplitPair &P, bool role_b, int m, int key, int *__restrict__ E,
+                                             int *__restrict__ F) {
+  const bool two = CPLX && (role_b ? P.dupb != 0 : P.dupb == 0);
+  int *dst = role_b ? F + P.foff : E + P.eoff;
+  const int e = key - 1022 + (role_b ? 0 : P.e_afac);
+  if (two) {
+    atomicMax(&dst[2 * m], e);
+    atomicMax(&dst[2 * m + 1], e);
+  } else {
+    atomicMax(&dst[m], e);
+  }
+}
+
 // Exponents of lines strided along k: rows of a plain op(A~) (ROLE_B =
 // false) or columns of a transposed op(B~) (ROLE_B = true); per output
 // block, max over its pairs.  A block of 256 threads covers lines
@@ -264,17 +292,7 @@ exp_lines_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ t
     for (int p = 1; p < KS; ++p) key = max(key, keys[p * R + r]);
   }
   if (r >= rows || !key) return;
-  if (ROLE_B) {
-    atomicMax(&F[P.foff + m], key - 1022);
-    return;
-  }
-  const int e = key - 1022 + P.e_afac;
-  if (CPLX) {
-    atomicMax(&E[P.eoff + 2 * m], e);
-    atomicMax(&E[P.eoff + 2 * m + 1], e);
-  } else {
-    atomicMax(&E[P.eoff + m], e);
-  }
+  put_line_exp<CPLX>(P, ROLE_B, m, key, E, F);
 }
 
 // Same maxima for lines stored contiguously along k (rows of a transposed
@@ -305,17 +323,7 @@ exp_contig_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ 
   }
   key = __reduce_max_sync(0xffffffffu, key);
   if (lane != 0 || !key) return;
-  if (rowsA) {
-    const int e = key - 1022 + P.e_afac;
-    if (CPLX) {
-      atomicMax(&E[P.eoff + 2 * line], e);
-      atomicMax(&E[P.eoff + 2 * line + 1], e);
-    } else {
-      atomicMax(&E[P.eoff + line], e);
-    }
-  } else {
-    atomicMax(&F[P.foff + line], key - 1022);
-  }
+  put_line_exp<CPLX>(P, !rowsA, line, key, E, F);
 }
 
 __global__ void fill_int_kernel(int *p, int64_t n, int v) {
@@ -333,6 +341,38 @@ __device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb,
   const bool ta = P.trans & 1, ca = P.trans & 4;
   const Factor Fa{P.fm, P.fe, P.fneg != 0};
   if constexpr (CPLX) {
+    if (P.dupb) {
+      // B-duplicated form: real row m of A' holds (Re, Im) of row m of op(A)
+      // along k; one task = one row x 4 complex k
+      for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
+        const int r = w % TMS, q = w / TMS;
+        const int m = mt * TMS + r;
+        if (m >= P.M) continue;  // feeds discarded outputs only: not written
+        const int Ei = E[P.eoff + m];
+        uint32_t pk[S][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k = (kb * TKS + q * 8) / 2 + j;
+          double re = 0.0, im = 0.0;
+          if (k < P.K) {
+            const double2 a = reinterpret_cast<const double2 *>(A)[
+                P.a_off + (ta ? (int64_t)k + (int64_t)m * P.lda : (int64_t)m + (int64_t)k * P.lda)];
+            re = a.x;
+            im = ca ? -a.y : a.y;
+          }
+          float dr[S], di[S];
+          digits_f<S, B>(scaled_int(re, Ei, B * S, Fa), dr);
+          digits_f<S, B>(scaled_int(im, Ei, B * S, Fa), di);
+#pragma unroll
+          for (int t = 0; t < S; ++t) pk[t][j] = pack2(dr[t], di[t]);
+        }
+        uint8_t *dst = tile + ((r >> 3) * KCM + q) * 128 + (r & 7) * 16;
+#pragma unroll
+        for (int t = 0; t < S; ++t)
+          *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+      }
+      return;
+    }
     // one task = one complex row m (real rows 2m, 2m+1 of A~) x 4 complex k:
     // the digits of re and im are cut once and placed as
     //   row 2m:   ( re, -im )    row 2m+1: ( im, re )
@@ -425,6 +465,42 @@ template <bool CPLX, int S, int B>
 __device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb, const double *__restrict__ Bm,
                                              const int *__restrict__ F, uint8_t *__restrict__ tile) {
   const bool tb = P.trans & 2, cb = P.trans & 8;
+  if constexpr (CPLX) {
+    if (P.dupb) {
+      // B-duplicated form: real column n of B' is (Re; -Im) (n even) or
+      // (Im; Re) (n odd) of complex column n / 2 of op(B)
+      for (int w = threadIdx.x; w < TNS * (TKS / 8); w += blockDim.x) {
+        const int c = w % TNS, q = w / TNS;
+        const int n = nt * TNS + c;
+        if (n >= P.Nr) continue;  // feeds discarded outputs only: not written
+        const int nc = n >> 1;
+        const bool odd = n & 1;
+        const int Fj = F[P.foff + n];
+        uint32_t pk[S][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k = (kb * TKS + q * 8) / 2 + j;
+          double re = 0.0, im = 0.0;
+          if (k < P.K) {
+            const double2 x = reinterpret_cast<const double2 *>(Bm)[
+                P.b_off + (tb ? (int64_t)nc + (int64_t)k * P.ldb : (int64_t)k + (int64_t)nc * P.ldb)];
+            re = x.x;
+            im = cb ? -x.y : x.y;
+          }
+          float dr[S], di[S];
+          digits_f<S, B>(scaled_int(re, Fj, B * S, Factor{0ull, 0, false}), dr);
+          digits_f<S, B>(scaled_int(im, Fj, B * S, Factor{0ull, 0, false}), di);
+#pragma unroll
+          for (int t = 0; t < S; ++t) pk[t][j] = odd ? pack2(di[t], dr[t]) : pack2(dr[t], -di[t]);
+        }
+        uint8_t *dst = tile + ((c >> 3) * KCM + q) * 128 + (c & 7) * 16;
+#pragma unroll
+        for (int t = 0; t < S; ++t)
+          *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+      }
+      return;
+    }
+  }
   for (int w = threadIdx.x; w < TNS * (TKS / 8); w += blockDim.x) {
     const int c = w % TNS, q = w / TNS;
     const int n = nt * TNS + c;
@@ -898,13 +974,15 @@ gemm_split_kernel(const SplitTile *__restrict__ tiles, int ntiles, const SplitPa
       }
       if (!ok) break;
       if (rv) {
-        double *crow = C + T.c_off + (int64_t)(i_glob >> T.rsplit) * T.rs + (i_glob & T.rsplit);
+        const int rsplit = T.splits & 1, csplit = T.splits >> 1;
+        double *crow = C + T.c_off + (int64_t)(i_glob >> rsplit) * T.rs + (i_glob & rsplit);
 #pragma unroll
         for (int jj = 0; jj < CW; ++jj) {
           const int j = j0 + jj;
           if (j < T.N) {
             const long long V = (long long)(((unsigned long long)Vh[jj] << 32) + Vl[jj]);
-            crow[(int64_t)j * T.ldc] = fixed_to_double(V, Ei + F[T.foff + j] + rsh + scale_b);
+            crow[(int64_t)(j >> csplit) * T.ldc + (j & csplit)] =
+                fixed_to_double(V, Ei + F[T.foff + j] + rsh + scale_b);
           }
         }
       }
@@ -1101,34 +1179,50 @@ struct SplitDev {
 // Host half of the split path: digit plan, per-pair digit geometry and arena
 // offsets, and the device work lists (exponent lines, slicing tiles, output
 // tiles in launch order).
-// Orientation of each output block: computed as C^T = op(B)^T op(A)^T when
-// that is estimated at least 3 % cheaper.  The estimate per k-block of the
-// block's pairs, in bytes of slicing traffic: 26900 per 128 x 32 output tile
-// (GEMM), plus the digit bytes the slicing writes for the A role (128-row
-// tiles of the 2x2 real form, 48 KB at six digits) and for the B role
+// Layout of each output block: computed as C or as C^T = op(B)^T op(A)^T,
+// and for complex blocks with the real form duplicating A (A~ is 2M x 2K) or
+// B (B' is 2K x 2N; see SplitPair), whichever is estimated cheapest (a layout
+// other than the plain one must be at least 3 % cheaper).  The estimate per
+// k-block of the block's pairs, in bytes of slicing traffic: 26900 per
+// 128 x 32 output tile (GEMM), plus the digit bytes the slicing writes for
+// the A role (128-row tiles, 48 KB at six digits) and for the B role
 // (32-column tiles, 12 KB, weighted 0.86) -- fitted to GB300 timings of the
-// split GEMM (5.65 ns per tile and k-block) and of the slicing kernels (0.21 and
-// 0.18 ps per byte).  Turning a wide block gives the 128-row tiles the larger
-// side but also the duplicated real form to the larger operand.  A swapped
-// pair exchanges the roles and storage of its operands: A' = op(B)^T reads
-// B's storage (transposed unless op(B) was), B' = op(A)^T reads A's, with the
-// conjugation flags exchanged; the tiles store C^T transposed.
+// split GEMM (5.65 ns per tile and k-block) and of the slicing kernels (0.21
+// and 0.18 ps per byte).  A swapped pair exchanges the roles and storage of
+// its operands: A' = op(B)^T reads B's storage (transposed unless op(B) was),
+// B' = op(A)^T reads A's, with the conjugation flags exchanged; the tiles
+// store C^T transposed.  Returns per block bit 0 = swapped, bit 1 = B
+// duplicated.
 static std::vector<uint8_t> orient_blocks(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                                           std::vector<int32_t> &bM, std::vector<int32_t> &bN, int cm,
                                           std::vector<PairDesc> &tp) {
   const int64_t nb = (int64_t)bM.size();
-  std::vector<uint8_t> swp(nb, 0);
+  std::vector<uint8_t> mode(nb, 0);
   bool any = false;
-  auto cost = [&](int64_t m, int64_t n) {
-    const double mt = double((m * cm + TMS - 1) / TMS), nt = double((n + TNS - 1) / TNS);
+  // rows of the A role and columns of the B role, real form
+  auto cost = [&](int64_t rows, int64_t cols) {
+    const double mt = double((rows + TMS - 1) / TMS), nt = double((cols + TNS - 1) / TNS);
     return 26900.0 * mt * nt + 49152.0 * mt + 10530.0 * nt;
   };
-  for (int64_t g = 0; g < nb; ++g)
-    if (cost(bN[g], bM[g]) < 0.97 * cost(bM[g], bN[g])) swp[g] = 1, any = true;
-  if (!any) return swp;
+  for (int64_t g = 0; g < nb; ++g) {
+    const int64_t m = bM[g], n = bN[g];
+    double c[4] = {cost(m * cm, n), cost(n * cm, m), 1e300, 1e300};
+    if (cm == 2) {
+      c[2] = cost(m, 2 * n);
+      c[3] = cost(n, 2 * m);
+    }
+    int best = 0;
+    for (int o = 1; o < 4; ++o)
+      if (c[o] < c[best]) best = o;
+    if (c[best] >= 0.97 * c[0]) best = 0;
+    // bit 0: swapped (layouts 1 and 3), bit 1: B duplicated (layouts 2 and 3)
+    mode[g] = (uint8_t)(((best & 1) ? 1 : 0) | (best >= 2 ? 2 : 0));
+    if (mode[g] & 1) any = true;
+  }
+  if (!any) return mode;
   tp = pairs;
   for (int64_t g = 0; g < nb; ++g) {
-    if (!swp[g]) continue;
+    if (!(mode[g] & 1)) continue;
     std::swap(bM[g], bN[g]);
     for (int64_t p = grp[g]; p < grp[g + 1]; ++p) {
       PairDesc &d = tp[p];
@@ -1139,7 +1233,7 @@ static std::vector<uint8_t> orient_blocks(const std::vector<PairDesc> &pairs, co
       d.trans = ((t & 2) ? 0 : 1) | ((t & 1) ? 0 : 2) | ((t & 8) ? 4 : 0) | ((t & 4) ? 8 : 0);
     }
   }
-  return swp;
+  return mode;
 }
 
 static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::vector<int64_t> &grp,
@@ -1151,7 +1245,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
   const int cm = cplx ? 2 : 1;
   std::vector<int32_t> blk_M = blk_M_in, blk_N = blk_N_in;
   std::vector<PairDesc> swapped_pairs;
-  const std::vector<uint8_t> swp = orient_blocks(pairs_in, grp, blk_M, blk_N, cm, swapped_pairs);
+  const std::vector<uint8_t> mode = orient_blocks(pairs_in, grp, blk_M, blk_N, cm, swapped_pairs);
   const std::vector<PairDesc> &pairs = swapped_pairs.empty() ? pairs_in : swapped_pairs;
   DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices, forced_bits);
   const int S = dp.nslices, b = dp.bits;
@@ -1169,11 +1263,16 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
   std::vector<int64_t> eoff(nb), foff(nb);
   int64_t &nE = w.nE, &nF = w.nF;
   nE = nF = 0;
+  // real rows of the A role and real columns of the B role per block
+  std::vector<int64_t> rows_r(nb), cols_r(nb);
   for (int64_t g = 0; g < nb; ++g) {
+    const bool dupb = mode[g] & 2;
+    rows_r[g] = (int64_t)blk_M[g] * (dupb ? 1 : cm);
+    cols_r[g] = (int64_t)blk_N[g] * (dupb ? 2 : 1);
     eoff[g] = nE;
     foff[g] = nF;
-    nE += (int64_t)blk_M[g] * cm;
-    nF += blk_N[g];
+    nE += rows_r[g];
+    nF += cols_r[g];
   }
   if (nE > INT32_MAX || nF > INT32_MAX) fail(QS_ERR_SHAPE, "split: exponent arrays too large");
   int64_t &arena = w.arena;
@@ -1197,10 +1296,12 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
       s.lda = d.lda;
       s.ldb = d.ldb;
       s.trans = d.trans;
-      s.Mr = d.M * cm;
+      s.dupb = (mode[g] & 2) ? 1 : 0;
+      s.Mr = d.M * (s.dupb ? 1 : cm);
+      s.Nr = d.N * (s.dupb ? 2 : 1);
       s.Kr = d.K * cm;
       s.MT = (s.Mr + TMS - 1) / TMS;
-      s.NT = (s.N + TNS - 1) / TNS;
+      s.NT = (s.Nr + TNS - 1) / TNS;
       s.KB = std::max(1, (s.Kr + TKS - 1) / TKS);
       s.eoff = (int32_t)eoff[g];
       s.foff = (int32_t)foff[g];
@@ -1211,7 +1312,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
       int e = 0;
       if (d.afac != 1.0 && d.afac != 0.0) std::frexp(d.afac, &e);
       s.e_afac = e;
-      s.swap = swp[g];
+      s.swap = mode[g] & 1;
       s.as_off = arena;
       arena += (int64_t)s.MT * s.KB * S * A_DIGIT_BYTES;
       s.bs_off = arena;
@@ -1245,7 +1346,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
     // land exactly on bit 31
     for (int t = 0; t < S; ++t)
       if (b * (S - 1 - t) - rshift == 31) ++rshift;
-    const int MT = (blk_M[g] * cm + TMS - 1) / TMS, NT = (blk_N[g] + TNS - 1) / TNS;
+    const int MT = (int)((rows_r[g] + TMS - 1) / TMS), NT = (int)((cols_r[g] + TNS - 1) / TNS);
     for (int nt = 0; nt < NT; ++nt)
       for (int mt = 0; mt < MT; ++mt) {
         SplitTile t{};
@@ -1254,22 +1355,34 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
         t.p1 = (int32_t)grp[g + 1];
         t.mt = mt;
         t.nt = nt;
-        t.Mr = blk_M[g] * cm;
-        t.N = blk_N[g];
+        t.Mr = (int32_t)rows_r[g];
+        t.N = (int32_t)cols_r[g];
         // column stride of C in its elements, in the caller's orientation
         const int64_t ldc0 = blk_ldc ? (*blk_ldc)[g] : std::max(blk_M_in[g], 1);
-        if (!swp[g]) {
+        const bool swp = mode[g] & 1, dupb = mode[g] & 2;
+        if (!swp && !dupb) {
           t.ldc = (int32_t)(ldc0 * cm);
           t.rs = 1;
-          t.rsplit = 0;
-        } else if (cm == 1) {
+          t.splits = 0;
+        } else if (!dupb && cm == 1) {
           t.ldc = 1;
           t.rs = (int32_t)ldc0;
-          t.rsplit = 0;
-        } else {
+          t.splits = 0;
+        } else if (!dupb) {
           t.ldc = 2;
           t.rs = (int32_t)(2 * ldc0);
-          t.rsplit = 1;
+          t.splits = 1;
+        } else if (!swp) {
+          // C' = M x 2N: row m at 2m, column j at (j/2) of C's columns, part j%2
+          t.rs = 2;
+          t.ldc = (int32_t)(2 * ldc0);
+          t.splits = 2;
+        } else {
+          // C'^T = N x 2M: row n at column n of C, column j = element j of the
+          // interleaved (Re, Im) column
+          t.rs = (int32_t)(2 * ldc0);
+          t.ldc = 1;
+          t.splits = 0;
         }
         t.eoff = (int32_t)eoff[g];
         t.foff = (int32_t)foff[g];

@@ -1,5 +1,6 @@
 """Output blocks that the split path computes transposed (C^T = op(B)^T op(A)^T,
-chosen when that pads the 128-row tiles much less): every transpose /
+chosen when that pads the 128-row tiles much less) or, for complex data,
+with the real form duplicating B instead of A: every transpose /
 conjugation flag of both operands, real and complex, several pairs summing
 into one block, and output blocks stored with a leading dimension larger than
 their row count.  Results are checked against numpy (split: 1e-12 relative,
@@ -106,3 +107,33 @@ def test_transposed_shared_blocks(ctx, cplx):
     cbuf, ref = _run(ctx, shapes, flags, [0, 0, 0, 1, 1, 2], cplx, "split", seed=3)
     assert _rel(cbuf, ref) <= 1e-12
     assert np.all(cbuf[ref == 0] == 0)
+
+
+def _layout(m, n, cm=2):
+    """The library's layout choice for an m x n complex block (0 plain, 1 C^T,
+    2 B duplicated, 3 C^T with B duplicated), restated for picking shapes."""
+    def cost(rows, cols):
+        mt, nt = -(-rows // 128), -(-cols // 32)
+        return 26900.0 * mt * nt + 49152.0 * mt + 10530.0 * nt
+    c = [cost(m * cm, n), cost(n * cm, m), cost(m, 2 * n), cost(n, 2 * m)]
+    best = min(range(4), key=lambda o: (c[o], o))
+    return best if c[best] < 0.97 * c[0] else 0
+
+
+def test_complex_layouts_all_flags(ctx):
+    """Every real-form layout of a complex block (A or B duplicated, plain or
+    transposed) under every transpose / conjugation flag, with pairs of
+    different depth summing into each block."""
+    base = [(64, 256, 40), (10, 64, 33), (400, 9, 70), (8, 300, 51)]
+    assert sorted(_layout(m, n) for m, n, _ in base) == [0, 1, 2, 3]
+    shapes, flags, blk = [], [], []
+    for f in range(16):
+        m, n, k = base[f % 4]
+        for j, kk in enumerate((k, 1 + (k * 7) % 97)):
+            shapes.append((m, n, kk))
+            flags.append((f + 5 * j) % 16)
+            blk.append(f)
+    for prec, tol in (("split", 1e-12), ("fp64", 1e-14)):
+        cbuf, ref = _run(ctx, shapes, flags, blk, True, prec, seed=11)
+        assert _rel(cbuf, ref) <= tol
+        assert np.all(cbuf[ref == 0] == 0)

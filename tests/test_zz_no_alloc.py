@@ -22,12 +22,15 @@ TOL = 1e-12               # split path target, relative Frobenius error
 
 
 def _digit_bytes_bound(pk: Packed) -> int:
-    """Upper bound of the BF16 digit arena of a batch (8 digits per operand)."""
+    """Upper bound of the BF16 digit arena of a batch (8 digits per operand;
+    the larger of the real-form layouts a block may take)."""
     cm = 2 if pk.cplx else 1
     tot = 0
     for M, N, K in zip(pk.M, pk.N, pk.K):
+        M, N = int(M), int(N)
         kb = max(1, -(-int(K) * cm // 32))
-        tot += (-(-int(M) * cm // 128) * kb * 8 * 8192) + (-(-int(N) // 32) * kb * 8 * 2048)
+        lay = [(cm * M, N), (cm * N, M)] + ([(M, 2 * N), (N, 2 * M)] if cm == 2 else [])
+        tot += max(-(-r // 128) * kb * 8 * 8192 + -(-c // 32) * kb * 8 * 2048 for r, c in lay)
     return tot
 
 
