@@ -148,12 +148,12 @@ def measured_peaks():
 
 
 # DRAM traffic of the split GEMM kernel, from one ncu capture of the same
-# kernel on the 300-pair case of this workload (dram__bytes_read.sum 1.187 GB
-# against a 1.118 GB digit arena; dram__bytes_write.sum 0.178 GB against
+# kernel on the 300-pair case of this workload (dram__bytes_read.sum 0.980 GB
+# against a 0.948 GB digit arena; dram__bytes_write.sum 0.176 GB against
 # 0.232 GB of output): the kernel reads its digit arena about once and writes
 # the output once, so the full launch is scaled by arena and output bytes.
-GEMM_DRAM_READ_PER_ARENA_BYTE = 1.186651e9 / 1118060544
-GEMM_DRAM_WRITE_PER_OUTPUT_BYTE = 177.814784e6 / 231684512
+GEMM_DRAM_READ_PER_ARENA_BYTE = 0.980110592e9 / 947933184
+GEMM_DRAM_WRITE_PER_OUTPUT_BYTE = 175.655168e6 / 231684512
 
 
 def split_arena_bytes(pk, S: int) -> float:
