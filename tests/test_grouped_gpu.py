@@ -47,6 +47,26 @@ def test_split_edges(ctx, shape, cplx):
     assert rel(C64, numpy_ref(w)) <= 1e-14
 
 
+@pytest.mark.parametrize("cplx", [False, True])
+def test_split_large_accumulators(ctx, cplx):
+    """Operands whose digits all carry the same sign and nearly full size:
+    every accumulator chunk sums to beyond 2^22, close to the 2^24 bound of
+    exact FP32 accumulation that sets the chunk depth; products of constant
+    blocks come out exact."""
+    M, N, K = 200, 72, 900
+    a = np.full((M, K), 0.9990234375)          # 1023/1024: top digits near full size
+    b = np.full((K, N), -0.998046875)
+    if cplx:
+        a = a + 1j * a
+        b = b - 1j * b
+    w = {"M": np.array([M]), "N": np.array([N]), "K": np.array([K]), "afac": np.array([1.0]),
+         "A": [np.asfortranarray(a)], "B": [np.asfortranarray(b)], "complex": cplx}
+    C = grouped.run_host(w, prec="split", ctx=ctx)
+    R = numpy_ref(w)
+    assert rel(C, R) <= 1e-15
+    assert np.array_equal(C[0], R[0])
+
+
 def test_split_wide_dynamic_range(ctx):
     """Rows and columns spanning many binades: per-row/column scales."""
     rng = np.random.default_rng(11)
