@@ -5,6 +5,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <unordered_set>
+#include <mutex>
 #include <new>
 #include <numeric>
 
@@ -45,6 +47,24 @@ void *Ctx::ensure_scratch(size_t bytes) {
 // through the page-locked ring, read by a copy kernel (not a copy engine).
 // A region of the ring is reused only after the copy that last read it has
 // completed.
+namespace {
+std::mutex g_live_mu;
+std::unordered_set<const Ctx *> g_live;
+}  // namespace
+
+void ctx_register(const Ctx *c) {
+  std::lock_guard<std::mutex> lk(g_live_mu);
+  g_live.insert(c);
+}
+void ctx_unregister(const Ctx *c) {
+  std::lock_guard<std::mutex> lk(g_live_mu);
+  g_live.erase(c);
+}
+bool ctx_alive(const Ctx *c) {
+  std::lock_guard<std::mutex> lk(g_live_mu);
+  return g_live.count(c) != 0;
+}
+
 void Ctx::stage_upload(void *dst, const void *src, size_t bytes) {
   if (!bytes) return;
   const int64_t n = (int64_t)((bytes + 255) & ~size_t(255));
@@ -683,12 +703,14 @@ qs_status qs_ctx_create(int device, qs_ctx **out) {
   QS_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
   QS_CUDA(cudaMalloc(&c->c.d_err, 64));
   QS_CUDA(cudaMemset(c->c.d_err, 0, 64));
+  ctx_register(&c->c);
   *out = c.release();
   QS_API_END
 }
 
 void qs_ctx_destroy(qs_ctx *ctx) {
   if (!ctx) return;
+  ctx_unregister(&ctx->c);
   cudaSetDevice(ctx->c.device);
   xcache_orphan_all(&ctx->c);
   if (ctx->c.scratch) cudaFreeAsync(ctx->c.scratch, ctx->c.stream);

@@ -151,6 +151,12 @@ void launch_block_axpy(Ctx *ctx, const int64_t *d_soff, const int64_t *d_doff, c
 // copies `bytes` from mapped page-locked host memory to device memory with a kernel
 void launch_stage_copy(Ctx *ctx, const void *src, void *dst, size_t bytes);
 
+// Contexts alive in this process (qs_capi.cpp).  Objects that outlive their
+// context (device tensors, plans) release their memory without its stream.
+void ctx_register(const Ctx *c);
+void ctx_unregister(const Ctx *c);
+bool ctx_alive(const Ctx *c);
+
 // qs_linalg.cu
 void destroy_solver(Ctx *ctx);
 

@@ -13,7 +13,11 @@ struct qs_tensor {
   double *d = nullptr;   // owned arena (stream-ordered allocation)
   qs::Ctx *ctx = nullptr;  // context whose stream frees the arena
   ~qs_tensor() {
-    if (d && ctx) cudaFreeAsync(d, ctx->stream);
+    if (!d) return;
+    if (ctx && qs::ctx_alive(ctx))
+      cudaFreeAsync(d, ctx->stream);
+    else
+      cudaFree(d);  // the context is gone: device pool memory, freed synchronously
   }
 };
 

@@ -256,8 +256,10 @@ qs_status qs_grouped_plan_run(qs_grouped_plan *p, const double *A, const double 
 
 void qs_grouped_plan_destroy(qs_grouped_plan *p) {
   if (!p) return;
-  cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
+  if (p->ctx && ctx_alive(p->ctx)) {  // else the context's stream is gone
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->ctx->stream);
+  }
   if (p->exec) cudaGraphExecDestroy(p->exec);
   split_plan_destroy(p->split);
   if (p->d_pairs) cudaFree(p->d_pairs);
