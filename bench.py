@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--prec", default="split", choices=["split", "fp64"])
     ap.add_argument("--npairs", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--shard", action="store_true",
+                    help="split one batch over the ranks by output block (strong scaling) instead of one "
+                         "independent batch per rank")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=3)
@@ -269,8 +272,15 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
         pg = dist
     ctx = default_context(local)
-    w = grouped_pairs(seed=a.seed + rank, npairs=a.npairs, complex_data=True)
-    pk = Packed(w["A"], w["B"], w["afac"], cplx=True)
+    if a.shard:
+        # one batch, its output blocks spread over the ranks by flops
+        from qspace_gb300.shard import block_flops, partition_blocks, shard
+        w = grouped_pairs(seed=a.seed, npairs=a.npairs, complex_data=True)
+        full = Packed(w["A"], w["B"], w["afac"], cplx=True)
+        pk = shard(full, partition_blocks(block_flops(full), ws)[rank])
+    else:
+        w = grouped_pairs(seed=a.seed + rank, npairs=a.npairs, complex_data=True)
+        pk = Packed(w["A"], w["B"], w["afac"], cplx=True)
     flops = pk.flops()
     db = DeviceBatch(pk, ctx)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr)
@@ -559,12 +569,14 @@ def main():
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": a.steps,
-                "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "strong" if a.shard else "weak",
                 "vs_baseline": None, "dtype": "f64 (split: bf16 digits, fp32 exact accumulation)",
                 "data": "synthetic (seeded normal)",
                 "config": {"workload": WORKLOAD, "npairs": a.npairs, "seed": a.seed, "prec": a.prec,
                            "nslices": st.get("nslices"), "digit_bits": st.get("digit_bits"),
-                           "parallelism": f"replicas x{ws}", "l2": "inputs 2.8 GB > L2, no flush",
+                           "parallelism": f"output-block shards x{ws}" if a.shard else f"replicas x{ws}",
+                           "l2": "inputs 2.8 GB > L2, no flush",
                            "mode": a.mode + ("" if a.mode == "oneshot" else
                                              " (reusable plan, CUDA graph replay"
                                              + (", autotuned digit width)" if not a.no_autotune else ")"))},
