@@ -569,14 +569,15 @@ def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float 
     (Source/gathered.cc:1822-2040) with eigQS's option handling
     (Source/eigQS.cc:55-100): deps > 0 averages near-degenerate levels and
     moves the cut to the largest weighted gap near Nkeep (b=-1, dmax=-1).
-    Returns (list of bool arrays, number kept).  (The reference's NK output
-    is that number except with Etrunc > 0 and deps = 0, where markSet leaves
-    it at min(Nkeep, N): only its gap-search branch rewrites Nkeep.)"""
+    Returns (list of bool arrays, the reference's NK output): NK is the
+    number kept, except with Etrunc > 0 and deps = 0, where markSet leaves it
+    at min(Nkeep, N) (only its gap-search branch rewrites Nkeep)."""
     sizes = [len(e) for e in E_blocks]
     E = np.concatenate([np.asarray(e, float) for e in E_blocks]) if E_blocks else np.zeros(0)
     N = len(E)
     keep = np.zeros(N, bool)
-    out = lambda: ([keep[s:s + n] for s, n in zip(np.cumsum([0] + sizes[:-1]), sizes)], int(keep.sum()))
+    out = lambda nk=None: ([keep[s:s + n] for s, n in zip(np.cumsum([0] + sizes[:-1]), sizes)],
+                           int(keep.sum()) if nk is None else int(nk))
     if N == 0:
         return out()
     P = np.argsort(E, kind="stable")
@@ -624,7 +625,7 @@ def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float 
                 xmax, imax = x, i
         l = imax
     keep[P[:min(l, N)]] = True
-    return out()
+    return out(Nk if (etrunc > 0 and not deps > 0) else None)
 
 
 def svd_keep(S_blocks: list, nkeep: int = -1, nkmin: int = 0, stol: float = 0.0):

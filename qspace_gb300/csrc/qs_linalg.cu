@@ -187,8 +187,9 @@ __global__ void scale_kernel(double *__restrict__ v, int64_t n, const double *__
 // levels (relative to the spectral width) and moves the cut to the largest
 // weighted gap near Nkeep (b = -1, dmax = -1); otherwise the Nkeep lowest
 // levels are kept, or those below E_min + Etrunc when Etrunc > 0.
-// *nkeep_out is the number kept (the reference's NK output differs only with
-// Etrunc > 0 and deps = 0, where markSet leaves it at min(Nkeep, N)).
+// *nkeep_out is the reference's NK output: the number kept, except with
+// Etrunc > 0 and deps = 0, where markSet leaves it at min(Nkeep, N) (only its
+// gap-search branch writes the cut back); `keep` holds the kept states.
 void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nkeep_in, double etrunc,
                     double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
   int64_t N = 0;
@@ -259,7 +260,7 @@ void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nke
   }
   if (l >= N) l = N;
   for (int64_t i = 0; i < l; ++i) keep[P[i]] = 1;
-  if (nkeep_out) *nkeep_out = l;
+  if (nkeep_out) *nkeep_out = (etrunc > 0 && !(deps > 0)) ? Nkeep : l;
   if (etrunc_out) *etrunc_out = (l < N) ? s[l] - s[0] : 0.0;
 }
 

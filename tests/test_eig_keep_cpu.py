@@ -2,9 +2,9 @@
 degeneracy averaging with the weighted-gap cut for deps > 0) against fixtures
 made by the REFERENCE's own eigQS (tests/golden/make_eig_golden.py): the
 oracle's restatement and the library's host implementation (qs_mark_keep)
-keep the same states of every sector as the reference, and report its NK
-where the reference updates it (with Etrunc > 0 and deps = 0 its NK stays
-min(Nkeep, N) while its kept set EK follows Etrunc)."""
+keep the same states of every sector as the reference and report the same NK
+(with Etrunc > 0 and deps = 0 the reference's NK stays min(Nkeep, N) while
+its kept set EK follows Etrunc)."""
 import json
 from pathlib import Path
 
@@ -36,10 +36,8 @@ def test_eig_truncation_matches_reference(impl):
             keep, nk = orc.mark_keep(E, *args)
         else:
             keep, nk, _ = mark_keep(E, *args)
-        kept_ref = sum(np.size(d) for d in EK["data"])
-        assert nk == kept_ref, c
-        if o.get("deps", 0.0) > 0 or o.get("Etrunc", 0.0) <= 0:
-            assert nk == c["NK"], c      # otherwise the reference's NK stays min(Nkeep, N)
+        assert nk == c["NK"], c
+        assert sum(int(np.sum(k)) for k in keep) == sum(np.size(d) for d in EK["data"]), c
         got = {tuple(np.asarray(H["Q"][0][i]).ravel()): E[i][np.asarray(keep[i], bool)] for i in range(len(E))
                if np.any(keep[i])}
         ref = {tuple(np.asarray(EK["Q"][0][i]).ravel()): np.sort(np.asarray(d).ravel()) for i, d in enumerate(EK["data"])}
