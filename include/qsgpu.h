@@ -312,8 +312,14 @@ QS_EXPORT void qs_grouped_plan_destroy(qs_grouped_plan *plan);
  *    overlap in time (two host threads, two contexts) race on it and corrupt
  *    each other's results.  Serialise them.
  *  - A, B, C are device pointers as for qs_grouped_gemm; the call returns
- *    after the product is complete (it synchronises the context's stream to
- *    read the error word). */
+ *    after the product is complete: it synchronises the context's stream to
+ *    read the error word, so it must not be called while that stream is
+ *    being captured into a CUDA graph.
+ *  - The array is device memory of every process that loads the module
+ *    holding it: on each device where that module is loaded (at the first
+ *    call with lazy module loading, at context creation with
+ *    CUDA_MODULE_LOADING=EAGER), even if the entry point is never called,
+ *    and until the process exits. */
 #define QS_STATIC_SCRATCH_BYTES 33554432 /* 32 MiB */
 QS_EXPORT qs_status qs_grouped_gemm_split_static(qs_ctx *ctx, const qs_pair_list *pairs,
                                                  const double *A, const double *B, double *C,
@@ -363,10 +369,16 @@ QS_EXPORT qs_status qs_eig_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *n,
 
 /* Global truncation over all blocks' eigenvalues (markSet,
  * Source/gathered.cc:1822-1990, as used by EigenSymmetric :4814): marks the
- * Nkeep lowest (weighted by multiplet dimension `qdim_w`, NULL = 1), widened to
- * keep degenerate multiplets within deps, capped by Etrunc when > 0.  Host
- * arrays; `keep` receives 0/1 per eigenvalue.  Returns the kept count in
- * *nkeep_out and the truncation energy in *etrunc_out. */
+ * Nkeep lowest, moved to the widest gap near the cut when deps > 0 (so that
+ * degenerate multiplets stay together), capped by Etrunc when > 0.  Host
+ * arrays; `keep` receives 0/1 per eigenvalue.  `qdim_w` (weighting by
+ * multiplet dimension) must be NULL: weights are refused with
+ * QS_ERR_UNSUPPORTED.
+ * *nkeep_out receives NK exactly as markSet leaves it: min(Nkeep, N) (N = all
+ * eigenvalues; Nkeep < 0 counts as N) when Etrunc > 0 and deps == 0, even
+ * where Etrunc keeps fewer states; otherwise the number of kept states.  To
+ * size buffers, count the 1s in `keep`.  *etrunc_out receives the
+ * truncation energy. */
 QS_EXPORT qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E,
                        const double *qdim_w, int64_t nkeep, double etrunc,
                        double deps, uint8_t *keep, int64_t *nkeep_out,
@@ -379,7 +391,9 @@ QS_EXPORT qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E
  * leg and the eigenstate index, labels of H's block; blocks without kept
  * resp. discarded states are omitted).  Optional host outputs: E (sum of the
  * block sizes) = ascending eigenvalues per block in H's block order, keep =
- * 0/1 per eigenvalue, the kept count and the truncation energy. */
+ * 0/1 per eigenvalue, NK as qs_mark_keep reports it (not always the kept
+ * count: count the kept states from `keep` or from *AK's blocks) and the
+ * truncation energy. */
 QS_EXPORT qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc,
                        double deps, qs_tensor **AK, qs_tensor **AD, double *E,
                        uint8_t *keep, int64_t *nkeep_out, double *etrunc_out);
@@ -405,6 +419,19 @@ QS_EXPORT qs_status qs_svd_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *m,
                         const int64_t *uoffs, const int64_t *soffs,
                         const int64_t *voffs, const double *A, double *U,
                         double *S, double *Vt);
+
+/* The same for real (is_complex = 0: FP64) or complex (is_complex = 1:
+ * interleaved complex128, offsets in complex elements; Vt = V^H) blocks,
+ * with the Jacobi sweep limit (0 = 100) and tolerance (<= 0: 1e-15).  A
+ * block that does not converge within max_sweeps fails the call with
+ * QS_ERR_NUMERIC (wbSVD stops on a LAPACK info != 0,
+ * Source/wbarray_blas.cc:1040-1060). */
+QS_EXPORT qs_status qs_svd_blocks_ex(qs_ctx *ctx, int64_t nblk, const int64_t *m,
+                        const int64_t *n, const int64_t *offs,
+                        const int64_t *uoffs, const int64_t *soffs,
+                        const int64_t *voffs, int32_t is_complex,
+                        const double *A, double *U, double *S, double *Vt,
+                        int32_t max_sweeps, double tol);
 
 /* ------------------------------------------- Davidson re-orthogonalisation
  * Double classical Gram-Schmidt of vector v (length n) against the nv

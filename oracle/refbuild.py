@@ -13,7 +13,7 @@ headers (its CG coefficients are then computed in double precision).
 Outputs go to oracle/_ref/ only (git-ignored).  Nothing here runs on the GPU
 box: the reference checkout is not there.
 
-    python -m oracle.refbuild [names...]
+    python -m oracle.refbuild [--source=<reference>/Source] [names...]
 """
 from __future__ import annotations
 
@@ -27,7 +27,10 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 SHIM = HERE / "refshim"
 OUT = HERE / "_ref"
-REF_SRC = Path(os.environ.get("QS_REFERENCE_SOURCE", "/root/reference/Source"))
+# Where the reference's Source/ directory is: QS_REFERENCE_SOURCE, a
+# --source=PATH argument, or else a checkout named "reference" beside this
+# repository's root.
+REF_SRC = Path(os.environ.get("QS_REFERENCE_SOURCE") or (HERE.parent.parent / "reference" / "Source"))
 DEFAULT = ("contractQS", "permuteQS", "eigQS", "svdQS", "getIdentityQS")
 
 
@@ -87,6 +90,9 @@ def build(names=DEFAULT, force=False, jobs=None) -> list[Path]:
 
 
 if __name__ == "__main__":
+    for a in sys.argv[1:]:
+        if a.startswith("--source="):
+            REF_SRC = Path(a.split("=", 1)[1])
     names = tuple(a for a in sys.argv[1:] if not a.startswith("-")) or DEFAULT
     for p in build(names, force="--force" in sys.argv):
         print(p)

@@ -144,6 +144,9 @@ SIGNATURES = {
     "qs_svd_blocks": (C.c_int, [C.c_void_p, C.c_int64, c_int64_p, c_int64_p, c_int64_p, c_int64_p,
                                 c_int64_p, c_int64_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p]),
+    "qs_svd_blocks_ex": (C.c_int, [C.c_void_p, C.c_int64, c_int64_p, c_int64_p, c_int64_p, c_int64_p,
+                                   c_int64_p, c_int64_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_int32, C.c_double]),
     "qs_gs_reortho": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                 c_double_p]),
     "qs_server_create": (C.c_int, [C.c_void_p, C.POINTER(ServerCfg), C.POINTER(C.c_void_p)]),

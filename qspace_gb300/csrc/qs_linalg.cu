@@ -605,47 +605,103 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
 }
 
 // -------------------------------------------------------------- svd blocks
+// One Jacobi SVD (gesvdj, FP64 or complex128) per block on the context's
+// stream.  The copy of the block, V and the solver workspace are allocated
+// once for the largest block and reused.  A block that does not converge
+// within max_sweeps (info > 0) fails the call with QS_ERR_NUMERIC, like the
+// reference's wbSVD, which stops on a LAPACK info != 0
+// (Source/wbarray_blas.cc:1040-1060).
 void svd_blocks(Ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
                 const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, const double *A, double *U,
-                double *S, double *Vt) {
+                double *S, double *Vt, int cplx, int max_sweeps, double tol) {
   if (nblk <= 0) return;
+  if (max_sweeps <= 0) max_sweeps = 100;
+  if (!(tol > 0)) tol = 1e-15;
+  const int64_t es = cplx ? 2 : 1;  // doubles per element
   cusolverDnHandle_t h = solver_of(ctx);
   gesvdjInfo_t params;
   QS_SOLVER(cusolverDnCreateGesvdjInfo(&params));
-  QS_SOLVER(cusolverDnXgesvdjSetTolerance(params, 1e-15));
-  QS_SOLVER(cusolverDnXgesvdjSetMaxSweeps(params, 100));
-  int *d_info = dev_alloc<int>(ctx, (size_t)nblk);
-  QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * nblk, ctx->stream));
+  struct ParamsGuard {
+    gesvdjInfo_t p;
+    ~ParamsGuard() { cusolverDnDestroyGesvdjInfo(p); }
+  } guard{params};
+  QS_SOLVER(cusolverDnXgesvdjSetTolerance(params, tol));
+  QS_SOLVER(cusolverDnXgesvdjSetMaxSweeps(params, max_sweeps));
+  int64_t maxa = 0, maxv = 0;
+  int lwork = 1;
   for (int64_t i = 0; i < nblk; ++i) {
     const int64_t mi = m[i], ni = n[i];
     if (mi < 0 || ni < 0 || mi > INT32_MAX || ni > INT32_MAX) fail(QS_ERR_SHAPE, "svd: bad block size");
     if (mi == 0 || ni == 0) continue;
-    const int64_t k = std::min(mi, ni);
-    double *a = dev_alloc<double>(ctx, (size_t)(mi * ni));
-    double *v = dev_alloc<double>(ctx, (size_t)(ni * k));
-    QS_CUDA(cudaMemcpyAsync(a, A + offs[i], (size_t)(mi * ni) * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    int lwork = 0;
-    QS_SOLVER(cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)mi, (int)ni, a, (int)mi, S + soffs[i],
-                                           U + uoffs[i], (int)mi, v, (int)ni, &lwork, params));
-    double *work = dev_alloc<double>(ctx, (size_t)std::max(lwork, 1));
-    QS_SOLVER(cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)mi, (int)ni, a, (int)mi, S + soffs[i],
-                                U + uoffs[i], (int)mi, v, (int)ni, work, lwork, d_info + i, params));
-    ctx->launches++;
-    const int64_t tot = ni * k;
-    transpose_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 1024), 256, 0, ctx->stream>>>(
-        v, Vt + voffs[i], ni, k, 0);
-    QS_LAUNCHED(ctx);
+    maxa = std::max(maxa, mi * ni);
+    maxv = std::max(maxv, ni * std::min(mi, ni));
+  }
+  if (maxa == 0) return;
+  double *a = dev_alloc<double>(ctx, (size_t)(maxa * es));
+  double *v = dev_alloc<double>(ctx, (size_t)(maxv * es));
+  int *d_info = dev_alloc<int>(ctx, (size_t)nblk);
+  double *work = nullptr;
+  try {
+    // workspace for the largest need over the distinct block shapes
+    std::vector<std::pair<int64_t, int64_t>> shapes;
+    for (int64_t i = 0; i < nblk; ++i)
+      if (m[i] > 0 && n[i] > 0) shapes.emplace_back(m[i], n[i]);
+    std::sort(shapes.begin(), shapes.end());
+    shapes.erase(std::unique(shapes.begin(), shapes.end()), shapes.end());
+    for (auto &sh : shapes) {
+      const int mi = (int)sh.first, ni = (int)sh.second;
+      int lw = 0;
+      if (cplx)
+        QS_SOLVER(cusolverDnZgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, mi, ni, (cuDoubleComplex *)a, mi, S,
+                                               (cuDoubleComplex *)U, mi, (cuDoubleComplex *)v, ni, &lw, params));
+      else
+        QS_SOLVER(cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, mi, ni, a, mi, S, U, mi, v, ni, &lw,
+                                               params));
+      lwork = std::max(lwork, lw);
+    }
+    work = dev_alloc<double>(ctx, (size_t)lwork * es);
+    QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * nblk, ctx->stream));
+    for (int64_t i = 0; i < nblk; ++i) {
+      const int64_t mi = m[i], ni = n[i];
+      if (mi == 0 || ni == 0) continue;
+      const int64_t k = std::min(mi, ni);
+      QS_CUDA(cudaMemcpyAsync(a, A + offs[i] * es, (size_t)(mi * ni * es) * 8, cudaMemcpyDeviceToDevice,
+                              ctx->stream));
+      if (cplx)
+        QS_SOLVER(cusolverDnZgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)mi, (int)ni, (cuDoubleComplex *)a, (int)mi,
+                                    S + soffs[i], (cuDoubleComplex *)(U + uoffs[i] * es), (int)mi,
+                                    (cuDoubleComplex *)v, (int)ni, (cuDoubleComplex *)work, lwork, d_info + i,
+                                    params));
+      else
+        QS_SOLVER(cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)mi, (int)ni, a, (int)mi, S + soffs[i],
+                                    U + uoffs[i], (int)mi, v, (int)ni, work, lwork, d_info + i, params));
+      ctx->launches++;
+      const int64_t tot = ni * k;
+      transpose_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 1024), 256, 0, ctx->stream>>>(
+          v, Vt + voffs[i] * es, ni, k, cplx);
+      QS_LAUNCHED(ctx);
+    }
+    std::vector<int> info(nblk);
+    QS_CUDA(cudaMemcpyAsync(info.data(), d_info, nblk * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QS_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int64_t i = 0; i < nblk; ++i) {
+      if (info[i] < 0) fail(QS_ERR_NUMERIC, "svd: block %lld argument error %d", (long long)i, info[i]);
+      if (info[i] > 0)
+        fail(QS_ERR_NUMERIC, "svd: block %lld (%lld x %lld) did not converge within %d sweeps (info %d)",
+             (long long)i, (long long)m[i], (long long)n[i], max_sweeps, info[i]);
+    }
+  } catch (...) {
+    cudaStreamSynchronize(ctx->stream);  // buffers may be in use by queued work
     dev_free(ctx, a);
     dev_free(ctx, v);
-    dev_free(ctx, work);
+    dev_free(ctx, d_info);
+    if (work) dev_free(ctx, work);
+    throw;
   }
-  std::vector<int> info(nblk);
-  QS_CUDA(cudaMemcpyAsync(info.data(), d_info, nblk * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, a);
+  dev_free(ctx, v);
   dev_free(ctx, d_info);
-  cusolverDnDestroyGesvdjInfo(params);
-  for (int64_t i = 0; i < nblk; ++i)
-    if (info[i] < 0) fail(QS_ERR_NUMERIC, "svd: block %lld argument error %d", (long long)i, info[i]);
+  dev_free(ctx, work);
 }
 
 // ------------------------------------------------------------ Gram-Schmidt
@@ -828,7 +884,19 @@ qs_status qs_svd_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *m, const int64
   if (!ctx || (nblk > 0 && (!m || !n || !offs || !uoffs || !soffs || !voffs || !A || !U || !S || !Vt)))
     fail(QS_ERR_ARG, "null argument");
   QS_CUDA(cudaSetDevice(ctx->c.device));
-  svd_blocks(&ctx->c, nblk, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt);
+  svd_blocks(&ctx->c, nblk, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt, 0, 0, 0.0);
+  QS_API_END
+}
+
+qs_status qs_svd_blocks_ex(qs_ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
+                           const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, int32_t is_complex,
+                           const double *A, double *U, double *S, double *Vt, int32_t max_sweeps, double tol) {
+  QS_API_BEGIN
+  if (!ctx || (nblk > 0 && (!m || !n || !offs || !uoffs || !soffs || !voffs || !A || !U || !S || !Vt)))
+    fail(QS_ERR_ARG, "null argument");
+  if (max_sweeps < 0) fail(QS_ERR_ARG, "svd: negative sweep limit");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  svd_blocks(&ctx->c, nblk, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt, is_complex ? 1 : 0, max_sweeps, tol);
   QS_API_END
 }
 

@@ -58,6 +58,29 @@ class Packed:
         self.afac = np.ascontiguousarray(afac, np.float64)
         self.n = n
 
+    @classmethod
+    def from_operands(cls, A: list, B: list, ia, ib, afac, blk=None, cplx: bool | None = None) -> "Packed":
+        """A batch whose pairs share operand blocks: pair p multiplies A[ia[p]]
+        by B[ib[p]]; each distinct operand block is stored once in the arenas
+        (as a contraction's pair list reads its input tensors' blocks)."""
+        ia = np.asarray(ia, np.int64)
+        ib = np.asarray(ib, np.int64)
+        pk = cls([A[i] for i in ia], [B[i] for i in ib], afac, blk=blk, cplx=cplx)
+        dt = pk.abuf.dtype
+        asz = np.array([a.shape[0] * a.shape[1] for a in A], np.int64)
+        bsz = np.array([b.shape[0] * b.shape[1] for b in B], np.int64)
+        aoff = np.concatenate([[0], np.cumsum(asz)[:-1]]).astype(np.int64)
+        boff = np.concatenate([[0], np.cumsum(bsz)[:-1]]).astype(np.int64)
+        pk.abuf = np.concatenate([np.asarray(a, dt).reshape(-1, order="F") for a in A]) if A else np.zeros(0, dt)
+        pk.bbuf = np.concatenate([np.asarray(b, dt).reshape(-1, order="F") for b in B]) if B else np.zeros(0, dt)
+        pk.a_off = aoff[ia].copy()
+        pk.b_off = boff[ib].copy()
+        return pk
+
+    def operand_bytes(self) -> int:
+        """Bytes of the operand arenas (each stored block once)."""
+        return int(self.abuf.nbytes + self.bbuf.nbytes)
+
     def pair_list(self) -> PairList:
         pl = PairList()
         pl.npairs = self.n

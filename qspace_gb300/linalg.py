@@ -120,27 +120,36 @@ def svd_keep(S_blocks: list, nkeep: int = -1, nkmin: int = 0, stol: float = 0.0)
             sfac.value)
 
 
-def svd_blocks(blocks: list, ctx: Context | None = None):
-    """Thin SVD of real blocks on the GPU: returns lists U, S, Vt."""
+def svd_blocks(blocks: list, ctx: Context | None = None, max_sweeps: int = 0, tol: float = 0.0):
+    """Thin SVD of real or complex blocks on the GPU (qs_svd_blocks_ex):
+    returns lists U, S, Vt with A = U diag(S) Vt.  ``max_sweeps`` / ``tol``
+    bound the Jacobi iteration (0: the library defaults); a block that does
+    not converge raises QSError (QS_ERR_NUMERIC)."""
     import torch
     ctx = ctx or default_context()
+    cplx = any(np.iscomplexobj(b) for b in blocks)
+    dt = np.complex128 if cplx else np.float64
+    es = 2 if cplx else 1
     m = np.array([b.shape[0] for b in blocks], np.int64)
     n = np.array([b.shape[1] for b in blocks], np.int64)
     k = np.minimum(m, n)
-    cum = lambda x: np.concatenate([[0], np.cumsum(x)[:-1]]).astype(np.int64)
+    cum = lambda x: np.concatenate([[0], np.cumsum(x)[:-1]]).astype(np.int64)  # noqa: E731
     offs, uoffs, soffs, voffs = cum(m * n), cum(m * k), cum(k), cum(k * n)
-    A = np.concatenate([np.asarray(b, np.float64).reshape(-1, order="F") for b in blocks])
+    A = np.concatenate([np.asarray(b, dt).reshape(-1, order="F") for b in blocks]) if blocks else np.zeros(0, dt)
     dev = torch.device("cuda", ctx.device)
-    dA = torch.from_numpy(A).to(dev)
-    dU = torch.zeros(max(int((m * k).sum()), 1), dtype=torch.float64, device=dev)
+    dA = torch.from_numpy(A.view(np.float64)).to(dev)
+    dU = torch.zeros(max(int((m * k).sum()) * es, 1), dtype=torch.float64, device=dev)
     dS = torch.zeros(max(int(k.sum()), 1), dtype=torch.float64, device=dev)
-    dV = torch.zeros(max(int((k * n).sum()), 1), dtype=torch.float64, device=dev)
+    dV = torch.zeros(max(int((k * n).sum()) * es, 1), dtype=torch.float64, device=dev)
     torch.cuda.synchronize(dev)
-    check(ctx.lib.qs_svd_blocks(ctx.h, len(blocks), _ptr(m), _ptr(n), _ptr(offs), _ptr(uoffs), _ptr(soffs),
-                                _ptr(voffs), C.c_void_p(dA.data_ptr()), C.c_void_p(dU.data_ptr()),
-                                C.c_void_p(dS.data_ptr()), C.c_void_p(dV.data_ptr())))
+    check(ctx.lib.qs_svd_blocks_ex(ctx.h, len(blocks), _ptr(m), _ptr(n), _ptr(offs), _ptr(uoffs), _ptr(soffs),
+                                   _ptr(voffs), 1 if cplx else 0, C.c_void_p(dA.data_ptr()),
+                                   C.c_void_p(dU.data_ptr()), C.c_void_p(dS.data_ptr()), C.c_void_p(dV.data_ptr()),
+                                   int(max_sweeps), float(tol)))
     ctx.sync()
     U, S, V = dU.cpu().numpy(), dS.cpu().numpy(), dV.cpu().numpy()
+    if cplx:
+        U, V = U.view(np.complex128), V.view(np.complex128)
     Us = [U[uoffs[i]:uoffs[i] + m[i] * k[i]].reshape((m[i], k[i]), order="F") for i in range(len(blocks))]
     Ss = [S[soffs[i]:soffs[i] + k[i]] for i in range(len(blocks))]
     Vs = [V[voffs[i]:voffs[i] + k[i] * n[i]].reshape((k[i], n[i]), order="F") for i in range(len(blocks))]
@@ -169,7 +178,9 @@ def eigQS_dev(H, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0):
     device.  Returns (Etot, I) with Etot the ascending eigenvalues of all
     blocks, I['AK'] / I['AD'] device Tensors of the kept / discarded
     eigenvectors, I['E'] the per-block eigenvalues (H's block order),
-    I['keep'] their 0/1 flags, I['NK'] the kept count, I['Etrunc']."""
+    I['keep'] their 0/1 flags, I['NK'] the reference's NK (markSet's
+    min(Nkeep, N) when Etrunc > 0 and deps == 0, else the kept count; the
+    kept states are the 1s of I['keep']), I['Etrunc']."""
     from .qspace import Tensor
     ctx = H.ctx
     rank, qdim, nblk, nelem, cx = H.meta()

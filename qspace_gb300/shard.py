@@ -48,17 +48,31 @@ def partition_blocks(flops, nranks: int) -> list:
 def shard(pk: Packed, blocks) -> Packed:
     """The sub-batch of the pairs of output blocks `blocks` (indices into
     pk.blocks), in their original order, with only the A and B blocks those
-    pairs read.  Its output blocks are the selected ones, in ascending order."""
+    pairs read, each stored once even when several of its pairs read it.  An
+    operand block read by output blocks of several ranks is copied to each of
+    them.  Its output blocks are the selected ones, in ascending order; its
+    ``pairs`` attribute holds the selected pairs' indices in pk."""
     want = set(int(b) for b in blocks)
     first = {}
     for p in range(pk.n):
         first.setdefault(int(pk.blk[p]), len(first))
     sel = [p for p in range(pk.n) if first[int(pk.blk[p])] in want]
-    A = [pk.abuf[pk.a_off[p]:pk.a_off[p] + int(pk.M[p]) * int(pk.K[p])].reshape(
-        (int(pk.M[p]), int(pk.K[p])), order="F") for p in sel]
-    B = [pk.bbuf[pk.b_off[p]:pk.b_off[p] + int(pk.K[p]) * int(pk.N[p])].reshape(
-        (int(pk.K[p]), int(pk.N[p])), order="F") for p in sel]
-    return Packed(A, B, pk.afac[sel], blk=pk.blk[sel], cplx=pk.cplx)
+    # distinct operand blocks by their place in pk's arenas
+    amap, bmap, A, B = {}, {}, [], []
+    for p in sel:
+        ka = (int(pk.a_off[p]), int(pk.M[p]), int(pk.K[p]))
+        if ka not in amap:
+            amap[ka] = len(A)
+            A.append(pk.abuf[ka[0]:ka[0] + ka[1] * ka[2]].reshape((ka[1], ka[2]), order="F"))
+        kb = (int(pk.b_off[p]), int(pk.K[p]), int(pk.N[p]))
+        if kb not in bmap:
+            bmap[kb] = len(B)
+            B.append(pk.bbuf[kb[0]:kb[0] + kb[1] * kb[2]].reshape((kb[1], kb[2]), order="F"))
+    ia = [amap[(int(pk.a_off[p]), int(pk.M[p]), int(pk.K[p]))] for p in sel]
+    ib = [bmap[(int(pk.b_off[p]), int(pk.K[p]), int(pk.N[p]))] for p in sel]
+    out = Packed.from_operands(A, B, ia, ib, pk.afac[sel], blk=pk.blk[sel], cplx=pk.cplx)
+    out.pairs = np.array(sel, np.int64)
+    return out
 
 
 def assemble(pk: Packed, parts: list, results: list) -> list:

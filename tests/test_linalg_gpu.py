@@ -79,6 +79,34 @@ def test_svd_blocks(ctx):
         assert np.max(np.abs(Vt @ Vt.T - np.eye(k))) <= 1e-12 * k
 
 
+def test_svd_blocks_complex(ctx):
+    rng = np.random.default_rng(10)
+    shapes = [(1, 1), (6, 2), (2, 6), (50, 50), (90, 33), (33, 90)]
+    blocks = [rng.standard_normal(s) + 1j * rng.standard_normal(s) for s in shapes]
+    Us, Ss, Vs = svd_blocks(blocks, ctx)
+    for A, U, S, Vt in zip(blocks, Us, Ss, Vs):
+        ref = np.linalg.svd(A, compute_uv=False)
+        assert np.max(np.abs(np.sort(S)[::-1] - ref)) <= 1e-12 * ref.max()
+        assert np.max(np.abs((U * S[None, :]) @ Vt - A)) <= 1e-11 * max(1.0, np.abs(A).max())
+        k = min(A.shape)
+        assert np.max(np.abs(U.conj().T @ U - np.eye(k))) <= 1e-12 * k
+        assert np.max(np.abs(Vt @ Vt.conj().T - np.eye(k))) <= 1e-12 * k
+
+
+def test_svd_not_converged_is_an_error(ctx):
+    """One Jacobi sweep at a tolerance of 1e-15 cannot diagonalise a dense
+    random 120 x 90 block: the call reports QS_ERR_NUMERIC instead of
+    returning unconverged factors."""
+    from qspace_gb300._capi import QSError
+    rng = np.random.default_rng(12)
+    blocks = [rng.standard_normal((4, 3)), rng.standard_normal((120, 90))]
+    with pytest.raises(QSError, match="did not converge"):
+        svd_blocks(blocks, ctx, max_sweeps=1, tol=1e-15)
+    # the context stays usable; the default sweep limit converges
+    _, Ss, _ = svd_blocks(blocks, ctx)
+    assert np.allclose(Ss[1], np.linalg.svd(blocks[1], compute_uv=False), rtol=1e-12, atol=1e-13)
+
+
 @pytest.mark.parametrize("n,nv", [(1000, 4), (100003, 8), (5, 0), (2_000_000, 3)])
 def test_gs_reortho(ctx, n, nv):
     rng = np.random.default_rng(n)

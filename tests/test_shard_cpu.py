@@ -65,6 +65,42 @@ def test_shard_keeps_only_referenced_operands():
     assert sizes == pk.abuf.size + pk.bbuf.size        # every operand block goes to one rank
 
 
+def _shared_operand_batch():
+    """Six output blocks; A block 0 feeds blocks 0, 2 and 5, A block 1 feeds
+    blocks 1 and 3; B blocks are shared the same way."""
+    rng = np.random.default_rng(21)
+    M, N, K = [7, 9], [5, 4, 6], [3, 8]
+    A = [rng.standard_normal((M[i], K[i])) + 1j * rng.standard_normal((M[i], K[i])) for i in range(2)]
+    B = [rng.standard_normal((K[0], N[j])) + 1j * rng.standard_normal((K[0], N[j])) for j in range(3)] + \
+        [rng.standard_normal((K[1], N[j])) + 1j * rng.standard_normal((K[1], N[j])) for j in range(3)]
+    #        out: 0  1  2  3  4  5
+    ia = np.array([0, 1, 0, 1, 0, 0])
+    ib = np.array([0, 4, 1, 3, 2, 2])
+    afac = rng.uniform(-1, 1, 6)
+    return Packed.from_operands(A, B, ia, ib, afac, cplx=True), A, B, ia, ib
+
+
+def test_shard_copies_shared_operands_to_every_rank_that_reads_them():
+    pk, A, B, ia, ib = _shared_operand_batch()
+    # the packed batch stores each operand block once
+    assert pk.operand_bytes() == 16 * (sum(a.size for a in A) + sum(b.size for b in B))
+    parts = partition_blocks(block_flops(pk), 2)
+    total = 0
+    for idx in parts:
+        s = shard(pk, idx)
+        pairs = set(int(p) for p in s.pairs)
+        want = 16 * (sum(A[i].size for i in set(ia[list(pairs)].tolist()))
+                     + sum(B[j].size for j in set(ib[list(pairs)].tolist())))
+        assert s.operand_bytes() == want          # distinct blocks of its pairs, once each
+        total += s.operand_bytes()
+        # the shard computes its blocks exactly as the full batch does
+        full = _oracle_blocks(pk)
+        for b, x in zip(idx, _oracle_blocks(s)):
+            assert np.array_equal(x, full[int(b)])
+    # blocks read by both ranks' pairs are duplicated, so the ranks hold more than the batch
+    assert total > pk.operand_bytes()
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))

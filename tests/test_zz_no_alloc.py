@@ -1,7 +1,9 @@
 """qs_grouped_gemm_split_static: the split grouped GEMM whose device scratch is
 one file-scope array per device (nothing allocated).  Called twice in a row
 through the C-ABI it must reproduce qs_grouped_gemm (split) on the same pair
-list within 1e-12 relative error, without changing the device's free memory;
+list within 1e-12 relative error, without changing the device's free memory
+(the first call of a process may only add the array itself, when it loads
+the module that holds it);
 a pair list that needs more than QS_STATIC_SCRATCH_BYTES is refused with
 QS_ERR_OOM before anything runs.  The file name sorts last so that the suite
 also runs it after every other GPU test; it passes alone as well."""
@@ -19,6 +21,8 @@ pytestmark = pytest.mark.gpu
 
 STATIC_BYTES = 32 << 20   # QS_STATIC_SCRATCH_BYTES
 TOL = 1e-12               # split path target, relative Frobenius error
+MODULE_SLACK = 8 << 20    # module image and the driver's allocation granularity
+_MODULE_LOADED = [False]  # set once a call of this process has returned
 
 
 def _digit_bytes_bound(pk: Packed) -> int:
@@ -56,22 +60,27 @@ def _check_twice(ctx, pk: Packed):
     ref = [b.copy() for b in db.result()]
     exact = [a @ b * f for a, b, f in zip([np.asarray(x) for x in _A(pk)], _B(pk), pk.afac)] \
         if len(set(pk.blk.tolist())) == pk.n else None
-    free0 = None
     for call in range(2):
         db.dC.fill_(float("nan"))            # a call that wrote nothing would fail
         torch.cuda.synchronize()
-        if call == 1:
-            free0 = torch.cuda.mem_get_info(ctx.device)[0]
+        free0 = torch.cuda.mem_get_info(ctx.device)[0]
         rc, st = _static(db)
         assert rc == 0, ctx.lib.qs_last_error().decode()
+        free1 = torch.cuda.mem_get_info(ctx.device)[0]
         assert st.nslices >= 2 and st.npairs == pk.n and st.launches >= 3
         got = db.result()
         assert all(np.all(np.isfinite(g)) for g in got)
         assert _rel(got, ref) <= TOL, call
         if exact is not None:
             assert _rel(got, exact) <= TOL, call
-    # the second call ran on a loaded module: no device memory came or went
-    assert torch.cuda.mem_get_info(ctx.device)[0] == free0
+        if _MODULE_LOADED[0]:
+            # the array is resident: no device memory comes or goes
+            assert free1 == free0, (call, free0 - free1)
+        else:
+            # the first call of the process may load the module that holds the
+            # array (lazy loading): at most the array plus the module image
+            assert 0 <= free0 - free1 <= STATIC_BYTES + MODULE_SLACK, (call, free0 - free1)
+            _MODULE_LOADED[0] = True
 
 
 def _A(pk: Packed):
