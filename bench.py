@@ -479,6 +479,41 @@ def main():
                 ts.append(time.perf_counter() - t0)
             rdm[pr + "_ms_p50"] = 1e3 * statistics.median(ts)
 
+    # ---- permuteQS kernels on a device-resident two-site wave function
+    # psi(L, s1, s2, R), U(1)xU(1), bond dimension 8192, complex128 (257 MB,
+    # larger than L2): bytes = read + write of every element once
+    permute = None
+    if not a.no_extras:
+        from qspace_gb300 import permute_dev, upload
+        from qspace_gb300.workloads import rank4_psi
+        psi_h = rank4_psi(seed=0, D=8192, complex_data=True)
+        nbytes = 16.0 * sum(x.size for x in psi_h.data)
+        tpsi = upload(psi_h, ctx)
+        del psi_h
+        permute = {"workload": "two-site wave function psi(L,s1,s2,R), U(1)xU(1), D=8192, complex128, "
+                               f"{nbytes / 1e6:.0f} MB", "bytes_per_call": 2 * nbytes, "rows": []}
+        _, hbm_pk, hbm_kind = measured_peaks()
+        for perm_, what in (([4, 2, 3, 1], "R,s1,s2,L: blocks transposed (shared-memory tiles)"),
+                            ([1, 4, 2, 3], "L,R,s1,s2: contiguous blocks (output-order lines)")):
+            permute_dev(tpsi, perm_).free()
+            ctx.sync()
+            ctx.set_timing(True)
+            kms, cms = [], []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                tp = permute_dev(tpsi, perm_)
+                kms.append(ctx.phase_ms()[0])
+                ctx.sync()
+                cms.append(1e3 * (time.perf_counter() - t0))
+                tp.free()
+            ctx.set_timing(False)
+            km = statistics.median(kms)
+            gbs = 2 * nbytes / (km * 1e-3) / 1e9
+            permute["rows"].append({"perm": perm_, "layout": what, "kernel_ms": km, "GB/s": gbs,
+                                    "frac_of_hbm": gbs / hbm_pk, "peak_kind": hbm_kind,
+                                    "call_ms": statistics.median(cms)})
+        tpsi.free()
+
     # ---- FP64 block eigendecompositions of one NRG step (abelian U(1)xU(1)
     # stand-in for the SU(2)xU(1) Wilson chain): every symmetry block of a
     # 39300-state Hamiltonian, 336 blocks of sizes 1..690, on the device;
@@ -618,7 +653,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "slices": slices, "rdm_latency": rdm, "eig": eig, "nrg": nrg, "serving": serving,
+                "slices": slices, "rdm_latency": rdm, "permute": permute, "eig": eig, "nrg": nrg, "serving": serving,
                 "clocks": ck}
         if shard_info is not None:
             line["shard"] = shard_info

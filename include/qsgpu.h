@@ -125,7 +125,8 @@ QS_EXPORT int64_t qs_ctx_launches(const qs_ctx *ctx);
  * contraction records CUDA events on the context stream around operand
  * preparation (digit slicing; empty for the FP64 path) and around the GEMM
  * kernel; qs_ctx_phase_ms waits for the most recent call and returns both
- * device times in milliseconds. */
+ * device times in milliseconds.  For qs_permuteQS / qs_permute_dev the first
+ * time is that of the permute kernels and the second is zero. */
 QS_EXPORT qs_status qs_ctx_set_timing(qs_ctx *ctx, int32_t enable);
 QS_EXPORT qs_status qs_ctx_phase_ms(qs_ctx *ctx, double *prep_ms, double *gemm_ms);
 

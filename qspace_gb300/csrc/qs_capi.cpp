@@ -135,24 +135,83 @@ void Ctx::destroy_copy_streams() {
   h2d = d2h = nullptr;
 }
 
-// Chunk tables for the permute kernel.
-static void run_permute(Ctx *ctx, const std::vector<PermDesc> &descs, const double *in, double *out,
-                        bool cplx) {
-  if (descs.empty()) return;
-  const int CH = 4096;
-  std::vector<int64_t> cb, cs;
-  for (size_t i = 0; i < descs.size(); ++i)
-    for (int64_t s = 0; s < descs[i].n; s += CH) {
-      cb.push_back((int64_t)i);
-      cs.push_back(s);
+// A block's permutation on its fewest legs: legs of size 1 dropped, and
+// output legs k, k+1 merged where they are also adjacent (and in order) in
+// the input.  The element order of input and output is unchanged.
+static PermDesc reduce_perm(const PermDesc &d) {
+  PermDesc r = d;
+  int n = 0;
+  for (int k = 0; k < d.rank; ++k) {
+    if (d.out_dims[k] == 1) continue;
+    if (n > 0 && r.in_stride[n - 1] * r.out_dims[n - 1] == d.in_stride[k]) {
+      r.out_dims[n - 1] *= d.out_dims[k];
+      continue;
     }
-  if (cb.empty()) return;
+    r.out_dims[n] = d.out_dims[k];
+    r.in_stride[n] = d.in_stride[k];
+    ++n;
+  }
+  if (n == 0) {  // a single element
+    r.out_dims[0] = 1;
+    r.in_stride[0] = 1;
+    n = 1;
+  }
+  for (int k = n; k < 8; ++k) {
+    r.out_dims[k] = 1;
+    r.in_stride[k] = 0;
+  }
+  r.rank = n;
+  r.fast_in_leg = -1;
+  for (int k = 0; k < n; ++k)
+    if (r.in_stride[k] == 1) r.fast_in_leg = k;
+  return r;
+}
+
+// Work lists of the permute kernels: blocks whose output-fastest leg differs
+// from the input-fastest one, both spanning >= 8 elements, go through 32 x 32
+// shared-memory tiles; the others through output-order lines.
+static void run_permute(Ctx *ctx, const std::vector<PermDesc> &descs_in, const double *in, double *out,
+                        bool cplx, bool timed = false) {
+  if (descs_in.empty()) return;
+  const int CH = 4096, TILE = 32, MIN_EDGE = 8;
+  std::vector<PermDesc> descs;
+  descs.reserve(descs_in.size());
+  std::vector<int64_t> cb, cs;
+  std::vector<PermTile> tiles;
+  for (size_t i = 0; i < descs_in.size(); ++i) {
+    if (descs_in[i].n <= 0) continue;
+    PermDesc d = reduce_perm(descs_in[i]);
+    const int b = d.fast_in_leg;
+    const int64_t di = (int64_t)descs.size();
+    if (b > 0 && d.out_dims[0] >= MIN_EDGE && d.out_dims[b] >= MIN_EDGE) {
+      const int64_t nt0 = (d.out_dims[0] + TILE - 1) / TILE, ntb = (d.out_dims[b] + TILE - 1) / TILE;
+      const int64_t nrest = d.n / (d.out_dims[0] * d.out_dims[b]);
+      for (int64_t rest = 0; rest < nrest; ++rest)
+        for (int64_t tj = 0; tj < ntb; ++tj)
+          for (int64_t ti = 0; ti < nt0; ++ti) tiles.push_back(PermTile{di, rest, (int32_t)ti, (int32_t)tj});
+    } else {
+      for (int64_t s0 = 0; s0 < d.n; s0 += CH) {
+        cb.push_back(di);
+        cs.push_back(s0);
+      }
+    }
+    descs.push_back(d);
+  }
+  if (descs.empty()) return;
   PermDesc *dd = dev_upload(ctx, descs);
-  int64_t *dcb = dev_upload(ctx, cb), *dcs = dev_upload(ctx, cs);
-  launch_permute(ctx, dd, dcb, dcs, (int64_t)cb.size(), in, out, cplx ? 1 : 0, CH);
+  int64_t *dcb = cb.empty() ? nullptr : dev_upload(ctx, cb);
+  int64_t *dcs = cs.empty() ? nullptr : dev_upload(ctx, cs);
+  PermTile *dt = tiles.empty() ? nullptr : dev_upload(ctx, tiles);
+  if (timed) ctx->mark(0);
+  launch_permute(ctx, dd, dcb, dcs, (int64_t)cb.size(), dt, (int64_t)tiles.size(), in, out, cplx ? 1 : 0, CH);
+  if (timed) {
+    ctx->mark(1);
+    ctx->mark(2);
+  }
   dev_free(ctx, dd);
-  dev_free(ctx, dcb);
-  dev_free(ctx, dcs);
+  if (dcb) dev_free(ctx, dcb);
+  if (dcs) dev_free(ctx, dcs);
+  if (dt) dev_free(ctx, dt);
 }
 
 // Rank-2 exemption of SkipZeroData (Source/QSpace.cc:3225-3229): zero blocks
@@ -1077,7 +1136,7 @@ static std::unique_ptr<qs_tensor> permute_core(Ctx *ctx, const QMeta &m, const d
   const int es = m.cplx ? 2 : 1;
   T->d = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(ne, 1) * es);
   std::vector<PermDesc> pd = make_perm_descs(m, P, conj && m.cplx, M.offs);
-  run_permute(ctx, pd, d, T->d, m.cplx);
+  run_permute(ctx, pd, d, T->d, m.cplx, true);
   return T;
 }
 

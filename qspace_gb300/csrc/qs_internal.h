@@ -122,13 +122,24 @@ struct PermDesc {
   int32_t conj;
   int64_t out_dims[8];
   int64_t in_stride[8]; // stride in the input of output leg k
+  int32_t fast_in_leg;  // output leg with input stride 1 (tiled blocks)
+  int32_t pad_;
+};
+
+// One 32 x 32 tile of a tiled block: tile (ti, tj) of (output leg 0,
+// output leg fast_in_leg) at linear index `rest` of the other legs.
+struct PermTile {
+  int64_t desc;
+  int64_t rest;
+  int32_t ti, tj;
 };
 
 // ------------------------------------------------------- kernel launchers
-// qs_permute.cu
+// qs_permute.cu: tiles through shared memory (ntiles items) and output-order
+// lines (nchunks chunks of chunk_elems elements); either list may be empty
 void launch_permute(Ctx *ctx, const PermDesc *d_desc, const int64_t *d_chunk_blk,
-                    const int64_t *d_chunk_start, int64_t nchunks, const double *in,
-                    double *out, int is_complex, int chunk_elems);
+                    const int64_t *d_chunk_start, int64_t nchunks, const PermTile *d_tiles, int64_t ntiles,
+                    const double *in, double *out, int is_complex, int chunk_elems);
 
 // qs_gemm_f64.cu -- plain FP64 grouped GEMM (deterministic: one CTA owns an
 // output tile, pairs summed in order)

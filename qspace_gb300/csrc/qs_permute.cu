@@ -1,12 +1,21 @@
-// Generalised transpose of many blocks in one launch (the device counterpart
-// of wbperm_helper::permute, Source/wbarray.cc:4453-4600, which QSpace runs
-// per block from permute_to / Permute, Source/QSpace.hh:2670-2866).
+// Generalised transpose of many blocks (the device counterpart of
+// wbperm_helper::permute, Source/wbarray.cc:4453-4600, which QSpace runs per
+// block from permute_to / Permute, Source/QSpace.hh:2670-2866).
 //
-// Work is cut into chunks of `chunk_elems` output elements; chunk c belongs to
-// block chunk_blk[c] and starts at output element chunk_start[c].  Each CTA
-// writes its chunk in output order (coalesced stores) and gathers the inputs
-// through the permuted strides.  When the permutation keeps the first leg in
-// place the gathers are unit-stride runs as well.
+// The host first drops legs of size 1 and merges legs that stay adjacent in
+// both orders, so every block is described by its fewest legs.  Two kernels
+// then cover all blocks of a call:
+//  * permute_tile_kernel -- blocks whose output-fastest leg is not the
+//    input-fastest one and where both of those legs span >= 8 elements: a
+//    32 x 32 tile of (input-fastest, output-fastest) moves through shared
+//    memory, read with lanes along the input's unit stride and written with
+//    lanes along the output's, so both sides are full coalesced lines
+//    (complex elements are single 16-byte accesses).  One CTA per tile; the
+//    remaining legs' offsets are decoded once per CTA.
+//  * permute_lines_kernel -- every other block (the fastest leg kept in
+//    place: contiguous runs on both sides; or short legs): each thread walks
+//    output elements in order; its multi-index advances by the mixed-radix
+//    digits of the CTA stride, so the inner loop has no division.
 #include <algorithm>
 
 #include "qs_internal.h"
@@ -14,48 +23,136 @@
 namespace qs {
 
 template <bool CPLX>
+struct PermElem {
+  using T = double;
+};
+template <>
+struct PermElem<true> {
+  using T = double2;
+};
+
+__device__ __forceinline__ double perm_conj(double v, int) { return v; }
+__device__ __forceinline__ double2 perm_conj(double2 v, int c) { return make_double2(v.x, c ? -v.y : v.y); }
+
+constexpr int PT = 32;       // tile edge
+constexpr int PT_ROWS = 8;   // warps per tile CTA
+
+template <bool CPLX>
+__global__ void __launch_bounds__(PT * PT_ROWS)
+permute_tile_kernel(const PermDesc *__restrict__ desc, const PermTile *__restrict__ tiles,
+                    const double *__restrict__ in_, double *__restrict__ out_) {
+  using T = typename PermElem<CPLX>::T;
+  __shared__ T tile[PT][PT + 1];
+  const PermTile w = tiles[blockIdx.x];
+  const PermDesc &d = desc[w.desc];
+  const T *in = reinterpret_cast<const T *>(in_) + d.in_off;
+  T *out = reinterpret_cast<T *>(out_) + d.out_off;
+  const int b = d.fast_in_leg;  // output leg that is the input's unit-stride leg
+  const int64_t n0 = d.out_dims[0], nb = d.out_dims[b];
+  // offsets of the other legs (decoded once per CTA)
+  int64_t rem = w.rest, ioff = 0, ooff = 0, ostride = 1, ob = 1;
+  for (int k = 0; k < d.rank; ++k) {
+    if (k == b) ob = ostride;
+    if (k != 0 && k != b) {
+      const int64_t j = rem % d.out_dims[k];
+      rem /= d.out_dims[k];
+      ioff += j * d.in_stride[k];
+      ooff += j * ostride;
+    }
+    ostride *= d.out_dims[k];
+  }
+  const int64_t s0 = d.in_stride[0];
+  const int64_t i0 = (int64_t)w.ti * PT, j0 = (int64_t)w.tj * PT;
+  const int lane = threadIdx.x, row = threadIdx.y;
+  // read: lanes along the input's unit-stride leg (output leg b)
+  if (j0 + lane < nb) {
+#pragma unroll
+    for (int r = row; r < PT; r += PT_ROWS)
+      if (i0 + r < n0) tile[r][lane] = in[ioff + (i0 + r) * s0 + j0 + lane];
+  }
+  __syncthreads();
+  // write: lanes along the output's unit-stride leg 0
+  if (i0 + lane < n0) {
+#pragma unroll
+    for (int r = row; r < PT; r += PT_ROWS)
+      if (j0 + r < nb) out[ooff + (j0 + r) * ob + i0 + lane] = perm_conj(tile[lane][r], d.conj);
+  }
+}
+
+template <bool CPLX>
 __global__ void __launch_bounds__(256)
-permute_kernel(const PermDesc *__restrict__ desc, const int64_t *__restrict__ chunk_blk,
-               const int64_t *__restrict__ chunk_start, int chunk_elems,
-               const double *__restrict__ in, double *__restrict__ out) {
+permute_lines_kernel(const PermDesc *__restrict__ desc, const int64_t *__restrict__ chunk_blk,
+                     const int64_t *__restrict__ chunk_start, int chunk_elems,
+                     const double *__restrict__ in_, double *__restrict__ out_) {
+  using T = typename PermElem<CPLX>::T;
   const int64_t c = blockIdx.x;
   const PermDesc &d = desc[chunk_blk[c]];
+  const T *in = reinterpret_cast<const T *>(in_) + d.in_off;
+  T *out = reinterpret_cast<T *>(out_) + d.out_off;
   const int64_t s0 = chunk_start[c];
   const int64_t s1 = min(d.n, s0 + (int64_t)chunk_elems);
   const int r = d.rank;
-  for (int64_t e = s0 + threadIdx.x; e < s1; e += blockDim.x) {
-    int64_t rem = e, src = 0;
+  int64_t e = s0 + threadIdx.x;
+  if (e >= s1) return;
+  // multi-index of e and the mixed-radix digits of the step blockDim.x
+  int64_t j[8], step[8], src = 0;
+  {
+    int64_t rem = e, st = blockDim.x;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       if (k < r) {
         const int64_t dk = d.out_dims[k];
-        const int64_t j = rem % dk;
+        j[k] = rem % dk;
         rem /= dk;
-        src += j * d.in_stride[k];
+        step[k] = st % dk;
+        st /= dk;
+        src += j[k] * d.in_stride[k];
+      } else {
+        j[k] = step[k] = 0;
       }
     }
-    if (CPLX) {
-      const double2 v = reinterpret_cast<const double2 *>(in)[d.in_off + src];
-      reinterpret_cast<double2 *>(out)[d.out_off + e] = make_double2(v.x, d.conj ? -v.y : v.y);
-    } else {
-      out[d.out_off + e] = in[d.in_off + src];
+  }
+  for (;;) {
+    out[e] = perm_conj(in[src], d.conj);
+    e += blockDim.x;
+    if (e >= s1) break;
+    // j += step with carries: every digit of the step is below its radix
+    int carry = 0;
+    src = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < r) {
+        int64_t v = j[k] + step[k] + carry;
+        carry = v >= d.out_dims[k];
+        if (carry) v -= d.out_dims[k];
+        j[k] = v;
+        src += v * d.in_stride[k];
+      }
     }
   }
 }
 
 void launch_permute(Ctx *ctx, const PermDesc *d_desc, const int64_t *d_chunk_blk,
-                    const int64_t *d_chunk_start, int64_t nchunks, const double *in,
-                    double *out, int is_complex, int chunk_elems) {
-  if (nchunks <= 0) return;
-  if (nchunks > 0x7fffffff) fail(QS_ERR_SHAPE, "permute: too many chunks");
-  dim3 grid((unsigned)nchunks);
-  if (is_complex)
-    permute_kernel<true><<<grid, 256, 0, ctx->stream>>>(d_desc, d_chunk_blk, d_chunk_start,
-                                                        chunk_elems, in, out);
-  else
-    permute_kernel<false><<<grid, 256, 0, ctx->stream>>>(d_desc, d_chunk_blk, d_chunk_start,
-                                                         chunk_elems, in, out);
-  QS_LAUNCHED(ctx);
+                    const int64_t *d_chunk_start, int64_t nchunks, const PermTile *d_tiles, int64_t ntiles,
+                    const double *in, double *out, int is_complex, int chunk_elems) {
+  if (nchunks > 0x7fffffff || ntiles > 0x7fffffff) fail(QS_ERR_SHAPE, "permute: too many work items");
+  if (ntiles > 0) {
+    const dim3 blk(PT, PT_ROWS);
+    if (is_complex)
+      permute_tile_kernel<true><<<(unsigned)ntiles, blk, 0, ctx->stream>>>(d_desc, d_tiles, in, out);
+    else
+      permute_tile_kernel<false><<<(unsigned)ntiles, blk, 0, ctx->stream>>>(d_desc, d_tiles, in, out);
+    QS_LAUNCHED(ctx);
+  }
+  if (nchunks > 0) {
+    if (is_complex)
+      permute_lines_kernel<true><<<(unsigned)nchunks, 256, 0, ctx->stream>>>(d_desc, d_chunk_blk, d_chunk_start,
+                                                                             chunk_elems, in, out);
+    else
+      permute_lines_kernel<false><<<(unsigned)nchunks, 256, 0, ctx->stream>>>(d_desc, d_chunk_blk, d_chunk_start,
+                                                                              chunk_elems, in, out);
+    QS_LAUNCHED(ctx);
+  }
 }
 
 // Real -> complex widening of an arena (operands of mixed real/complex

@@ -60,6 +60,33 @@ def mps_site_tensor(seed: int = 0, D: int = 512, complex_data: bool = False) -> 
     return QSpace(Q, data, {"itags": ["L", "s", "R*"]})
 
 
+def rank4_psi(seed: int = 0, D: int = 512, complex_data: bool = False) -> QSpace:
+    """Two-site wave function psi(L, s1, s2, R) of the U(1)xU(1) chain: the
+    bonds of ``mps_site_tensor`` (bond dimension D), two local fermion sites;
+    a block for every (L, s1, s2) whose fused label is a sector of R, N(0,1)
+    entries."""
+    rng = np.random.default_rng(seed)
+    L = bond_sectors(rng, D)
+    R = bond_sectors(rng, D)
+    rmap = {(q, s): d for q, s, d in R}
+    Q = [[], [], [], []]
+    data = []
+    for (ql, sl, dl) in L:
+        for (q1, s1) in LOCAL_FERMION_SITE:
+            for (q2, s2) in LOCAL_FERMION_SITE:
+                key = (ql + q1 + q2, sl + s1 + s2)
+                if key not in rmap:
+                    continue
+                dr = rmap[key]
+                for k, lab in enumerate(((ql, sl), (q1, s1), (q2, s2), key)):
+                    Q[k].append(lab)
+                blk = rng.standard_normal((dl, 1, 1, dr))
+                if complex_data:
+                    blk = blk + 1j * rng.standard_normal((dl, 1, 1, dr))
+                data.append(blk)
+    return QSpace([np.asarray(q, np.int32) for q in Q], data, {"itags": ["L", "s1", "s2", "R*"]})
+
+
 def grouped_pairs(seed: int = 0, npairs: int = 2000, lo: int = 8, hi: int = 1024,
                   complex_data: bool = True):
     """Returns dict with M, N, K, afac arrays and lists of A (MxK), B (KxN)."""
