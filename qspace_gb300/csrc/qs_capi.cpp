@@ -168,12 +168,12 @@ static PermDesc reduce_perm(const PermDesc &d) {
 }
 
 // Work lists of the permute kernels: blocks whose output-fastest leg differs
-// from the input-fastest one, both spanning >= 8 elements, go through 32 x 32
+// from the input-fastest one, both spanning >= 8 elements, go through 64 x 32
 // shared-memory tiles; the others through output-order lines.
 static void run_permute(Ctx *ctx, const std::vector<PermDesc> &descs_in, const double *in, double *out,
                         bool cplx, bool timed = false) {
   if (descs_in.empty()) return;
-  const int CH = 4096, TILE = 32, MIN_EDGE = 8;
+  const int CH = 8192, TILE_I = 64, TILE_J = 32, MIN_EDGE = 8;
   std::vector<PermDesc> descs;
   descs.reserve(descs_in.size());
   std::vector<int64_t> cb, cs;
@@ -184,7 +184,7 @@ static void run_permute(Ctx *ctx, const std::vector<PermDesc> &descs_in, const d
     const int b = d.fast_in_leg;
     const int64_t di = (int64_t)descs.size();
     if (b > 0 && d.out_dims[0] >= MIN_EDGE && d.out_dims[b] >= MIN_EDGE) {
-      const int64_t nt0 = (d.out_dims[0] + TILE - 1) / TILE, ntb = (d.out_dims[b] + TILE - 1) / TILE;
+      const int64_t nt0 = (d.out_dims[0] + TILE_I - 1) / TILE_I, ntb = (d.out_dims[b] + TILE_J - 1) / TILE_J;
       const int64_t nrest = d.n / (d.out_dims[0] * d.out_dims[b]);
       for (int64_t rest = 0; rest < nrest; ++rest)
         for (int64_t tj = 0; tj < ntb; ++tj)

@@ -7,15 +7,17 @@
 // then cover all blocks of a call:
 //  * permute_tile_kernel -- blocks whose output-fastest leg is not the
 //    input-fastest one and where both of those legs span >= 8 elements: a
-//    32 x 32 tile of (input-fastest, output-fastest) moves through shared
+//    64 x 32 tile of (output-fastest, input-fastest) moves through shared
 //    memory, read with lanes along the input's unit stride and written with
 //    lanes along the output's, so both sides are full coalesced lines
-//    (complex elements are single 16-byte accesses).  One CTA per tile; the
-//    remaining legs' offsets are decoded once per CTA.
+//    (complex elements are single 16-byte accesses; eight loads in flight
+//    per thread).  One CTA per tile; the remaining legs' offsets are decoded
+//    once per CTA.
 //  * permute_lines_kernel -- every other block (the fastest leg kept in
 //    place: contiguous runs on both sides; or short legs): each thread walks
-//    output elements in order; its multi-index advances by the mixed-radix
-//    digits of the CTA stride, so the inner loop has no division.
+//    output elements in order, four loads in flight; its multi-index
+//    advances by the mixed-radix digits of the CTA stride, so the inner loop
+//    has no division.  A block that is one contiguous run is a plain copy.
 #include <algorithm>
 
 #include "qs_internal.h"
@@ -34,7 +36,8 @@ struct PermElem<true> {
 __device__ __forceinline__ double perm_conj(double v, int) { return v; }
 __device__ __forceinline__ double2 perm_conj(double2 v, int c) { return make_double2(v.x, c ? -v.y : v.y); }
 
-constexpr int PT = 32;       // tile edge
+constexpr int PT = 32;       // tile edge along the input's unit-stride leg
+constexpr int PTI = 64;      // tile edge along the output's unit-stride leg
 constexpr int PT_ROWS = 8;   // warps per tile CTA
 
 template <bool CPLX>
@@ -42,7 +45,7 @@ __global__ void __launch_bounds__(PT * PT_ROWS)
 permute_tile_kernel(const PermDesc *__restrict__ desc, const PermTile *__restrict__ tiles,
                     const double *__restrict__ in_, double *__restrict__ out_) {
   using T = typename PermElem<CPLX>::T;
-  __shared__ T tile[PT][PT + 1];
+  __shared__ T tile[PTI][PT + 1];
   const PermTile w = tiles[blockIdx.x];
   const PermDesc &d = desc[w.desc];
   const T *in = reinterpret_cast<const T *>(in_) + d.in_off;
@@ -62,20 +65,30 @@ permute_tile_kernel(const PermDesc *__restrict__ desc, const PermTile *__restric
     ostride *= d.out_dims[k];
   }
   const int64_t s0 = d.in_stride[0];
-  const int64_t i0 = (int64_t)w.ti * PT, j0 = (int64_t)w.tj * PT;
+  const int64_t i0 = (int64_t)w.ti * PTI, j0 = (int64_t)w.tj * PT;
   const int lane = threadIdx.x, row = threadIdx.y;
-  // read: lanes along the input's unit-stride leg (output leg b)
+  // read: lanes along the input's unit-stride leg (output leg b); all eight
+  // loads of a thread are issued before the first use
   if (j0 + lane < nb) {
+    T v[PTI / PT_ROWS];
 #pragma unroll
-    for (int r = row; r < PT; r += PT_ROWS)
-      if (i0 + r < n0) tile[r][lane] = in[ioff + (i0 + r) * s0 + j0 + lane];
+    for (int u = 0; u < PTI / PT_ROWS; ++u) {
+      const int r = row + u * PT_ROWS;
+      if (i0 + r < n0) v[u] = in[ioff + (i0 + r) * s0 + j0 + lane];
+    }
+#pragma unroll
+    for (int u = 0; u < PTI / PT_ROWS; ++u) tile[row + u * PT_ROWS][lane] = v[u];
   }
   __syncthreads();
-  // write: lanes along the output's unit-stride leg 0
-  if (i0 + lane < n0) {
+  // write: lanes along the output's unit-stride leg 0, two 32-wide halves
 #pragma unroll
-    for (int r = row; r < PT; r += PT_ROWS)
-      if (j0 + r < nb) out[ooff + (j0 + r) * ob + i0 + lane] = perm_conj(tile[lane][r], d.conj);
+  for (int h = 0; h < PTI / PT; ++h) {
+    const int il = h * PT + lane;
+    if (i0 + il < n0) {
+#pragma unroll
+      for (int r = row; r < PT; r += PT_ROWS)
+        if (j0 + r < nb) out[ooff + (j0 + r) * ob + i0 + il] = perm_conj(tile[il][r], d.conj);
+    }
   }
 }
 
@@ -85,6 +98,7 @@ permute_lines_kernel(const PermDesc *__restrict__ desc, const int64_t *__restric
                      const int64_t *__restrict__ chunk_start, int chunk_elems,
                      const double *__restrict__ in_, double *__restrict__ out_) {
   using T = typename PermElem<CPLX>::T;
+  constexpr int U = 4;  // elements in flight per thread
   const int64_t c = blockIdx.x;
   const PermDesc &d = desc[chunk_blk[c]];
   const T *in = reinterpret_cast<const T *>(in_) + d.in_off;
@@ -94,6 +108,19 @@ permute_lines_kernel(const PermDesc *__restrict__ desc, const int64_t *__restric
   const int r = d.rank;
   int64_t e = s0 + threadIdx.x;
   if (e >= s1) return;
+  if (r == 1 && d.in_stride[0] == 1) {
+    // one contiguous run: a plain copy
+    for (; e < s1; e += (int64_t)U * blockDim.x) {
+      T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (e + u * blockDim.x < s1) v[u] = in[e + u * blockDim.x];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (e + u * blockDim.x < s1) out[e + u * blockDim.x] = perm_conj(v[u], d.conj);
+    }
+    return;
+  }
   // multi-index of e and the mixed-radix digits of the step blockDim.x
   int64_t j[8], step[8], src = 0;
   {
@@ -112,23 +139,38 @@ permute_lines_kernel(const PermDesc *__restrict__ desc, const int64_t *__restric
       }
     }
   }
-  for (;;) {
-    out[e] = perm_conj(in[src], d.conj);
-    e += blockDim.x;
-    if (e >= s1) break;
-    // j += step with carries: every digit of the step is below its radix
-    int carry = 0;
-    src = 0;
+  while (e < s1) {
+    // source offsets of the next U elements of this thread, then their loads
+    int64_t srcs[U];
+    int n = 0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (k < r) {
-        int64_t v = j[k] + step[k] + carry;
-        carry = v >= d.out_dims[k];
-        if (carry) v -= d.out_dims[k];
-        j[k] = v;
-        src += v * d.in_stride[k];
+    for (int u = 0; u < U; ++u) {
+      if (e + (int64_t)u * blockDim.x < s1) {
+        srcs[u] = src;
+        n = u + 1;
+        // j += step with carries: every digit of the step is below its radix
+        int carry = 0;
+        src = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (k < r) {
+            int64_t v = j[k] + step[k] + carry;
+            carry = v >= d.out_dims[k];
+            if (carry) v -= d.out_dims[k];
+            j[k] = v;
+            src += v * d.in_stride[k];
+          }
+        }
       }
     }
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (u < n) v[u] = in[srcs[u]];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (u < n) out[e + (int64_t)u * blockDim.x] = perm_conj(v[u], d.conj);
+    e += (int64_t)U * blockDim.x;
   }
 }
 
