@@ -69,10 +69,6 @@ constexpr int KCM = TKS / 8;      // core matrices along K in a digit tile
 constexpr int A_DIGIT_BYTES = TMS * TKS * 2;  // 8 KB
 constexpr int B_DIGIT_BYTES = TNS * TKS * 2;  // 2 KB
 constexpr int MAX_STAGES = 8;
-// slicing threads per digit tile: one per (row, core matrix along K); a
-// complex task cuts one complex row into the two real rows of A~
-constexpr int SLICE_A_THREADS_R = TMS * KCM < 256 ? TMS * KCM : 256, SLICE_A_THREADS_C = TMS / 2 * KCM,
-              SLICE_B_THREADS = TNS * KCM;
 constexpr int EMPTY_EXP = -30000;
 constexpr int SMEM_HDR = 2048;   // barriers, TMEM slot, abort flag; tile-descriptor slots at 1024
 constexpr int SMEM_LIMIT = 227 * 1024;
@@ -215,348 +211,310 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// --------------------------------------------------------- exponent passes
-// Records the exponent key of one line (row m of op(A) or column m of op(B),
-// max over Re and Im for complex data) for every real line it becomes: rows
-// 2m, 2m+1 of A~ (A-duplicated form) or columns 2m, 2m+1 of B' (B-duplicated
-// form), else the one line m.  Row exponents include the CG factor's.
-template <bool CPLX>
-__device__ __forceinline__ void put_line_exp(const SplitPair &P, bool role_b, int m, int key, int *__restrict__ E,
-                                             int *__restrict__ F) {
-  const bool two = CPLX && (role_b ? P.dupb != 0 : P.dupb == 0);
-  int *dst = role_b ? F + P.foff : E + P.eoff;
-  const int e = key - 1022 + (role_b ? 0 : P.e_afac);
-  if (two) {
-    atomicMax(&dst[2 * m], e);
-    atomicMax(&dst[2 * m + 1], e);
-  } else {
-    atomicMax(&dst[m], e);
-  }
-}
+// ---------------------------------------------- exponents and slicing, fused
+// One CTA per strip of STRIP real lines of one output block: rows of op(A~)
+// (A role) or columns of op(B~) (B role), over every pair of the block and
+// its whole depth.
+//  Phase 1: the exponent of each line of the strip -- the largest exponent
+//    key over all pairs and all k (both parts of a complex element), plus the
+//    pair's CG-factor exponent for the A role -- kept in shared memory and
+//    written to E / F for the epilogue (every line belongs to one strip, so
+//    plain stores).  A line of zeros keeps EMPTY_EXP.
+//  Phase 2: the digits of the strip's lines for every pair and k-block,
+//    written into the pre-tiled digit arena.  It re-reads what phase 1 has
+//    just read: a strip holds at most STRIP lines of the block's depth, so
+//    the re-read is mostly served from L2 and the FP64 operands cross HBM
+//    once.
+// A complex block in the A-duplicated form turns each row m of op(A) into
+// the real rows 2m, 2m+1 of A~ (rows (Re, -Im) and (Im, Re) along k) and
+// each column of op(B) into one column of B~ (rows 2k, 2k+1 = (Re, Im));
+// in the B-duplicated form row m of op(A) is one row of A' ((Re, Im) along
+// k) and column n of op(B) the columns 2n, 2n+1 of B' ((Re; -Im), (Im; Re)).
+constexpr int STRIP = 16;          // real lines per strip (two core-matrix groups)
+constexpr int STRIP_THREADS = 128;
 
-// Exponents of lines strided along k: rows of a plain op(A~) (ROLE_B =
-// false) or columns of a transposed op(B~) (ROLE_B = true); per output
-// block, max over its pairs.  A block of 256 threads covers lines
-// [m0, m0 + min(256, lines - m0)) and depths [k0, k1): R threads per depth
-// phase (R a power of two >= the line count), 256 / R phases splitting the
-// depth, so short blocks keep every thread loading and neighbouring threads
-// read neighbouring elements.  Deep operands are split into several tasks
-// along k (maxima combine atomically).
+// Phase 1 for the lines l0 .. l0+nl-1 of op(X) (X = A role: rows, line m at
+// m + k*ld (contig: k + m*ld); X = B role: columns, line n at k + n*ld
+// (contig) or n + k*ld), max over the pairs p0..p1-1 into smax[line].
 template <bool CPLX, bool ROLE_B>
-__global__ void __launch_bounds__(256)
-exp_lines_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-                 const double *__restrict__ Aarena, const double *__restrict__ Barena, int *__restrict__ E,
-                 int *__restrict__ F) {
-  __shared__ int keys[256];
-  const int4 tk = tasks[blockIdx.x];  // (pair, m0, k0, k1)
-  const SplitPair P = pairs[tk.x];
-  // a swapped pair's roles read the other arena
-  const double *__restrict__ A = (ROLE_B != (P.swap != 0)) ? Barena : Aarena;
-  const int rows = min((ROLE_B ? P.N : P.M) - tk.y, 256);
-  int R = 1;
-  while (R < rows) R <<= 1;
-  const int KS = 256 / R;
-  const int r = threadIdx.x % R, ph = threadIdx.x / R;
-  const int m = tk.y + r;
-  const int64_t sk = ROLE_B ? P.ldb : P.lda, base = (ROLE_B ? P.b_off : P.a_off) + (int64_t)m;
-  int key = 0;
-  if (r < rows) {
-    int k = tk.z + ph;
-    // four independent loads in flight per thread
-    for (; k + 3 * KS < tk.w; k += 4 * KS) {
-      if (CPLX) {
-        const double2 *a = reinterpret_cast<const double2 *>(A) + base;
-        const double2 v0 = a[(int64_t)k * sk], v1 = a[(int64_t)(k + KS) * sk], v2 = a[(int64_t)(k + 2 * KS) * sk],
-                      v3 = a[(int64_t)(k + 3 * KS) * sk];
-        key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
-                           max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
-      } else {
-        const double *a = A + base;
-        key = max(key, max(max(exp_key(a[(int64_t)k * sk]), exp_key(a[(int64_t)(k + KS) * sk])),
-                           max(exp_key(a[(int64_t)(k + 2 * KS) * sk]), exp_key(a[(int64_t)(k + 3 * KS) * sk]))));
+__device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs, int p0, int p1, int l0, int nl,
+                                             const double *__restrict__ Aarena, const double *__restrict__ Barena,
+                                             int *smax) {
+  if (threadIdx.x < STRIP) smax[threadIdx.x] = EMPTY_EXP;
+  __syncthreads();
+  for (int p = p0; p < p1; ++p) {
+    const SplitPair &P = pairs[p];
+    // a swapped pair's roles read the other arena
+    const double *__restrict__ X = (ROLE_B != (P.swap != 0)) ? Barena : Aarena;
+    const int64_t off = ROLE_B ? P.b_off : P.a_off;
+    const int64_t ld = ROLE_B ? P.ldb : P.lda;
+    // lines contiguous along k: rows of a transposed op(A), columns of a plain op(B)
+    const bool contig = ROLE_B ? !(P.trans & 2) : (P.trans & 1);
+    constexpr int NPH = STRIP_THREADS / STRIP;
+    const int line = contig ? threadIdx.x / NPH : threadIdx.x % STRIP;
+    const int ph = contig ? threadIdx.x % NPH : threadIdx.x / STRIP;
+    int key = 0;
+    if (line < nl) {
+      const int64_t m = l0 + line;
+      const int64_t sk = contig ? 1 : ld, base = off + (contig ? m * ld : m);
+      int k = ph;
+      for (; k + 3 * NPH < P.K; k += 4 * NPH) {
+        if (CPLX) {
+          const double2 *x = reinterpret_cast<const double2 *>(X) + base;
+          const double2 v0 = x[k * sk], v1 = x[(k + NPH) * sk], v2 = x[(k + 2 * NPH) * sk],
+                        v3 = x[(k + 3 * NPH) * sk];
+          key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
+                             max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
+        } else {
+          const double *x = X + base;
+          key = max(key, max(max(exp_key(x[k * sk]), exp_key(x[(k + NPH) * sk])),
+                             max(exp_key(x[(k + 2 * NPH) * sk]), exp_key(x[(k + 3 * NPH) * sk]))));
+        }
+      }
+      for (; k < P.K; k += NPH) {
+        if (CPLX) {
+          const double2 v = reinterpret_cast<const double2 *>(X)[base + k * sk];
+          key = max(key, max(exp_key(v.x), exp_key(v.y)));
+        } else {
+          key = max(key, exp_key(X[base + k * sk]));
+        }
       }
     }
-    for (; k < tk.w; k += KS) {
-      if (CPLX) {
-        const double2 v = reinterpret_cast<const double2 *>(A)[base + (int64_t)k * sk];
-        key = max(key, max(exp_key(v.x), exp_key(v.y)));
-      } else {
-        key = max(key, exp_key(A[base + (int64_t)k * sk]));
-      }
-    }
+    if (key) atomicMax(&smax[line], key - 1022 + (ROLE_B ? 0 : P.e_afac));
   }
-  if (KS > 1) {
-    keys[threadIdx.x] = key;
-    __syncthreads();
-    if (ph != 0) return;
-    for (int p = 1; p < KS; ++p) key = max(key, keys[p * R + r]);
-  }
-  if (r >= rows || !key) return;
-  put_line_exp<CPLX>(P, ROLE_B, m, key, E, F);
+  __syncthreads();
 }
 
-// Same maxima for lines stored contiguously along k (rows of a transposed
-// op(A), columns of a plain op(B)): one warp per line, lanes stride over k
-// (coalesced), warp max reduction.  Task = (pair, first line, role 0 = A
-// rows / 1 = B columns); 8 lines per CTA.
-template <bool CPLX>
-__global__ void __launch_bounds__(256)
-exp_contig_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-                  const double *__restrict__ A, const double *__restrict__ B, int *__restrict__ E,
-                  int *__restrict__ F) {
-  const int4 tk = tasks[blockIdx.x];
-  const SplitPair P = pairs[tk.x];
-  const int lane = threadIdx.x & 31;
-  const int line = tk.y + (threadIdx.x >> 5);
-  const bool rowsA = tk.z == 0;
-  if (line >= (rowsA ? P.M : P.N)) return;
-  const double *base = (rowsA != (P.swap != 0)) ? A : B;  // a swapped pair's roles read the other arena
-  const int64_t off = rowsA ? P.a_off + (int64_t)line * P.lda : P.b_off + (int64_t)line * P.ldb;
-  int key = 0;
-  for (int k = lane; k < P.K; k += 32) {
-    if (CPLX) {
-      const double2 v = reinterpret_cast<const double2 *>(base)[off + k];
-      key = max(key, max(exp_key(v.x), exp_key(v.y)));
-    } else {
-      key = max(key, exp_key(base[off + k]));
-    }
-  }
-  key = __reduce_max_sync(0xffffffffu, key);
-  if (lane != 0 || !key) return;
-  put_line_exp<CPLX>(P, !rowsA, line, key, E, F);
-}
-
-__global__ void fill_int_kernel(int *p, int64_t n, int v) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = v;
-}
-
-// ------------------------------------------------------------ slicing
-// A~ digit tile (mt, kb): 128 rows x TKS k, core matrix (row group g, k core c)
-// at byte ((g*KCM + c)*128), row r%8 at +16*(r%8), k%8 at +2*(k%8).
+// A role.  Task = (first pair, end pair, first real row r0 of the strip).
 template <bool CPLX, int S, int B>
-__device__ __forceinline__ void slice_a_tile(const SplitPair &P, int mt, int kb, const double *__restrict__ A,
-                                             const int *__restrict__ E, uint8_t *__restrict__ tile) {
-  const bool ta = P.trans & 1, ca = P.trans & 4;
-  const Factor Fa{P.fm, P.fe, P.fneg != 0};
-  if constexpr (CPLX) {
-    if (P.dupb) {
-      // B-duplicated form: real row m of A' holds (Re, Im) of row m of op(A)
-      // along k; one task = one row x 4 complex k
-      for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
-        const int r = w % TMS, q = w / TMS;
-        const int m = mt * TMS + r;
-        if (m >= P.M) continue;  // feeds discarded outputs only: not written
-        const int Ei = E[P.eoff + m];
-        uint32_t pk[S][4];
+__device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int4 tk,
+                                        const double *__restrict__ Aarena, const double *__restrict__ Barena,
+                                        int *__restrict__ E, uint8_t *__restrict__ arena) {
+  __shared__ int smax[STRIP];
+  const int p0 = tk.x, p1 = tk.y, r0 = tk.z;
+  const SplitPair &Q = pairs[p0];
+  const bool dup = CPLX && Q.dupb == 0;  // two real rows per row of op(A)
+  const int l0 = dup ? r0 / 2 : r0;
+  const int nl = min(dup ? STRIP / 2 : STRIP, Q.M - l0);
+  strip_maxima<CPLX, false>(pairs, p0, p1, l0, nl, Aarena, Barena, smax);
+  if (threadIdx.x < nl) {
+    const int e = smax[threadIdx.x];
+    if (dup) {
+      E[Q.eoff + 2 * (l0 + threadIdx.x)] = e;
+      E[Q.eoff + 2 * (l0 + threadIdx.x) + 1] = e;
+    } else {
+      E[Q.eoff + l0 + threadIdx.x] = e;
+    }
+  }
+  const int mt = r0 / TMS, rl = r0 % TMS;
+  for (int p = p0; p < p1; ++p) {
+    const SplitPair &P = pairs[p];
+    const double *__restrict__ A = P.swap ? Barena : Aarena;
+    const bool ta = P.trans & 1, ca = P.trans & 4;
+    const Factor Fa{P.fm, P.fe, P.fneg != 0};
+    uint8_t *tiles = arena + P.as_off + (int64_t)mt * P.KB * S * A_DIGIT_BYTES;
+    if (dup) {
+      // item = one row of op(A) (real rows 2m, 2m+1) x 4 complex k
+      const int items = (STRIP / 2) * KCM * P.KB;
+      for (int w = threadIdx.x; w < items; w += blockDim.x) {
+        const int kb = w / ((STRIP / 2) * KCM), i = w % ((STRIP / 2) * KCM);
+        const int ml = i % (STRIP / 2), q = i / (STRIP / 2);
+        if (ml >= nl) continue;  // rows past the block feed discarded outputs only: not written
+        const int64_t m = l0 + ml;
+        const int Ei = smax[ml];
+        double2 a[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int k = (kb * TKS + q * 8) / 2 + j;
-          double re = 0.0, im = 0.0;
-          if (k < P.K) {
-            const double2 a = reinterpret_cast<const double2 *>(A)[
-                P.a_off + (ta ? (int64_t)k + (int64_t)m * P.lda : (int64_t)m + (int64_t)k * P.lda)];
-            re = a.x;
-            im = ca ? -a.y : a.y;
-          }
-          float dr[S], di[S];
-          digits_f<S, B>(scaled_int(re, Ei, B * S, Fa), dr);
-          digits_f<S, B>(scaled_int(im, Ei, B * S, Fa), di);
-#pragma unroll
-          for (int t = 0; t < S; ++t) pk[t][j] = pack2(dr[t], di[t]);
+          a[j] = make_double2(0.0, 0.0);
+          if (k < P.K)
+            a[j] = reinterpret_cast<const double2 *>(A)[P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda)];
         }
-        uint8_t *dst = tile + ((r >> 3) * KCM + q) * 128 + (r & 7) * 16;
+        uint32_t p0w[S][4], p1w[S][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float dr[S], di[S];
+          digits_f<S, B>(scaled_int(a[j].x, Ei, B * S, Fa), dr);
+          digits_f<S, B>(scaled_int(ca ? -a[j].y : a[j].y, Ei, B * S, Fa), di);
+#pragma unroll
+          for (int t = 0; t < S; ++t) {
+            p0w[t][j] = pack2(dr[t], -di[t]);  // ( re, -im )
+            p1w[t][j] = pack2(di[t], dr[t]);   // ( im,  re )
+          }
+        }
+        const int rr0 = rl + 2 * ml, rr1 = rr0 + 1;
+        uint8_t *tile = tiles + (int64_t)kb * S * A_DIGIT_BYTES;
+        uint8_t *d0 = tile + ((rr0 >> 3) * KCM + q) * 128 + (rr0 & 7) * 16;
+        uint8_t *d1 = tile + ((rr1 >> 3) * KCM + q) * 128 + (rr1 & 7) * 16;
+#pragma unroll
+        for (int t = 0; t < S; ++t) {
+          *reinterpret_cast<uint4 *>(d0 + t * A_DIGIT_BYTES) = make_uint4(p0w[t][0], p0w[t][1], p0w[t][2], p0w[t][3]);
+          *reinterpret_cast<uint4 *>(d1 + t * A_DIGIT_BYTES) = make_uint4(p1w[t][0], p1w[t][1], p1w[t][2], p1w[t][3]);
+        }
+      }
+    } else {
+      // item = one real row x 8 real k (4 complex k of the B-duplicated form)
+      const int items = STRIP * KCM * P.KB;
+      for (int w = threadIdx.x; w < items; w += blockDim.x) {
+        const int kb = w / (STRIP * KCM), i = w % (STRIP * KCM);
+        const int rloc = i % STRIP, q = i / STRIP;
+        if (rloc >= nl) continue;
+        const int64_t m = l0 + rloc;
+        const int Ei = smax[rloc];
+        uint32_t pk[S][4];
+        if constexpr (CPLX) {
+          double2 a[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int k = (kb * TKS + q * 8) / 2 + j;
+            a[j] = make_double2(0.0, 0.0);
+            if (k < P.K)
+              a[j] = reinterpret_cast<const double2 *>(A)[P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda)];
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            float dr[S], di[S];
+            digits_f<S, B>(scaled_int(a[j].x, Ei, B * S, Fa), dr);
+            digits_f<S, B>(scaled_int(ca ? -a[j].y : a[j].y, Ei, B * S, Fa), di);
+#pragma unroll
+            for (int t = 0; t < S; ++t) pk[t][j] = pack2(dr[t], di[t]);
+          }
+        } else {
+          double v[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            const int kk = kb * TKS + q * 8 + e;
+            v[e] = 0.0;
+            if (kk < P.Kr) v[e] = A[P.a_off + (ta ? (int64_t)kk + m * P.lda : m + (int64_t)kk * P.lda)];
+          }
+#pragma unroll
+          for (int e = 0; e < 8; e += 2) {
+            float d0[S], d1[S];
+            digits_f<S, B>(scaled_int(v[e], Ei, B * S, Fa), d0);
+            digits_f<S, B>(scaled_int(v[e + 1], Ei, B * S, Fa), d1);
+#pragma unroll
+            for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(d0[t], d1[t]);
+          }
+        }
+        const int rr = rl + rloc;
+        uint8_t *dst = tiles + (int64_t)kb * S * A_DIGIT_BYTES + ((rr >> 3) * KCM + q) * 128 + (rr & 7) * 16;
 #pragma unroll
         for (int t = 0; t < S; ++t)
           *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
       }
-      return;
-    }
-    // one task = one complex row m (real rows 2m, 2m+1 of A~) x 4 complex k:
-    // the digits of re and im are cut once and placed as
-    //   row 2m:   ( re, -im )    row 2m+1: ( im, re )
-    for (int w = threadIdx.x; w < (TMS / 2) * (TKS / 8); w += blockDim.x) {
-      const int ml = w % (TMS / 2), q = w / (TMS / 2);
-      const int m = mt * (TMS / 2) + ml;
-      // rows past the block only feed outputs the epilogue discards: not written
-      if (m >= P.M) continue;
-      const bool rv = true;
-      const int Ei = E[P.eoff + 2 * m];
-      uint32_t p0[S][4], p1[S][4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int k = (kb * TKS + q * 8) / 2 + j;
-        double re = 0.0, im = 0.0;
-        if (rv && k < P.K) {
-          const double2 a = reinterpret_cast<const double2 *>(A)[
-              P.a_off + (ta ? (int64_t)k + (int64_t)m * P.lda : (int64_t)m + (int64_t)k * P.lda)];
-          re = a.x;
-          im = ca ? -a.y : a.y;
-        }
-        float dr[S], di[S];
-        digits_f<S, B>(scaled_int(re, Ei, B * S, Fa), dr);
-        digits_f<S, B>(scaled_int(im, Ei, B * S, Fa), di);
-#pragma unroll
-        for (int t = 0; t < S; ++t) {
-          p0[t][j] = pack2(dr[t], -di[t]);  // ( re, -im )
-          p1[t][j] = pack2(di[t], dr[t]);   // ( im,  re )
-        }
-      }
-      const int r0 = 2 * ml, r1 = r0 + 1;
-      uint8_t *d0 = tile + ((r0 >> 3) * KCM + q) * 128 + (r0 & 7) * 16;
-      uint8_t *d1 = tile + ((r1 >> 3) * KCM + q) * 128 + (r1 & 7) * 16;
-#pragma unroll
-      for (int t = 0; t < S; ++t) {
-        *reinterpret_cast<uint4 *>(d0 + t * A_DIGIT_BYTES) = make_uint4(p0[t][0], p0[t][1], p0[t][2], p0[t][3]);
-        *reinterpret_cast<uint4 *>(d1 + t * A_DIGIT_BYTES) = make_uint4(p1[t][0], p1[t][1], p1[t][2], p1[t][3]);
-      }
-    }
-  } else {
-    for (int w = threadIdx.x; w < TMS * (TKS / 8); w += blockDim.x) {
-      const int r = w % TMS, q = w / TMS;
-      const int rr = mt * TMS + r;
-      if (rr >= P.Mr) continue;  // feeds discarded outputs only: not written
-      const bool rv = true;
-      const int Ei = E[P.eoff + rr];
-      uint32_t pk[S][4];
-#pragma unroll
-      for (int e = 0; e < 8; e += 2) {
-        float dd[2][S];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int kk = kb * TKS + q * 8 + e + h;
-          double v = 0.0;
-          if (rv && kk < P.Kr)
-            v = A[P.a_off + (ta ? (int64_t)kk + (int64_t)rr * P.lda : (int64_t)rr + (int64_t)kk * P.lda)];
-          digits_f<S, B>(scaled_int(v, Ei, B * S, Fa), dd[h]);
-        }
-#pragma unroll
-        for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(dd[0][t], dd[1][t]);
-      }
-      uint8_t *dst = tile + ((r >> 3) * KCM + q) * 128 + (r & 7) * 16;
-#pragma unroll
-      for (int t = 0; t < S; ++t)
-        *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
     }
   }
 }
 
-template <bool CPLX, int S>
-__global__ void __launch_bounds__(256)
-slice_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-               const double *__restrict__ Aarena, const double *__restrict__ Barena, const int *__restrict__ E,
-               uint8_t *__restrict__ arena, int b) {
-  const int4 tk = tasks[blockIdx.x];  // (pair, mt, kb, -)
-  const SplitPair P = pairs[tk.x];
-  const double *__restrict__ A = P.swap ? Barena : Aarena;
-  uint8_t *tile = arena + P.as_off + ((int64_t)(tk.y * P.KB + tk.z) * S) * A_DIGIT_BYTES;
-  switch (b) {  // the host admits b = 5..8 only
-    case 5: slice_a_tile<CPLX, S, 5>(P, tk.y, tk.z, A, E, tile); break;
-    case 6: slice_a_tile<CPLX, S, 6>(P, tk.y, tk.z, A, E, tile); break;
-    case 7: slice_a_tile<CPLX, S, 7>(P, tk.y, tk.z, A, E, tile); break;
-    default: slice_a_tile<CPLX, S, 8>(P, tk.y, tk.z, A, E, tile); break;
-  }
-}
-
-// B~ digit tile (nt, kb): 32 columns x TKS k, the same core-matrix layout
-// with the column index in the role of the row.
+// B role.  Task = (first pair, end pair, first real column c0 of the strip).
 template <bool CPLX, int S, int B>
-__device__ __forceinline__ void slice_b_tile(const SplitPair &P, int nt, int kb, const double *__restrict__ Bm,
-                                             const int *__restrict__ F, uint8_t *__restrict__ tile) {
-  const bool tb = P.trans & 2, cb = P.trans & 8;
-  if constexpr (CPLX) {
-    if (P.dupb) {
-      // B-duplicated form: real column n of B' is (Re; -Im) (n even) or
-      // (Im; Re) (n odd) of complex column n / 2 of op(B)
-      for (int w = threadIdx.x; w < TNS * (TKS / 8); w += blockDim.x) {
-        const int c = w % TNS, q = w / TNS;
-        const int n = nt * TNS + c;
-        if (n >= P.Nr) continue;  // feeds discarded outputs only: not written
-        const int nc = n >> 1;
-        const bool odd = n & 1;
-        const int Fj = F[P.foff + n];
-        uint32_t pk[S][4];
+__device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int4 tk,
+                                        const double *__restrict__ Aarena, const double *__restrict__ Barena,
+                                        int *__restrict__ F, uint8_t *__restrict__ arena) {
+  __shared__ int smax[STRIP];
+  const int p0 = tk.x, p1 = tk.y, c0 = tk.z;
+  const SplitPair &Q = pairs[p0];
+  const bool dup = CPLX && Q.dupb != 0;  // two real columns per column of op(B)
+  const int l0 = dup ? c0 / 2 : c0;
+  const int nl = min(dup ? STRIP / 2 : STRIP, Q.N - l0);
+  strip_maxima<CPLX, true>(pairs, p0, p1, l0, nl, Aarena, Barena, smax);
+  if (threadIdx.x < nl) {
+    const int e = smax[threadIdx.x];
+    if (dup) {
+      F[Q.foff + 2 * (l0 + threadIdx.x)] = e;
+      F[Q.foff + 2 * (l0 + threadIdx.x) + 1] = e;
+    } else {
+      F[Q.foff + l0 + threadIdx.x] = e;
+    }
+  }
+  const int nt = c0 / TNS, cl = c0 % TNS;
+  const int ncols = dup ? 2 * nl : nl;  // real columns of this strip inside the block
+  const Factor F1{0ull, 0, false};
+  for (int p = p0; p < p1; ++p) {
+    const SplitPair &P = pairs[p];
+    const double *__restrict__ Bm = P.swap ? Aarena : Barena;
+    const bool tb = P.trans & 2, cb = P.trans & 8;
+    uint8_t *tiles = arena + P.bs_off + (int64_t)nt * P.KB * S * B_DIGIT_BYTES;
+    // item = one real column x 8 real k
+    const int items = STRIP * KCM * P.KB;
+    for (int w = threadIdx.x; w < items; w += blockDim.x) {
+      const int kb = w / (STRIP * KCM), i = w % (STRIP * KCM);
+      const int cloc = i % STRIP, q = i / STRIP;
+      if (cloc >= ncols) continue;  // columns past the block feed discarded outputs only
+      const int c = cl + cloc;
+      const int Fj = smax[dup ? cloc >> 1 : cloc];
+      uint32_t pk[S][4];
+      if constexpr (CPLX) {
+        const int64_t n = dup ? l0 + (cloc >> 1) : l0 + cloc;
+        double2 x[4];
+        // B~ (A-duplicated form): rows 2k, 2k+1 = (Re, Im) of element k; B'
+        // (B-duplicated form): the same 4 complex k per 8 real rows
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int k = (kb * TKS + q * 8) / 2 + j;
-          double re = 0.0, im = 0.0;
-          if (k < P.K) {
-            const double2 x = reinterpret_cast<const double2 *>(Bm)[
-                P.b_off + (tb ? (int64_t)nc + (int64_t)k * P.ldb : (int64_t)k + (int64_t)nc * P.ldb)];
-            re = x.x;
-            im = cb ? -x.y : x.y;
-          }
+          x[j] = make_double2(0.0, 0.0);
+          if (k < P.K)
+            x[j] = reinterpret_cast<const double2 *>(Bm)[P.b_off + (tb ? n + (int64_t)k * P.ldb : (int64_t)k + n * P.ldb)];
+        }
+        const bool odd = dup && (cloc & 1);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
           float dr[S], di[S];
-          digits_f<S, B>(scaled_int(re, Fj, B * S, Factor{0ull, 0, false}), dr);
-          digits_f<S, B>(scaled_int(im, Fj, B * S, Factor{0ull, 0, false}), di);
+          digits_f<S, B>(scaled_int(x[j].x, Fj, B * S, F1), dr);
+          digits_f<S, B>(scaled_int(cb ? -x[j].y : x[j].y, Fj, B * S, F1), di);
 #pragma unroll
-          for (int t = 0; t < S; ++t) pk[t][j] = odd ? pack2(di[t], dr[t]) : pack2(dr[t], -di[t]);
+          for (int t = 0; t < S; ++t)
+            pk[t][j] = dup ? (odd ? pack2(di[t], dr[t]) : pack2(dr[t], -di[t])) : pack2(dr[t], di[t]);
         }
-        uint8_t *dst = tile + ((c >> 3) * KCM + q) * 128 + (c & 7) * 16;
-#pragma unroll
-        for (int t = 0; t < S; ++t)
-          *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
-      }
-      return;
-    }
-  }
-  for (int w = threadIdx.x; w < TNS * (TKS / 8); w += blockDim.x) {
-    const int c = w % TNS, q = w / TNS;
-    const int n = nt * TNS + c;
-    if (n >= P.N) continue;  // columns past the block feed discarded outputs only: not written
-    const bool nv = true;
-    const int Fj = F[P.foff + n];
-    uint32_t pk[S][4];
-#pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      float dd[2][S];
-      if constexpr (CPLX) {
-        // rows 2k, 2k+1 of B~ are (Re, Im) of one complex element
-        const int k = (kb * TKS + q * 8 + e) >> 1;
-        double re = 0.0, im = 0.0;
-        if (nv && 2 * k < P.Kr) {
-          const double2 x = reinterpret_cast<const double2 *>(Bm)[
-              P.b_off + (tb ? (int64_t)n + (int64_t)k * P.ldb : (int64_t)k + (int64_t)n * P.ldb)];
-          re = x.x;
-          im = cb ? -x.y : x.y;
-        }
-        digits_f<S, B>(scaled_int(re, Fj, B * S, Factor{0ull, 0, false}), dd[0]);
-        digits_f<S, B>(scaled_int(im, Fj, B * S, Factor{0ull, 0, false}), dd[1]);
       } else {
+        const int64_t n = l0 + cloc;
+        double v[8];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int kk = kb * TKS + q * 8 + e + h;
-          double v = 0.0;
-          if (nv && kk < P.Kr)
-            v = Bm[P.b_off + (tb ? (int64_t)n + (int64_t)kk * P.ldb : (int64_t)kk + (int64_t)n * P.ldb)];
-          digits_f<S, B>(scaled_int(v, Fj, B * S, Factor{0ull, 0, false}), dd[h]);
+        for (int e = 0; e < 8; ++e) {
+          const int kk = kb * TKS + q * 8 + e;
+          v[e] = 0.0;
+          if (kk < P.Kr) v[e] = Bm[P.b_off + (tb ? n + (int64_t)kk * P.ldb : (int64_t)kk + n * P.ldb)];
+        }
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          float d0[S], d1[S];
+          digits_f<S, B>(scaled_int(v[e], Fj, B * S, F1), d0);
+          digits_f<S, B>(scaled_int(v[e + 1], Fj, B * S, F1), d1);
+#pragma unroll
+          for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(d0[t], d1[t]);
         }
       }
+      uint8_t *dst = tiles + (int64_t)kb * S * B_DIGIT_BYTES + ((c >> 3) * KCM + q) * 128 + (c & 7) * 16;
 #pragma unroll
-      for (int t = 0; t < S; ++t) pk[t][e >> 1] = pack2(dd[0][t], dd[1][t]);
+      for (int t = 0; t < S; ++t)
+        *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
     }
-    uint8_t *dst = tile + ((c >> 3) * KCM + q) * 128 + (c & 7) * 16;
-#pragma unroll
-    for (int t = 0; t < S; ++t)
-      *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
   }
 }
 
 template <bool CPLX, int S>
-__global__ void __launch_bounds__(128)
-slice_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks,
-               const double *__restrict__ Aarena, const double *__restrict__ Barena, const int *__restrict__ F,
-               uint8_t *__restrict__ arena, int b) {
+__global__ void __launch_bounds__(STRIP_THREADS)
+strip_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks, const double *__restrict__ A,
+               const double *__restrict__ B, int *__restrict__ E, uint8_t *__restrict__ arena, int b) {
   const int4 tk = tasks[blockIdx.x];
-  const SplitPair P = pairs[tk.x];
-  const double *__restrict__ Bm = P.swap ? Aarena : Barena;
-  uint8_t *tile = arena + P.bs_off + ((int64_t)(tk.y * P.KB + tk.z) * S) * B_DIGIT_BYTES;
+  switch (b) {  // the host admits b = 5..8 only
+    case 5: strip_a<CPLX, S, 5>(pairs, tk, A, B, E, arena); break;
+    case 6: strip_a<CPLX, S, 6>(pairs, tk, A, B, E, arena); break;
+    case 7: strip_a<CPLX, S, 7>(pairs, tk, A, B, E, arena); break;
+    default: strip_a<CPLX, S, 8>(pairs, tk, A, B, E, arena); break;
+  }
+}
+
+template <bool CPLX, int S>
+__global__ void __launch_bounds__(STRIP_THREADS)
+strip_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks, const double *__restrict__ A,
+               const double *__restrict__ B, int *__restrict__ F, uint8_t *__restrict__ arena, int b) {
+  const int4 tk = tasks[blockIdx.x];
   switch (b) {
-    case 5: slice_b_tile<CPLX, S, 5>(P, tk.y, tk.z, Bm, F, tile); break;
-    case 6: slice_b_tile<CPLX, S, 6>(P, tk.y, tk.z, Bm, F, tile); break;
-    case 7: slice_b_tile<CPLX, S, 7>(P, tk.y, tk.z, Bm, F, tile); break;
-    default: slice_b_tile<CPLX, S, 8>(P, tk.y, tk.z, Bm, F, tile); break;
+    case 5: strip_b<CPLX, S, 5>(pairs, tk, A, B, F, arena); break;
+    case 6: strip_b<CPLX, S, 6>(pairs, tk, A, B, F, arena); break;
+    case 7: strip_b<CPLX, S, 7>(pairs, tk, A, B, F, arena); break;
+    default: strip_b<CPLX, S, 8>(pairs, tk, A, B, F, arena); break;
   }
 }
 
@@ -1010,32 +968,18 @@ int pick_stages() {
 }
 
 template <int S>
-void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d_rt, int nrt,
-                    const int4 *d_ct, int nct, const int4 *d_xt, int nxt, const int4 *d_at, int nat,
-                    const int4 *d_bt, int nbt,
-                    const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
-                    int *dE, int64_t nE, int *dF, int64_t nF, uint8_t *arena, int b, int kchunk,
-                    int *err) {
+void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d_sa, int nsa, const int4 *d_sb,
+                    int nsb, const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
+                    int *dE, int *dF, uint8_t *arena, int b, int kchunk, int *err) {
   if (b < 5 || b > 8 || b * S > 62) fail(QS_ERR_INTERNAL, "split: unsupported digit plan b=%d S=%d", b, S);
   cudaStream_t st = ctx->stream;
-  const int fg = (int)std::min<int64_t>(std::max<int64_t>((nE + nF + 255) / 256, 1), 4096);
   ctx->mark(0);
-  fill_int_kernel<<<fg, 256, 0, st>>>(dE, nE, EMPTY_EXP);
-  QS_LAUNCHED(ctx);
-  fill_int_kernel<<<fg, 256, 0, st>>>(dF, nF, EMPTY_EXP);
-  QS_LAUNCHED(ctx);
   if (cplx) {
-    if (nrt) { exp_lines_kernel<true, false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nct) { exp_lines_kernel<true, true><<<nct, 256, 0, st>>>(d_pairs, d_ct, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nxt) { exp_contig_kernel<true><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nat) { slice_a_kernel<true, S><<<nat, SLICE_A_THREADS_C, 0, st>>>(d_pairs, d_at, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<true, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nsa) { strip_a_kernel<true, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nsb) { strip_b_kernel<true, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
   } else {
-    if (nrt) { exp_lines_kernel<false, false><<<nrt, 256, 0, st>>>(d_pairs, d_rt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nct) { exp_lines_kernel<false, true><<<nct, 256, 0, st>>>(d_pairs, d_ct, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nxt) { exp_contig_kernel<false><<<nxt, 256, 0, st>>>(d_pairs, d_xt, A, B, dE, dF); QS_LAUNCHED(ctx); }
-    if (nat) { slice_a_kernel<false, S><<<nat, SLICE_A_THREADS_R, 0, st>>>(d_pairs, d_at, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nbt) { slice_b_kernel<false, S><<<nbt, SLICE_B_THREADS, 0, st>>>(d_pairs, d_bt, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nsa) { strip_a_kernel<false, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nsb) { strip_b_kernel<false, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
   }
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);
@@ -1159,18 +1103,16 @@ struct SplitWork {
   int S = 0, b = 0, kchunk = 0;
   int64_t nE = 0, nF = 0, arena = 0;
   std::vector<SplitPair> sp;
-  std::vector<int4> rt;
-  std::vector<int4> ct;  // strided columns of op(B~): (pair, n0, k0, k1)
-  std::vector<int4> xt, at, bt;
+  // strips of STRIP real lines: (first pair, end pair, first line, 0) of the
+  // A role (rows of op(A~)) and of the B role (columns of op(B~))
+  std::vector<int4> sa, sb;
   std::vector<SplitTile> tiles;
 };
 
 // Their device copies, the exponent arrays and the digit arena.
 struct SplitDev {
   SplitPair *pairs = nullptr;
-  int4 *rt = nullptr;
-  int4 *ct = nullptr;
-  int4 *xt = nullptr, *at = nullptr, *bt = nullptr;
+  int4 *sa = nullptr, *sb = nullptr;
   SplitTile *tiles = nullptr;
   int *E = nullptr, *F = nullptr;
   uint8_t *arena = nullptr;
@@ -1277,10 +1219,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
   if (nE > INT32_MAX || nF > INT32_MAX) fail(QS_ERR_SHAPE, "split: exponent arrays too large");
   int64_t &arena = w.arena;
   arena = 0;
-  std::vector<int4> &rt = w.rt;
-  std::vector<int4> &ct = w.ct;
-  std::vector<int4> &xt = w.xt;
-  std::vector<int4> &at = w.at, &bt = w.bt;
+  std::vector<int4> &sa = w.sa, &sb = w.sb;
   std::vector<SplitTile> &tiles = w.tiles;
   for (int64_t g = 0; g < nb; ++g) {
     // every pair's CG factor is folded into its A digits (exact integer
@@ -1317,23 +1256,13 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
       arena += (int64_t)s.MT * s.KB * S * A_DIGIT_BYTES;
       s.bs_off = arena;
       arena += (int64_t)s.NT * s.KB * S * B_DIGIT_BYTES;
-      // exponent tasks: lines contiguous along k get a warp each (coalesced),
-      // strided lines a thread each (neighbouring lanes read neighbouring
-      // elements)
-      if (d.trans & 1)
-        for (int m0 = 0; m0 < d.M; m0 += 8) xt.push_back(make_int4((int)p, m0, 0, 0));
-      else
-        for (int m0 = 0; m0 < d.M; m0 += 256)
-          for (int k0 = 0; k0 < d.K; k0 += 256) rt.push_back(make_int4((int)p, m0, k0, std::min(d.K, k0 + 256)));
-      if (d.trans & 2)
-        for (int n0 = 0; n0 < d.N; n0 += 256)
-          for (int k0 = 0; k0 < d.K; k0 += 256) ct.push_back(make_int4((int)p, n0, k0, std::min(d.K, k0 + 256)));
-      else
-        for (int n0 = 0; n0 < d.N; n0 += 8) xt.push_back(make_int4((int)p, n0, 1, 0));
-      for (int mt = 0; mt < s.MT; ++mt)
-        for (int kb = 0; kb < s.KB; ++kb) at.push_back(make_int4((int)p, mt, kb, 0));
-      for (int nt = 0; nt < s.NT; ++nt)
-        for (int kb = 0; kb < s.KB; ++kb) bt.push_back(make_int4((int)p, nt, kb, 0));
+    }
+    // exponent + slicing strips over all pairs of the block
+    if (grp[g + 1] > grp[g]) {
+      for (int64_t r0 = 0; r0 < rows_r[g]; r0 += STRIP)
+        sa.push_back(make_int4((int)grp[g], (int)grp[g + 1], (int)r0, 0));
+      for (int64_t c0 = 0; c0 < cols_r[g]; c0 += STRIP)
+        sb.push_back(make_int4((int)grp[g], (int)grp[g + 1], (int)c0, 0));
     }
     const int nchunk = chunks_of(pairs, grp[g], grp[g + 1], cm, kchunk);
     // int64 headroom of the fixed-point sum over all chunks:
@@ -1399,7 +1328,7 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
     return kx > ky;
   });
   if (tiles.empty()) return res;
-  if (tiles.size() > 0x7fffffff || at.size() > 0x7fffffff || bt.size() > 0x7fffffff)
+  if (tiles.size() > 0x7fffffff || sa.size() > 0x7fffffff || sb.size() > 0x7fffffff)
     fail(QS_ERR_SHAPE, "split: launch too large");
   res.slice_bytes = arena;
   res.ntiles = (int64_t)tiles.size();
@@ -1415,9 +1344,8 @@ static void launch_split(Ctx *ctx, const SplitWork &w, bool cplx, const SplitDev
   switch (w.S) {
 #define QS_CASE(SS)                                                                                      \
   case SS:                                                                                               \
-    launch_split_s<SS>(ctx, cplx, d.pairs, d.rt, (int)w.rt.size(), d.ct, (int)w.ct.size(), d.xt,        \
-                       (int)w.xt.size(), d.at, (int)w.at.size(), d.bt, (int)w.bt.size(), d.tiles,        \
-                       (int)w.tiles.size(), A, B, C, d.E, w.nE, d.F, w.nF, d.arena, w.b, w.kchunk, err); \
+    launch_split_s<SS>(ctx, cplx, d.pairs, d.sa, (int)w.sa.size(), d.sb, (int)w.sb.size(), d.tiles,     \
+                       (int)w.tiles.size(), A, B, C, d.E, d.F, d.arena, w.b, w.kchunk, err);             \
     break;
     QS_CASE(2)
     QS_CASE(3)
@@ -1444,11 +1372,8 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   SplitDev d;
   d.arena = static_cast<uint8_t *>(ctx->ensure_scratch((size_t)std::max<int64_t>(w.arena, 256)));
   d.pairs = dev_upload(ctx, w.sp);
-  d.rt = dev_upload(ctx, w.rt);
-  d.ct = dev_upload(ctx, w.ct);
-  d.xt = dev_upload(ctx, w.xt);
-  d.at = dev_upload(ctx, w.at);
-  d.bt = dev_upload(ctx, w.bt);
+  d.sa = dev_upload(ctx, w.sa);
+  d.sb = dev_upload(ctx, w.sb);
   d.tiles = dev_upload(ctx, w.tiles);
   d.E = dev_alloc<int>(ctx, (size_t)w.nE);
   d.F = dev_alloc<int>(ctx, (size_t)w.nF);
@@ -1460,11 +1385,8 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   }
   launch_split(ctx, w, cplx, d, A, B, C, ctx->d_err);
   dev_free(ctx, d.pairs);
-  dev_free(ctx, d.rt);
-  dev_free(ctx, d.ct);
-  dev_free(ctx, d.xt);
-  dev_free(ctx, d.at);
-  dev_free(ctx, d.bt);
+  dev_free(ctx, d.sa);
+  dev_free(ctx, d.sb);
   dev_free(ctx, d.tiles);
   dev_free(ctx, d.E);
   dev_free(ctx, d.F);
@@ -1486,9 +1408,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
     return o;
   };
   const size_t o_pairs = take(w.sp.size() * sizeof(SplitPair));
-  const size_t o_rt = take(w.rt.size() * sizeof(int4)), o_ct = take(w.ct.size() * sizeof(int4));
-  const size_t o_xt = take(w.xt.size() * sizeof(int4)), o_at = take(w.at.size() * sizeof(int4));
-  const size_t o_bt = take(w.bt.size() * sizeof(int4));
+  const size_t o_sa = take(w.sa.size() * sizeof(int4)), o_sb = take(w.sb.size() * sizeof(int4));
   const size_t o_tiles = take(w.tiles.size() * sizeof(SplitTile));
   const size_t o_E = take((size_t)w.nE * sizeof(int)), o_F = take((size_t)w.nF * sizeof(int));
   const size_t o_arena = take((size_t)w.arena);
@@ -1497,11 +1417,8 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
          "BF16 digits), more than the %zu available", used, (long long)w.arena, cap);
   SplitDev d;
   d.pairs = reinterpret_cast<SplitPair *>(scratch + o_pairs);
-  d.rt = reinterpret_cast<int4 *>(scratch + o_rt);
-  d.ct = reinterpret_cast<int4 *>(scratch + o_ct);
-  d.xt = reinterpret_cast<int4 *>(scratch + o_xt);
-  d.at = reinterpret_cast<int4 *>(scratch + o_at);
-  d.bt = reinterpret_cast<int4 *>(scratch + o_bt);
+  d.sa = reinterpret_cast<int4 *>(scratch + o_sa);
+  d.sb = reinterpret_cast<int4 *>(scratch + o_sb);
   d.tiles = reinterpret_cast<SplitTile *>(scratch + o_tiles);
   d.E = reinterpret_cast<int *>(scratch + o_E);
   d.F = reinterpret_cast<int *>(scratch + o_F);
@@ -1510,11 +1427,8 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
     if (bytes) QS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
   };
   put(d.pairs, w.sp.data(), w.sp.size() * sizeof(SplitPair));
-  put(d.rt, w.rt.data(), w.rt.size() * sizeof(int4));
-  put(d.ct, w.ct.data(), w.ct.size() * sizeof(int4));
-  put(d.xt, w.xt.data(), w.xt.size() * sizeof(int4));
-  put(d.at, w.at.data(), w.at.size() * sizeof(int4));
-  put(d.bt, w.bt.data(), w.bt.size() * sizeof(int4));
+  put(d.sa, w.sa.data(), w.sa.size() * sizeof(int4));
+  put(d.sb, w.sb.data(), w.sb.size() * sizeof(int4));
   put(d.tiles, w.tiles.data(), w.tiles.size() * sizeof(SplitTile));
   launch_split(ctx, w, cplx, d, A, B, C, err);
   return res;
@@ -1573,11 +1487,8 @@ SplitPlanHandle *split_plan_create(const std::vector<PairDesc> &pairs, const std
     };
     SplitDev &d = h->d;
     d.pairs = put(h->w.sp);
-    d.rt = put(h->w.rt);
-    d.ct = put(h->w.ct);
-    d.xt = put(h->w.xt);
-    d.at = put(h->w.at);
-    d.bt = put(h->w.bt);
+    d.sa = put(h->w.sa);
+    d.sb = put(h->w.sb);
     d.tiles = put(h->w.tiles);
     d.E = static_cast<int *>(own((size_t)h->w.nE * sizeof(int)));
     d.F = static_cast<int *>(own((size_t)h->w.nF * sizeof(int)));
