@@ -444,9 +444,9 @@ QS_EXPORT qs_status qs_gs_reortho(qs_ctx *ctx, int64_t n, int64_t nv, const doub
 
 /* ------------------------------------------------------------ serving loop
  * A continuous-batching request loop (no counterpart in the reference, whose
- * MEX calls are one at a time).  Requests are contractions between
- * device-resident tensors; each runs on its own slot stream once admitted
- * by HBM footprint; completions are polled. */
+ * MEX calls are one at a time).  Requests are contractions and block
+ * eigendecompositions (eigQS) of device-resident tensors; each runs on its
+ * own slot stream once admitted by HBM footprint; completions are polled. */
 typedef struct qs_server qs_server;
 typedef struct {
   int32_t nslots;          /* concurrent requests on the device               */
@@ -467,6 +467,21 @@ QS_EXPORT qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const cha
 QS_EXPORT qs_status qs_server_poll(qs_server *s, int64_t ticket, int32_t timeout_ms,
                          int32_t *done, qs_tensor **C, double *latency_ms);
 QS_EXPORT qs_status qs_server_cancel(qs_server *s, int64_t ticket);
+/* An eigQS request: qs_eigQS_dev of the device-resident rank-2 QSpace H
+ * (EigenSymmetric + markSet, Source/QSpace.cc:4673-4939) with the truncation
+ * options nkeep / etrunc / deps, run on a slot stream beside the contraction
+ * batches (no counterpart in the reference).  H must stay alive until the
+ * request completes. */
+QS_EXPORT qs_status qs_server_submit_eig(qs_server *s, const qs_tensor *H, int64_t nkeep, double etrunc,
+                                         double deps, int64_t *ticket);
+/* Completion of an eig request, as qs_server_poll: *AK / *AD receive the
+ * kept / discarded eigenvector tensors (owned by the caller; NULL to drop),
+ * E and keep (optional host arrays of sum(block sizes) entries) the
+ * eigenvalues in H's block order and their 0/1 keep flags, NK and Etrunc as
+ * qs_eigQS_dev reports them. */
+QS_EXPORT qs_status qs_server_poll_eig(qs_server *s, int64_t ticket, int32_t timeout_ms, int32_t *done,
+                                       qs_tensor **AK, qs_tensor **AD, double *E, uint8_t *keep,
+                                       int64_t *nkeep_out, double *etrunc_out, double *latency_ms);
 
 #ifdef __cplusplus
 }

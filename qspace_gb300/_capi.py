@@ -156,6 +156,11 @@ SIGNATURES = {
     "qs_server_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, c_int32_p,
                                  C.POINTER(C.c_void_p), c_double_p]),
     "qs_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
+    "qs_server_submit_eig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double,
+                                       c_int64_p]),
+    "qs_server_poll_eig": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), c_double_p,
+                                     C.POINTER(C.c_uint8), c_int64_p, c_double_p, c_double_p]),
 }
 
 _lib = None

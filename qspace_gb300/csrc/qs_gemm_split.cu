@@ -211,6 +211,36 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
+// L2 eviction priorities of the strip kernels (createpolicy, PTX ISA 7.4+):
+// the first read of an operand line is kept (evict_last) for the re-read of
+// phase 2, which is its last use (evict_first), and the digit stores stream
+// through (evict_first), so that they do not push the operand lines out.
+__device__ __forceinline__ uint64_t l2_policy_keep() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_stream() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ double2 ld_pol(const double2 *a, uint64_t pol) {
+  double2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_pol(const double *a, uint64_t pol) {
+  double v;
+  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_pol(uint8_t *a, uint4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.b32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "r"(v.x), "r"(v.y), "r"(v.z),
+               "r"(v.w), "l"(pol)
+               : "memory");
+}
+
 // ---------------------------------------------- exponents and slicing, fused
 // One CTA per strip of STRIP real lines of one output block: rows of op(A~)
 // (A role) or columns of op(B~) (B role), over every pair of the block and
@@ -255,28 +285,30 @@ __device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs
     const int ph = contig ? threadIdx.x % NPH : threadIdx.x / STRIP;
     int key = 0;
     if (line < nl) {
+      const uint64_t keep = l2_policy_keep();
       const int64_t m = l0 + line;
       const int64_t sk = contig ? 1 : ld, base = off + (contig ? m * ld : m);
       int k = ph;
       for (; k + 3 * NPH < P.K; k += 4 * NPH) {
         if (CPLX) {
           const double2 *x = reinterpret_cast<const double2 *>(X) + base;
-          const double2 v0 = x[k * sk], v1 = x[(k + NPH) * sk], v2 = x[(k + 2 * NPH) * sk],
-                        v3 = x[(k + 3 * NPH) * sk];
+          const double2 v0 = ld_pol(x + k * sk, keep), v1 = ld_pol(x + (k + NPH) * sk, keep),
+                        v2 = ld_pol(x + (k + 2 * NPH) * sk, keep), v3 = ld_pol(x + (k + 3 * NPH) * sk, keep);
           key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
                              max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
         } else {
           const double *x = X + base;
-          key = max(key, max(max(exp_key(x[k * sk]), exp_key(x[(k + NPH) * sk])),
-                             max(exp_key(x[(k + 2 * NPH) * sk]), exp_key(x[(k + 3 * NPH) * sk]))));
+          key = max(key, max(max(exp_key(ld_pol(x + k * sk, keep)), exp_key(ld_pol(x + (k + NPH) * sk, keep))),
+                             max(exp_key(ld_pol(x + (k + 2 * NPH) * sk, keep)),
+                                 exp_key(ld_pol(x + (k + 3 * NPH) * sk, keep)))));
         }
       }
       for (; k < P.K; k += NPH) {
         if (CPLX) {
-          const double2 v = reinterpret_cast<const double2 *>(X)[base + k * sk];
+          const double2 v = ld_pol(reinterpret_cast<const double2 *>(X) + base + k * sk, keep);
           key = max(key, max(exp_key(v.x), exp_key(v.y)));
         } else {
-          key = max(key, exp_key(X[base + k * sk]));
+          key = max(key, exp_key(ld_pol(X + base + k * sk, keep)));
         }
       }
     }
@@ -307,6 +339,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
     }
   }
   const int mt = r0 / TMS, rl = r0 % TMS;
+  const uint64_t last = l2_policy_stream();  // last use of operand lines; digit stores
   for (int p = p0; p < p1; ++p) {
     const SplitPair &P = pairs[p];
     const double *__restrict__ A = P.swap ? Barena : Aarena;
@@ -328,7 +361,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
           const int k = (kb * TKS + q * 8) / 2 + j;
           a[j] = make_double2(0.0, 0.0);
           if (k < P.K)
-            a[j] = reinterpret_cast<const double2 *>(A)[P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda)];
+            a[j] = ld_pol(reinterpret_cast<const double2 *>(A) + P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda), last);
         }
         uint32_t p0w[S][4], p1w[S][4];
 #pragma unroll
@@ -348,8 +381,8 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
         uint8_t *d1 = tile + ((rr1 >> 3) * KCM + q) * 128 + (rr1 & 7) * 16;
 #pragma unroll
         for (int t = 0; t < S; ++t) {
-          *reinterpret_cast<uint4 *>(d0 + t * A_DIGIT_BYTES) = make_uint4(p0w[t][0], p0w[t][1], p0w[t][2], p0w[t][3]);
-          *reinterpret_cast<uint4 *>(d1 + t * A_DIGIT_BYTES) = make_uint4(p1w[t][0], p1w[t][1], p1w[t][2], p1w[t][3]);
+          st_pol(d0 + t * A_DIGIT_BYTES, make_uint4(p0w[t][0], p0w[t][1], p0w[t][2], p0w[t][3]), last);
+          st_pol(d1 + t * A_DIGIT_BYTES, make_uint4(p1w[t][0], p1w[t][1], p1w[t][2], p1w[t][3]), last);
         }
       }
     } else {
@@ -369,7 +402,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
             const int k = (kb * TKS + q * 8) / 2 + j;
             a[j] = make_double2(0.0, 0.0);
             if (k < P.K)
-              a[j] = reinterpret_cast<const double2 *>(A)[P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda)];
+              a[j] = ld_pol(reinterpret_cast<const double2 *>(A) + P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda), last);
           }
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
@@ -385,7 +418,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
           for (int e = 0; e < 8; ++e) {
             const int kk = kb * TKS + q * 8 + e;
             v[e] = 0.0;
-            if (kk < P.Kr) v[e] = A[P.a_off + (ta ? (int64_t)kk + m * P.lda : m + (int64_t)kk * P.lda)];
+            if (kk < P.Kr) v[e] = ld_pol(A + P.a_off + (ta ? (int64_t)kk + m * P.lda : m + (int64_t)kk * P.lda), last);
           }
 #pragma unroll
           for (int e = 0; e < 8; e += 2) {
@@ -400,7 +433,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
         uint8_t *dst = tiles + (int64_t)kb * S * A_DIGIT_BYTES + ((rr >> 3) * KCM + q) * 128 + (rr & 7) * 16;
 #pragma unroll
         for (int t = 0; t < S; ++t)
-          *reinterpret_cast<uint4 *>(dst + t * A_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+          st_pol(dst + t * A_DIGIT_BYTES, make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]), last);
       }
     }
   }
@@ -430,6 +463,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
   const int nt = c0 / TNS, cl = c0 % TNS;
   const int ncols = dup ? 2 * nl : nl;  // real columns of this strip inside the block
   const Factor F1{0ull, 0, false};
+  const uint64_t last = l2_policy_stream();  // last use of operand lines; digit stores
   for (int p = p0; p < p1; ++p) {
     const SplitPair &P = pairs[p];
     const double *__restrict__ Bm = P.swap ? Aarena : Barena;
@@ -454,7 +488,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
           const int k = (kb * TKS + q * 8) / 2 + j;
           x[j] = make_double2(0.0, 0.0);
           if (k < P.K)
-            x[j] = reinterpret_cast<const double2 *>(Bm)[P.b_off + (tb ? n + (int64_t)k * P.ldb : (int64_t)k + n * P.ldb)];
+            x[j] = ld_pol(reinterpret_cast<const double2 *>(Bm) + P.b_off + (tb ? n + (int64_t)k * P.ldb : (int64_t)k + n * P.ldb), last);
         }
         const bool odd = dup && (cloc & 1);
 #pragma unroll
@@ -473,7 +507,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
         for (int e = 0; e < 8; ++e) {
           const int kk = kb * TKS + q * 8 + e;
           v[e] = 0.0;
-          if (kk < P.Kr) v[e] = Bm[P.b_off + (tb ? n + (int64_t)kk * P.ldb : (int64_t)kk + n * P.ldb)];
+          if (kk < P.Kr) v[e] = ld_pol(Bm + P.b_off + (tb ? n + (int64_t)kk * P.ldb : (int64_t)kk + n * P.ldb), last);
         }
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
@@ -487,7 +521,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
       uint8_t *dst = tiles + (int64_t)kb * S * B_DIGIT_BYTES + ((c >> 3) * KCM + q) * 128 + (c & 7) * 16;
 #pragma unroll
       for (int t = 0; t < S; ++t)
-        *reinterpret_cast<uint4 *>(dst + t * B_DIGIT_BYTES) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+        st_pol(dst + t * B_DIGIT_BYTES, make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]), last);
     }
   }
 }

@@ -767,12 +767,12 @@ qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E, const do
 // eigenvectors gathered into device tensors AK / AD without leaving the
 // device.  Every block's kept states are its lowest ones (markSet keeps a
 // prefix of the ascending global order), i.e. its first k columns.
-qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc, double deps, qs_tensor **AK,
-                       qs_tensor **AD, double *E, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
-  QS_API_BEGIN
-  if (!ctx || !H || !AK || !AD) fail(QS_ERR_ARG, "null argument");
-  Ctx *c = &ctx->c;
-  QS_CUDA(cudaSetDevice(c->device));
+}  // extern "C"
+
+namespace qs {
+void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double deps,
+                std::unique_ptr<qs_tensor> &AK, std::unique_ptr<qs_tensor> &AD, double *E, uint8_t *keep,
+                int64_t *nkeep_out, double *etrunc_out) {
   const QMeta &m = H->meta;
   if (m.rank != 2) fail(QS_ERR_SHAPE, "eigQS: rank-2 QSpace required (got rank %d)", m.rank);
   const int64_t nb = m.nblk;
@@ -857,13 +857,35 @@ qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double et
     if (keep && ntot) std::memcpy(keep, hk.data(), ntot);
     if (nkeep_out) *nkeep_out = nk;
     if (etrunc_out) *etrunc_out = et;
-    *AK = tk.release();
-    *AD = td.release();
+    AK = std::move(tk);
+    AD = std::move(td);
   } catch (...) {
     if (U) dev_free(c, U);
     if (dE) dev_free(c, dE);
     throw;
   }
+}
+
+int64_t eigqs_footprint(const QMeta &m) {
+  // eigenvectors, the kept and discarded copies, eigenvalues
+  const int64_t es = m.cplx ? 16 : 8;
+  int64_t ntot = 0;
+  for (int64_t i = 0; i < m.nblk; ++i) ntot += m.drow(i)[0];
+  return 2 * m.nelem * es + ntot * 8 + (64 << 20);
+}
+}  // namespace qs
+
+extern "C" {
+
+qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc, double deps, qs_tensor **AK,
+                       qs_tensor **AD, double *E, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
+  QS_API_BEGIN
+  if (!ctx || !H || !AK || !AD) fail(QS_ERR_ARG, "null argument");
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  std::unique_ptr<qs_tensor> tk, td;
+  eigqs_core(&ctx->c, H, nkeep, etrunc, deps, tk, td, E, keep, nkeep_out, etrunc_out);
+  *AK = tk.release();
+  *AD = td.release();
   QS_API_END
 }
 

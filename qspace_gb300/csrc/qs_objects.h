@@ -43,4 +43,12 @@ void contract_batch_core(Ctx *ctx, int n, const QMeta *const *Am, const double *
 // copies, digit arena): the admission footprint of the serving loop.
 int64_t contract_footprint(const QMeta &Am, const QMeta &Bm, const char *ia, const char *ib,
                            const qs_opts *opts);
+// eigQS of a device-resident rank-2 QSpace on ctx's stream: kept and
+// discarded eigenvectors as new tensors, optional host copies of the
+// eigenvalues / keep flags (sum of block sizes each), NK and Etrunc.
+void eigqs_core(Ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc, double deps,
+                std::unique_ptr<qs_tensor> &AK, std::unique_ptr<qs_tensor> &AD, double *E, uint8_t *keep,
+                int64_t *nkeep_out, double *etrunc_out);
+// Device bytes eigqs_core holds while it runs (admission footprint).
+int64_t eigqs_footprint(const QMeta &m);
 }  // namespace qs

@@ -1,6 +1,7 @@
-// Serving loop: continuous batching of contractions between device-resident
-// tensors for many concurrent NRG / DMRG instances.  (The reference has no
-// counterpart: its MEX calls run one at a time from MATLAB.)
+// Serving loop: continuous batching of contractions and block eigen-
+// decompositions (eigQS) between device-resident tensors for many concurrent
+// NRG / DMRG instances.  (The reference has no counterpart: its MEX calls
+// run one at a time from MATLAB.)
 //
 //  * qs_server_submit enqueues a request (FIFO) and records an event on the
 //    submitting context's stream, so the request sees every earlier write to
@@ -14,6 +15,9 @@
 //    arrive while others are on the GPU are admitted as slots and memory
 //    free up, and their kernels overlap on the device.  A request larger than the whole budget is
 //    refused at submit time (QS_ERR_OOM).
+//  * An eig request (qs_server_submit_eig) runs alone on a slot -- its block
+//    eigensolver already spreads the blocks over concurrent solver lanes --
+//    next to the contraction batches of the other slots.
 //  * Results are identical alone and in the mix: every kernel is
 //    deterministic (fixed reduction order) and requests share no buffers.
 //  * qs_server_poll waits a bounded time; qs_server_cancel removes a
@@ -38,7 +42,8 @@ using clk = std::chrono::steady_clock;
 
 struct Request {
   int64_t ticket = 0;
-  const qs_tensor *A = nullptr, *B = nullptr;
+  enum Kind { CONTRACT, EIG } kind = CONTRACT;
+  const qs_tensor *A = nullptr, *B = nullptr;  // eig: A = H
   std::string ia, ib;
   std::vector<int32_t> perm;
   qs_opts opts{};
@@ -51,6 +56,14 @@ struct Request {
   std::string err;
   qs_tensor *C = nullptr;
   double latency_ms = 0;
+  // eig requests: truncation options and results (C = kept eigenvectors)
+  int64_t nkeep = -1;
+  double etrunc = 0, deps = 0;
+  qs_tensor *D = nullptr;         // discarded eigenvectors
+  std::vector<double> E;          // eigenvalues, H's block order
+  std::vector<uint8_t> keep;
+  int64_t nk = 0;
+  double et = 0;
 };
 
 }  // namespace
@@ -70,6 +83,7 @@ struct qs_server {
   int max_batch = 16;
 
   static bool same_opts(const Request &a, const Request &b) {
+    if (a.kind != Request::CONTRACT || b.kind != Request::CONTRACT) return false;  // eig requests run alone
     if (a.has_opts != b.has_opts) return false;
     if (!a.has_opts) return true;
     return a.opts.prec == b.opts.prec && a.opts.nslices == b.opts.nslices && a.opts.tol == b.opts.tol;
@@ -139,7 +153,28 @@ struct qs_server {
       try {
         for (auto &r : batch)
           if (r->ready) QS_CUDA(cudaStreamWaitEvent(slot->stream, r->ready, 0));
-        if (n == 1) {
+        if (batch[0]->kind == Request::EIG) {
+          Request &r = *batch[0];
+          try {
+            std::unique_ptr<qs_tensor> tk, td;
+            int64_t ntot = 0;
+            for (int64_t i = 0; i < r.A->meta.nblk; ++i) ntot += r.A->meta.drow(i)[0];
+            r.E.assign((size_t)std::max<int64_t>(ntot, 1), 0.0);
+            r.keep.assign((size_t)std::max<int64_t>(ntot, 1), 0);
+            eigqs_core(slot, r.A, r.nkeep, r.etrunc, r.deps, tk, td, r.E.data(), r.keep.data(), &r.nk, &r.et);
+            QS_CUDA(cudaStreamSynchronize(slot->stream));
+            tk->ctx = &parent->c;
+            td->ctx = &parent->c;
+            C[0] = tk.release();
+            r.D = td.release();
+          } catch (const Error &e) {
+            st[0] = e.code;
+            msg[0] = e.what();
+          } catch (const std::exception &e) {
+            st[0] = QS_ERR_INTERNAL;
+            msg[0] = e.what();
+          }
+        } else if (n == 1) {
           run_alone(0);
         } else {
           std::vector<const QMeta *> am(n), bm(n);
@@ -229,6 +264,7 @@ void qs_server_destroy(qs_server *s) {
   for (auto &kv : s->reqs) {
     if (kv.second->ready) cudaEventDestroy(kv.second->ready);
     delete kv.second->C;  // results nobody collected
+    delete kv.second->D;
   }
   for (auto &c : s->slots) {
     if (c->scratch) cudaFreeAsync(c->scratch, c->stream);
@@ -280,6 +316,72 @@ qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const char *ia, con
   QS_API_END
 }
 
+qs_status qs_server_submit_eig(qs_server *s, const qs_tensor *H, int64_t nkeep, double etrunc, double deps,
+                               int64_t *ticket) {
+  QS_API_BEGIN
+  if (!s || !H || !ticket) fail(QS_ERR_ARG, "null argument");
+  if (H->meta.rank != 2) fail(QS_ERR_SHAPE, "eig request: rank-2 QSpace required (got rank %d)", H->meta.rank);
+  const int64_t fp = eigqs_footprint(H->meta);
+  if (fp > s->budget)
+    fail(QS_ERR_OOM, "admission refused: request needs %lld bytes, budget is %lld", (long long)fp,
+         (long long)s->budget);
+  auto r = std::make_shared<Request>();
+  r->kind = Request::EIG;
+  r->A = H;
+  r->nkeep = nkeep;
+  r->etrunc = etrunc;
+  r->deps = deps;
+  r->footprint = fp;
+  QS_CUDA(cudaSetDevice(s->parent->c.device));
+  QS_CUDA(cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming));
+  QS_CUDA(cudaEventRecord(r->ready, s->parent->c.stream));
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->ticket = s->next_ticket++;
+    r->t_submit = clk::now();
+    s->reqs[r->ticket] = r;
+    s->queue.push_back(r);
+    *ticket = r->ticket;
+  }
+  s->cv_work.notify_one();
+  QS_API_END
+}
+
+qs_status qs_server_poll_eig(qs_server *s, int64_t ticket, int32_t timeout_ms, int32_t *done, qs_tensor **AK,
+                             qs_tensor **AD, double *E, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out,
+                             double *latency_ms) {
+  QS_API_BEGIN
+  if (!s || !done) fail(QS_ERR_ARG, "null argument");
+  *done = 0;
+  if (AK) *AK = nullptr;
+  if (AD) *AD = nullptr;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) fail(QS_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  std::shared_ptr<Request> r = it->second;
+  if (r->kind != Request::EIG) fail(QS_ERR_ARG, "ticket %lld is not an eig request", (long long)ticket);
+  auto finished = [&] { return r->state == Request::DONE || r->state == Request::FAILED || r->state == Request::CANCELLED; };
+  if (!finished() && timeout_ms > 0) s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished);
+  if (!finished()) return QS_OK;
+  *done = 1;
+  if (latency_ms) *latency_ms = r->latency_ms;
+  s->reqs.erase(it);
+  if (r->state == Request::CANCELLED) fail(QS_ERR_CANCELLED, "request %lld was cancelled", (long long)ticket);
+  if (r->state == Request::FAILED) fail(r->status, "%s", r->err.c_str());
+  int64_t ntot = 0;
+  for (int64_t i = 0; i < r->A->meta.nblk; ++i) ntot += r->A->meta.drow(i)[0];
+  if (E && ntot) std::memcpy(E, r->E.data(), (size_t)ntot * 8);
+  if (keep && ntot) std::memcpy(keep, r->keep.data(), (size_t)ntot);
+  if (nkeep_out) *nkeep_out = r->nk;
+  if (etrunc_out) *etrunc_out = r->et;
+  if (AK) *AK = r->C;
+  else delete r->C;
+  if (AD) *AD = r->D;
+  else delete r->D;
+  r->C = r->D = nullptr;
+  QS_API_END
+}
+
 qs_status qs_server_poll(qs_server *s, int64_t ticket, int32_t timeout_ms, int32_t *done, qs_tensor **C,
                          double *latency_ms) {
   QS_API_BEGIN
@@ -290,6 +392,8 @@ qs_status qs_server_poll(qs_server *s, int64_t ticket, int32_t timeout_ms, int32
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) fail(QS_ERR_ARG, "unknown ticket %lld", (long long)ticket);
   std::shared_ptr<Request> r = it->second;
+  if (r->kind != Request::CONTRACT)
+    fail(QS_ERR_ARG, "ticket %lld is an eig request (qs_server_poll_eig)", (long long)ticket);
   auto finished = [&] { return r->state == Request::DONE || r->state == Request::FAILED || r->state == Request::CANCELLED; };
   if (!finished() && timeout_ms > 0) s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished);
   if (!finished()) return QS_OK;

@@ -177,19 +177,66 @@ class DeviceBackend:
     def eig(self, H, nkeep, deps=0.0):
         """(labels of H's blocks, per-block ascending energies, per-block
         kept flags, device tensor of the kept eigenvectors)."""
-        from . import _capi
         from .linalg import eigQS_dev
         _, I = eigQS_dev(H, Nkeep=nkeep, deps=deps)
-        rank, qdim, nblk, _, _ = H.meta()
-        q = np.empty(max(nblk * rank * qdim, 1), np.int32)
-        dims = np.empty(max(nblk * rank, 1), np.int64)
-        _capi.check(self.ctx.lib.qs_tensor_meta(H.h, q.ctypes.data_as(_capi.c_int32_p),
-                                                dims.ctypes.data_as(_capi.c_int64_p), None))
-        q = q[:nblk * rank * qdim].reshape(nblk, rank, qdim)
-        n = dims[:nblk * rank:rank]
-        o = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
-        labels = [tuple(int(x) for x in q[i, 0]) for i in range(nblk)]
-        E = [I["E"][o[i]:o[i] + n[i]] for i in range(nblk)]
-        keep = [I["keep"][o[i]:o[i] + n[i]] for i in range(nblk)]
         I["AD"].free()
-        return labels, E, keep, I["AK"]
+        return _split_blocks(H, I["E"], I["keep"]) + (I["AK"],)
+
+
+def _split_blocks(H, E, keep):
+    """Labels of H's diagonal blocks and the per-block slices of the
+    eigenvalues / keep flags (given in H's block order)."""
+    from . import _capi
+    rank, qdim, nblk, _, _ = H.meta()
+    q = np.empty(max(nblk * rank * qdim, 1), np.int32)
+    dims = np.empty(max(nblk * rank, 1), np.int64)
+    _capi.check(H.ctx.lib.qs_tensor_meta(H.h, q.ctypes.data_as(_capi.c_int32_p),
+                                         dims.ctypes.data_as(_capi.c_int64_p), None))
+    q = q[:nblk * rank * qdim].reshape(nblk, rank, qdim)
+    n = dims[:nblk * rank:rank]
+    o = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+    labels = [tuple(int(x) for x in q[i, 0]) for i in range(nblk)]
+    return (labels, [E[o[i]:o[i] + n[i]] for i in range(nblk)], [keep[o[i]:o[i] + n[i]] for i in range(nblk)])
+
+
+class ServingBackend(DeviceBackend):
+    """The iteration with its contractions and its eigQS sent as requests to
+    a serving loop (qspace_gb300.serve.Server): the way many NRG runs share
+    one GPU.  Uploads, permutations and sums run on the instance's own
+    context, which is synchronised before each request (the server orders a
+    request after its submitter's stream of the server's parent context
+    only).  Request latencies (submit to completion) are recorded per kind."""
+
+    def __init__(self, server, ctx=None, prec: str = "fp64"):
+        super().__init__(ctx, prec)
+        self.server = server
+        self.latency = {"contract": [], "eig": []}
+
+    def contract(self, A, ia, B, ib):
+        self.ctx.sync()
+        T, ms = self.server.wait(self.server.submit(A, ia, B, ib, prec=self.prec))
+        self.latency["contract"].append(ms)
+        return T
+
+    def eig(self, H, nkeep, deps=0.0):
+        self.ctx.sync()
+        r = self.server.wait_eig(self.server.submit_eig(H, nkeep, 0.0, deps))
+        self.latency["eig"].append(r["latency_ms"])
+        r["AD"].free()
+        return _split_blocks(H, r["E"], r["keep"]) + (r["AK"],)
+
+
+def wilson_hopping(n: int, Lam: float, z: float = 0.0) -> float:
+    """Hopping t_n of the Wilson chain in the rescaled units of the
+    iteration (H_{N+1} = sqrt(Lambda) H_N + t_N ...), with the z-shift of the
+    logarithmic discretisation entering as Lambda^(-z/2) (z in [0, 1))."""
+    a = 1.0 - Lam ** (-(n + 1))
+    b = math.sqrt((1.0 - Lam ** (-(2 * n + 1))) * (1.0 - Lam ** (-(2 * n + 3))))
+    return 0.5 * (1.0 + 1.0 / Lam) * a / b * Lam ** (-z / 2.0)
+
+
+def kept_schedule(iters: int, first: int = 256, last: int = 4096) -> list:
+    """Kept states per iteration growing geometrically from `first` to `last`."""
+    if iters <= 1:
+        return [last]
+    return [int(round(first * (last / first) ** (i / (iters - 1)))) for i in range(iters)]

@@ -1,11 +1,11 @@
-"""Serving loop: continuous batching of contractQS requests between
+"""Serving loop: continuous batching of contractQS and eigQS requests on
 device-resident tensors (qs_server_* of the C-ABI).
 
-Many NRG z-shift / DMRG instances submit contractions as requests; the
-server admits them onto slot streams as slots and HBM budget free up, so
-requests arriving while others run overlap on the device.  Each result is
-identical to the same contraction run alone (deterministic kernels, no
-shared buffers).
+Many NRG z-shift / DMRG instances submit their contractions and block
+eigendecompositions as requests; the server admits them onto slot streams
+as slots and HBM budget free up, so requests arriving while others run
+overlap on the device.  Each result is identical to the same operation run
+alone (deterministic kernels, no shared buffers).
 """
 from __future__ import annotations
 
@@ -27,6 +27,7 @@ class Server:
         h = C.c_void_p()
         check(self.ctx.lib.qs_server_create(self.ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h
+        self._eig_sizes = {}   # ticket -> H of pending eig requests
 
     def submit(self, A: Tensor, ia, B: Tensor, ib, perm=None, prec: str = "fp64", nslices: int = 0,
                tol: float = 1e-12) -> int:
@@ -55,6 +56,55 @@ class Server:
             done, T, lat = self.poll(ticket, 50)
             if done:
                 return T, lat
+            if time.monotonic() - t0 > timeout_s:
+                raise QSError(6, f"request {ticket} did not complete in {timeout_s} s")
+
+    def submit_eig(self, H: Tensor, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0) -> int:
+        """Enqueue eigQS(H, 'Nkeep', nkeep, 'Etrunc', etrunc) of a device
+        tensor (qs_server_submit_eig).  H must stay alive until the result is
+        collected."""
+        t = C.c_int64()
+        check(self.ctx.lib.qs_server_submit_eig(self.h, H.h, int(nkeep), float(etrunc), float(deps), C.byref(t)))
+        self._eig_sizes[t.value] = H
+        return t.value
+
+    def poll_eig(self, ticket: int, timeout_ms: int = 0):
+        """(done, result dict or None).  The dict holds AK / AD (device
+        tensors of the kept / discarded eigenvectors), E and keep (host arrays
+        in H's block order), NK, Etrunc and the latency in ms."""
+        import numpy as np
+        H = self._eig_sizes[ticket]
+        rank, qdim, nblk, _, _ = H.meta()
+        dims = np.empty(max(nblk * rank, 1), np.int64)
+        check(self.ctx.lib.qs_tensor_meta(H.h, None, dims.ctypes.data_as(_capi.c_int64_p), None))
+        ntot = int(dims[:nblk * rank:rank].sum()) if nblk else 0
+        E = np.zeros(max(ntot, 1))
+        keep = np.zeros(max(ntot, 1), np.uint8)
+        done, lat, et = C.c_int32(), C.c_double(), C.c_double()
+        nk = C.c_int64()
+        ak, ad = C.c_void_p(), C.c_void_p()
+        try:
+            check(self.ctx.lib.qs_server_poll_eig(self.h, int(ticket), int(timeout_ms), C.byref(done), C.byref(ak),
+                                                  C.byref(ad), E.ctypes.data_as(_capi.c_double_p),
+                                                  keep.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(nk),
+                                                  C.byref(et), C.byref(lat)))
+        except QSError:
+            self._eig_sizes.pop(ticket, None)
+            raise
+        if not done.value:
+            return False, None
+        self._eig_sizes.pop(ticket, None)
+        return True, {"AK": Tensor(self.ctx, ak), "AD": Tensor(self.ctx, ad), "E": E[:ntot],
+                      "keep": keep[:ntot].astype(bool), "NK": nk.value, "Etrunc": et.value,
+                      "latency_ms": lat.value}
+
+    def wait_eig(self, ticket: int, timeout_s: float = 120.0) -> dict:
+        import time
+        t0 = time.monotonic()
+        while True:
+            done, r = self.poll_eig(ticket, 50)
+            if done:
+                return r
             if time.monotonic() - t0 > timeout_s:
                 raise QSError(6, f"request {ticket} did not complete in {timeout_s} s")
 

@@ -39,3 +39,41 @@ def test_device_truncated_iterations_match_oracle(ctx):
         assert Kd.nkept == Kc.nkept and sorted(Kd.E) == sorted(Kc.E)
         for lab in Kc.E:
             assert np.max(np.abs(Kd.E[lab] - Kc.E[lab])) <= 1e-12 * max(1.0, np.abs(Kc.E[lab]).max())
+
+
+def test_concurrent_runs_through_the_serving_loop_match_runs_alone(ctx):
+    """Three NRG runs at different z-shifts drive their contractions and
+    eigQS through one serving loop from three host threads at once: every
+    run keeps the same states with the same energies as the same run alone
+    on the device backend."""
+    import threading
+
+    from qspace_gb300.nrg import ServingBackend, kept_schedule, wilson_hopping
+    from qspace_gb300.qspace import Context
+    from qspace_gb300.serve import Server
+
+    Lam, iters, zs = 2.5, 5, (0.0, 1 / 3, 2 / 3)
+    nk = kept_schedule(iters, 60, 200)
+
+    def run(be, z, out):
+        K = initial_space(be, -0.2, 0.6)
+        for n in range(iters):
+            K = step(K, be, wilson_hopping(n, Lam, z), Lam, nkeep=nk[n], deps=1e-8)
+        out.append(K)
+
+    alone = []
+    for z in zs:
+        run(DeviceBackend(ctx, "split"), z, alone)
+    mixed = [[] for _ in zs]
+    with Server(nslots=4, hbm_budget=8 << 30, ctx=ctx) as srv:
+        bes = [ServingBackend(srv, Context(ctx.device), "split") for _ in zs]
+        th = [threading.Thread(target=run, args=(be, z, o)) for be, z, o in zip(bes, zs, mixed)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join(300)
+        assert all(len(be.latency["eig"]) == iters for be in bes)
+    for Ka, (Km,) in zip(alone, mixed):
+        assert Km.nkept == Ka.nkept and sorted(Km.E) == sorted(Ka.E)
+        for lab in Ka.E:
+            assert np.max(np.abs(Km.E[lab] - Ka.E[lab])) <= 1e-12 * max(1.0, np.abs(Ka.E[lab]).max())
