@@ -31,6 +31,7 @@ import subprocess
 import sys
 import tempfile
 import time
+import types
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -366,9 +367,12 @@ def main():
         from qspace_gb300.shard import block_flops, partition_blocks, shard
         w = grouped_pairs(seed=a.seed, npairs=a.npairs, complex_data=True)
         full = Packed(w["A"], w["B"], w["afac"], cplx=True)
-        pk = shard(full, partition_blocks(block_flops(full), ws)[rank])
+        parts = partition_blocks(block_flops(full), ws)
+        pk = shard(full, parts[rank])
         shard_info = {"rank0_operand_bytes": pk.operand_bytes(), "batch_operand_bytes": full.operand_bytes(),
-                      "rank0_pairs": pk.n, "batch_pairs": full.n}
+                      "rank0_pairs": pk.n, "batch_pairs": full.n,
+                      "exchange": "C blocks gathered to rank 0 (NCCL gather) inside every timed step"}
+        full_blocks = types.SimpleNamespace(cplx=full.cplx, blocks=full.blocks, c_elems=full.c_elems)
         del full
     else:
         shard_info = None
@@ -399,6 +403,11 @@ def main():
             db.run_plan(p)
         else:
             db.run(prec)
+        if a.shard and ws > 1:
+            # the exchange of a sharded contraction: every rank's blocks to rank 0
+            from qspace_gb300.shard import gather_blocks
+            with torch.cuda.stream(stream):
+                gather_blocks(db.dC, parts, full_blocks, pg, dst=0)
 
     if plan is not None:
         st = {}

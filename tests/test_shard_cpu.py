@@ -135,3 +135,72 @@ def test_two_gloo_ranks_assemble_the_unsharded_result():
         p.join(120)
     assert all(p.exitcode == 0 for p in ps)
     assert q.get(timeout=10) is True
+
+
+def _gather_rank(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qspace_gb300.shard import gather_blocks
+    pk = _batch(shared=False, npairs=40)
+    parts = partition_blocks(block_flops(pk), world)
+    mine = np.concatenate([b.reshape(-1, order="F") for b in _oracle_blocks(shard(pk, parts[rank]))])
+    out = gather_blocks(torch.from_numpy(mine.view(np.float64).copy()), parts, pk, dist, dst=0)
+    if rank == 0:
+        full = out.numpy().view(np.complex128)
+        ref = np.concatenate([b.reshape(-1, order="F") for b in _oracle_blocks(pk)])
+        q.put(bool(np.array_equal(full, ref)))
+    else:
+        q.put(out is None)
+    dist.destroy_process_group()
+
+
+def _spawn(target, world=2):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=target, args=(r, world, port, q)) for r in range(world)]
+    for p in ps:
+        p.start()
+    for p in ps:
+        p.join(120)
+    assert all(p.exitcode == 0 for p in ps)
+    return [q.get(timeout=10) for _ in range(world)]
+
+
+def test_gather_blocks_to_the_owner_over_two_gloo_ranks():
+    """The exchange step of a sharded contraction: rank 0 receives every
+    rank's blocks and holds the unsharded C arena, bit for bit."""
+    assert all(_spawn(_gather_rank))
+
+
+def _eig_rank(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qspace_gb300.linalg import mark_keep
+    from qspace_gb300.shard import partition_eig_blocks, sharded_mark_keep
+    rng = np.random.default_rng(5)
+    n = rng.integers(1, 30, size=23)
+    E = []
+    for k in n:                       # spectra with exact two-fold degeneracies
+        e = np.sort(np.round(rng.standard_normal(int(k)), 3))
+        E.append(e)
+    parts = partition_eig_blocks(n, world)
+    out = []
+    for nkeep, etrunc, deps in ((50, 0.0, 0.0), (120, 0.0, 1e-6), (200, 1.5, 0.0), (-1, 0.8, 1e-9)):
+        mine, nk, et = sharded_mark_keep([E[int(b)] for b in parts[rank]], parts, len(n), dist, nkeep, etrunc, deps)
+        ref, nkr, etr = mark_keep(E, nkeep, etrunc, deps)
+        out.append(nk == nkr and et == etr and all(np.array_equal(m, ref[int(b)]) for m, b in zip(mine, parts[rank])))
+    q.put(all(out))
+    dist.destroy_process_group()
+
+
+def test_sharded_eig_truncation_agrees_with_one_process():
+    """Block eigendecomposition sharded by symmetry block: after the one
+    all-gather of the eigenvalues every rank's markSet keeps exactly the
+    states the unsharded truncation keeps in its blocks (Nkeep, Etrunc and
+    degeneracy averaging)."""
+    assert all(_spawn(_eig_rank))
