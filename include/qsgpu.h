@@ -385,12 +385,23 @@ QS_EXPORT qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E
                        double deps, uint8_t *keep, int64_t *nkeep_out,
                        double *etrunc_out);
 
+/* qs_mark_keep with the eigenvalues on the device (E: device array, blocks'
+ * ascending eigenvalues back to back; n: host array of block sizes) and the
+ * 0/1 flags written to the device array `keep`; NK and Etrunc as
+ * qs_mark_keep reports them, from the same arithmetic (the stable order by
+ * merging the blocks' runs and the degeneracy averaging run on the device;
+ * only the values around the cut reach the host). */
+QS_EXPORT qs_status qs_mark_keep_dev(qs_ctx *ctx, int64_t nblk, const int64_t *n, const double *E,
+                       int64_t nkeep, double etrunc, double deps, uint8_t *keep,
+                       int64_t *nkeep_out, double *etrunc_out);
+
 /* eigQS on a device-resident block-diagonal rank-2 QSpace H (EigenSymmetric,
  * Source/QSpace.cc:4673-4939, with markSet): block eig on the device, the
  * global truncation (as qs_mark_keep) from the eigenvalues, and the kept /
  * discarded eigenvectors as new device tensors *AK / *AD (legs: H's first
  * leg and the eigenstate index, labels of H's block; blocks without kept
- * resp. discarded states are omitted).  Optional host outputs: E (sum of the
+ * resp. discarded states are omitted).  The truncation runs on the device
+ * (qs_mark_keep_dev): the eigenvalues reach the host only when E is given.  Optional host outputs: E (sum of the
  * block sizes) = ascending eigenvalues per block in H's block order, keep =
  * 0/1 per eigenvalue, NK as qs_mark_keep reports it (not always the kept
  * count: count the kept states from `keep` or from *AK's blocks) and the
@@ -467,6 +478,15 @@ QS_EXPORT qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const cha
 QS_EXPORT qs_status qs_server_poll(qs_server *s, int64_t ticket, int32_t timeout_ms,
                          int32_t *done, qs_tensor **C, double *latency_ms);
 QS_EXPORT qs_status qs_server_cancel(qs_server *s, int64_t ticket);
+/* qs_server_submit for a client with its own context `client` (same device;
+ * NULL = the server's context): the request waits for the work queued on the
+ * client's stream so far, and its result tensor belongs to the client's
+ * context, so the client may keep using it on its own stream and frees it
+ * there. */
+QS_EXPORT qs_status qs_server_submit_from(qs_server *s, qs_ctx *client, const qs_tensor *A,
+                                          const char *ia, const qs_tensor *B, const char *ib,
+                                          const int32_t *perm, int32_t nperm, const qs_opts *opts,
+                                          int64_t *ticket);
 /* An eigQS request: qs_eigQS_dev of the device-resident rank-2 QSpace H
  * (EigenSymmetric + markSet, Source/QSpace.cc:4673-4939) with the truncation
  * options nkeep / etrunc / deps, run on a slot stream beside the contraction
@@ -474,6 +494,9 @@ QS_EXPORT qs_status qs_server_cancel(qs_server *s, int64_t ticket);
  * request completes. */
 QS_EXPORT qs_status qs_server_submit_eig(qs_server *s, const qs_tensor *H, int64_t nkeep, double etrunc,
                                          double deps, int64_t *ticket);
+/* The same for a client with its own context (as qs_server_submit_from). */
+QS_EXPORT qs_status qs_server_submit_eig_from(qs_server *s, qs_ctx *client, const qs_tensor *H,
+                                              int64_t nkeep, double etrunc, double deps, int64_t *ticket);
 /* Completion of an eig request, as qs_server_poll: *AK / *AD receive the
  * kept / discarded eigenvector tensors (owned by the caller; NULL to drop),
  * E and keep (optional host arrays of sum(block sizes) entries) the

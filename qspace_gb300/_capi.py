@@ -141,6 +141,8 @@ SIGNATURES = {
                                 C.c_void_p, C.c_void_p, C.c_int32]),
     "qs_mark_keep": (C.c_int, [C.c_int64, c_int64_p, c_double_p, c_double_p, C.c_int64, C.c_double,
                                C.c_double, C.POINTER(C.c_uint8), c_int64_p, c_double_p]),
+    "qs_mark_keep_dev": (C.c_int, [C.c_void_p, C.c_int64, c_int64_p, C.c_void_p, C.c_int64, C.c_double,
+                                   C.c_double, C.c_void_p, c_int64_p, c_double_p]),
     "qs_svd_blocks": (C.c_int, [C.c_void_p, C.c_int64, c_int64_p, c_int64_p, c_int64_p, c_int64_p,
                                 c_int64_p, c_int64_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p]),
@@ -158,6 +160,10 @@ SIGNATURES = {
     "qs_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
     "qs_server_submit_eig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double,
                                        c_int64_p]),
+    "qs_server_submit_eig_from": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_double,
+                                            C.c_double, c_int64_p]),
+    "qs_server_submit_from": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_void_p,
+                                        C.c_char_p, c_int32_p, C.c_int32, C.POINTER(Opts), c_int64_p]),
     "qs_server_poll_eig": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_int32),
                                      C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), c_double_p,
                                      C.POINTER(C.c_uint8), c_int64_p, c_double_p, c_double_p]),

@@ -264,6 +264,223 @@ void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nke
   if (etrunc_out) *etrunc_out = (l < N) ? s[l] - s[0] : 0.0;
 }
 
+// ------------------------------------------------------ markSet on device
+// The same truncation with the eigenvalues left on the device: the global
+// stable ascending order comes from merging the blocks' ascending runs
+// (ties keep the block order, as std::stable_sort over the global index
+// does), the degeneracy averaging runs one thread per cluster with the host's
+// summation order, and the first level above E_min + Etrunc is found on the
+// device.  Only the values around the cut that the weighted-gap search
+// reads (at most 2 NX + 1 of them) and s[0], s[N-1] travel to the host, which
+// takes the remaining scalar decisions with the host code's arithmetic, so
+// keep flags, NK and Etrunc are identical to mark_keep_host.
+
+// Merges runs 2j and 2j+1 of (v, idx) (run r = [bnd[r], bnd[r+1])) into out.
+__global__ void merge_runs_kernel(const double *__restrict__ v, const int64_t *__restrict__ ix,
+                                  double *__restrict__ ov, int64_t *__restrict__ oix,
+                                  const int64_t *__restrict__ bnd, int nruns, int64_t N) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nruns;  // run r with bnd[r] <= e < bnd[r+1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (bnd[mid] <= e) lo = mid; else hi = mid;
+    }
+    const int r = lo, p = r ^ 1;
+    const double x = v[e];
+    int64_t pos;
+    if (p >= nruns) {
+      pos = e;
+    } else {
+      const int64_t b0 = bnd[p], b1 = bnd[p + 1];
+      int64_t a = b0, z = b1;
+      if (r & 1) {  // second run: elements of the first run that are <= x go first
+        while (a < z) { const int64_t m = (a + z) / 2; if (v[m] <= x) a = m + 1; else z = m; }
+      } else {      // first run: elements of the second run that are < x go first
+        while (a < z) { const int64_t m = (a + z) / 2; if (v[m] < x) a = m + 1; else z = m; }
+      }
+      const int64_t start = bnd[r & ~1];
+      pos = start + (e - bnd[r]) + (a - b0);
+    }
+    ov[pos] = x;
+    oix[pos] = ix[e];
+  }
+}
+
+__global__ void iota_kernel(int64_t *p, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = i;
+}
+
+// s (sorted) -> a: clusters of consecutive levels closer than
+// eps = deps |s[N-1] - s[0]| replaced by their mean (summed in order);
+__global__ void average_clusters_kernel(const double *__restrict__ s, double *__restrict__ a, int64_t N,
+                                        double deps) {
+  const double eps = deps * fabs(s[N - 1] - s[0]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!(deps > 0)) {
+      a[i] = s[i];
+      continue;
+    }
+    if (i > 0 && !(fabs(s[i] - s[i - 1]) > eps)) continue;  // not the first level of its cluster
+    int64_t j = i + 1;
+    while (j < N && !(fabs(s[j] - s[j - 1]) > eps)) ++j;
+    const int64_t d = j - i;
+    if (d > 1) {
+      double avg = 0;
+      for (int64_t t = i; t < j; ++t) avg += s[t];
+      avg /= (double)d;
+      for (int64_t t = i; t < j; ++t) a[t] = avg;
+    } else {
+      a[i] = s[i];
+    }
+  }
+}
+
+// the first l >= 1 with a[l] >= a[0] + etrunc (a ascending), by atomicMin
+__global__ void first_above_kernel(const double *__restrict__ a, int64_t N, double etrunc,
+                                   unsigned long long *lcut) {
+  const double x = etrunc + a[0];
+  for (int64_t l = 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < N; l += (int64_t)gridDim.x * blockDim.x)
+    if (a[l] >= x) atomicMin(lcut, (unsigned long long)l);
+}
+
+__global__ void scatter_keep_kernel(const int64_t *__restrict__ P, int64_t N, int64_t l, uint8_t *__restrict__ keep) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    keep[P[i]] = i < l ? 1 : 0;
+}
+
+// kept levels of each block (its lowest ones: a prefix of the block)
+__global__ void count_kept_kernel(const uint8_t *__restrict__ keep, const int64_t *__restrict__ eoffs,
+                                  const int64_t *__restrict__ n, int64_t nblk, int64_t *__restrict__ k) {
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nblk; b += (int64_t)gridDim.x * blockDim.x) {
+    int64_t c = 0;
+    for (int64_t t = 0; t < n[b]; ++t) c += keep[eoffs[b] + t];
+    k[b] = c;
+  }
+}
+
+// Device counterpart of mark_keep_host: dE holds the ascending eigenvalues
+// of block i at eoffs[i] (host arrays n, eoffs); d_keep (device, N bytes)
+// receives the flags and kcount (host) the kept levels per block.
+void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoffs, const double *dE,
+                   int64_t nkeep_in, double etrunc, double deps, uint8_t *d_keep, std::vector<int64_t> &kcount,
+                   int64_t *nkeep_out, double *etrunc_out) {
+  int64_t N = 0;
+  for (int64_t i = 0; i < nblk; ++i) N += n[i];
+  kcount.assign((size_t)std::max<int64_t>(nblk, 0), 0);
+  if (nkeep_out) *nkeep_out = 0;
+  if (etrunc_out) *etrunc_out = etrunc;
+  if (N == 0) return;
+  cudaStream_t st = ctx->stream;
+  const int grid = (int)std::min<int64_t>((N + 255) / 256, (int64_t)std::max(ctx->num_sms, 1) * 8);
+  int64_t Nkeep = (nkeep_in < 0 || nkeep_in > N) ? N : nkeep_in;
+  int64_t l = 0;
+  std::vector<void *> tmp;
+  auto alloc = [&](size_t bytes) {
+    void *p = dev_alloc<uint8_t>(ctx, std::max<size_t>(bytes, 16));
+    tmp.push_back(p);
+    return p;
+  };
+  try {
+    if (Nkeep == 0 || (Nkeep >= N && etrunc <= 0)) {
+      l = Nkeep == 0 ? 0 : N;
+      QS_CUDA(cudaMemsetAsync(d_keep, l ? 1 : 0, (size_t)N, st));
+    } else {
+      // stable ascending order: log2(nblk) rounds of pairwise run merges
+      double *v0 = static_cast<double *>(alloc(N * 8)), *v1 = static_cast<double *>(alloc(N * 8));
+      int64_t *i0 = static_cast<int64_t *>(alloc(N * 8)), *i1 = static_cast<int64_t *>(alloc(N * 8));
+      QS_CUDA(cudaMemcpyAsync(v0, dE, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+      iota_kernel<<<grid, 256, 0, st>>>(i0, N);
+      QS_LAUNCHED(ctx);
+      std::vector<int64_t> bnd;
+      for (int64_t b = 0; b < nblk; ++b)
+        if (n[b] > 0) bnd.push_back(eoffs[b]);
+      bnd.push_back(N);
+      int64_t *d_bnd = static_cast<int64_t *>(alloc(bnd.size() * 8));
+      while (bnd.size() > 2) {
+        if (bnd.size() - 1 > 0x7fffffff) fail(QS_ERR_SHAPE, "markSet: too many blocks");
+        QS_CUDA(cudaMemcpyAsync(d_bnd, bnd.data(), bnd.size() * 8, cudaMemcpyHostToDevice, st));
+        merge_runs_kernel<<<grid, 256, 0, st>>>(v0, i0, v1, i1, d_bnd, (int)(bnd.size() - 1), N);
+        QS_LAUNCHED(ctx);
+        std::swap(v0, v1);
+        std::swap(i0, i1);
+        std::vector<int64_t> nb;
+        for (size_t r = 0; r + 1 < bnd.size(); r += 2) nb.push_back(bnd[r]);
+        nb.push_back(N);
+        bnd.swap(nb);  // the next round's boundary upload is stream-ordered after this merge
+      }
+      // v0 = sorted levels, i0 = their global indices; averaged levels in v1
+      unsigned long long *d_l = static_cast<unsigned long long *>(alloc(8));
+      const unsigned long long lN = (unsigned long long)N;
+      QS_CUDA(cudaMemcpyAsync(d_l, &lN, 8, cudaMemcpyHostToDevice, st));
+      average_clusters_kernel<<<grid, 256, 0, st>>>(v0, v1, N, deps);
+      QS_LAUNCHED(ctx);
+      if (etrunc > 0) {
+        first_above_kernel<<<grid, 256, 0, st>>>(v1, N, etrunc, d_l);
+        QS_LAUNCHED(ctx);
+      }
+      double ends[2];
+      unsigned long long lfirst = lN;
+      QS_CUDA(cudaMemcpyAsync(&ends[0], v1, 8, cudaMemcpyDeviceToHost, st));
+      QS_CUDA(cudaMemcpyAsync(&ends[1], v1 + N - 1, 8, cudaMemcpyDeviceToHost, st));
+      QS_CUDA(cudaMemcpyAsync(&lfirst, d_l, 8, cudaMemcpyDeviceToHost, st));
+      QS_CUDA(cudaStreamSynchronize(st));
+      l = etrunc > 0 ? std::min<int64_t>((int64_t)lfirst, Nkeep) : Nkeep;
+      if (l < N && l > 0 && deps > 0) {
+        // weighted-gap search over the window around the cut (host arithmetic)
+        const int64_t nx = std::max<int64_t>(16, l / 5);
+        const double q = 10.0 / (double)nx;
+        const int64_t NX = (int64_t)(5.0 / q);
+        int64_t i = std::max<int64_t>(1, l - NX);
+        const int64_t i2 = std::min<int64_t>(N, l + NX);
+        std::vector<double> w((size_t)(i2 - i + 1));
+        QS_CUDA(cudaMemcpyAsync(w.data(), v1 + (i - 1), w.size() * 8, cudaMemcpyDeviceToHost, st));
+        QS_CUDA(cudaStreamSynchronize(st));
+        const int64_t w0 = i - 1;
+        int64_t imax = l;
+        double xmax = 0;
+        for (; i < i2; ++i) {
+          const double t = q * (double)(i - l);
+          const double x = std::exp(-t * t) * std::fabs(w[i - w0] - w[i - 1 - w0]);
+          if (x > xmax) { xmax = x; imax = i; }
+        }
+        if (i == N) {
+          const double t = q * (double)(i - l);
+          const double x = 0.1 * std::exp(-t * t) * std::fabs(ends[1] - ends[0]);
+          if (x > xmax) { xmax = x; imax = i; }
+        }
+        l = imax;
+      }
+      if (l >= N) l = N;
+      scatter_keep_kernel<<<grid, 256, 0, st>>>(i0, N, l, d_keep);
+      QS_LAUNCHED(ctx);
+      if (etrunc_out) {
+        double sl = 0;
+        if (l < N) {
+          QS_CUDA(cudaMemcpyAsync(&sl, v1 + l, 8, cudaMemcpyDeviceToHost, st));
+          QS_CUDA(cudaStreamSynchronize(st));
+        }
+        *etrunc_out = (l < N) ? sl - ends[0] : 0.0;
+      }
+    }
+    int64_t *d_n = static_cast<int64_t *>(alloc(nblk * 8)), *d_eo = static_cast<int64_t *>(alloc(nblk * 8));
+    int64_t *d_k = static_cast<int64_t *>(alloc(nblk * 8));
+    QS_CUDA(cudaMemcpyAsync(d_n, n, nblk * 8, cudaMemcpyHostToDevice, st));
+    QS_CUDA(cudaMemcpyAsync(d_eo, eoffs, nblk * 8, cudaMemcpyHostToDevice, st));
+    count_kept_kernel<<<(int)std::min<int64_t>((nblk + 127) / 128, 1024), 128, 0, st>>>(d_keep, d_eo, d_n, nblk, d_k);
+    QS_LAUNCHED(ctx);
+    QS_CUDA(cudaMemcpyAsync(kcount.data(), d_k, nblk * 8, cudaMemcpyDeviceToHost, st));
+    QS_CUDA(cudaStreamSynchronize(st));
+  } catch (...) {
+    cudaStreamSynchronize(st);
+    for (void *p : tmp) dev_free(ctx, p);
+    throw;
+  }
+  for (void *p : tmp) dev_free(ctx, p);
+  if (nkeep_out) *nkeep_out = (etrunc > 0 && !(deps > 0)) ? Nkeep : l;
+  if (etrunc_out && (Nkeep == 0 || (Nkeep >= N && etrunc <= 0))) *etrunc_out = etrunc;
+}
+
 // ------------------------------------------------------- svd truncation
 // The truncation of svdQS: SVD_Data::dmrgTruncate (Source/mpsortho.cc:
 // 616-700) with markSet in descending mode (Source/gathered.cc:1822-1880,
@@ -791,24 +1008,20 @@ void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double
   const int es = m.cplx ? 2 : 1;
   double *U = dev_alloc<double>(c, (size_t)std::max<int64_t>(m.nelem, 1) * es);
   double *dE = dev_alloc<double>(c, (size_t)std::max<int64_t>(ntot, 1));
+  uint8_t *d_keep = nullptr;
   std::vector<double> hE((size_t)std::max<int64_t>(ntot, 1));
   std::vector<uint8_t> hk((size_t)std::max<int64_t>(ntot, 1));
   int64_t nk = 0;
   double et = 0;
   try {
     eig_blocks(c, nb, n.data(), m.offs.data(), eoffs.data(), H->d, dE, U, m.cplx);
-    if (ntot) QS_CUDA(cudaMemcpyAsync(hE.data(), dE, ntot * 8, cudaMemcpyDeviceToHost, c->stream));
-    QS_CUDA(cudaStreamSynchronize(c->stream));
-    mark_keep_host(nb, n.data(), hE.data(), nkeep, etrunc, deps, hk.data(), &nk, &et);
-    // kept / discarded parts of each block
-    std::vector<int64_t> k(nb);
-    for (int64_t i = 0; i < nb; ++i) {
-      int64_t j = 0;
-      while (j < n[i] && hk[eoffs[i] + j]) ++j;
-      k[i] = j;
-      for (int64_t t = j; t < n[i]; ++t)
-        if (hk[eoffs[i] + t]) fail(QS_ERR_INTERNAL, "eigQS: kept states of block %lld are not its lowest", (long long)i);
-    }
+    // markSet on the device: the eigenvalues stay there; the host gets the
+    // kept count of every block (a prefix: its lowest levels)
+    std::vector<int64_t> k;
+    d_keep = dev_alloc<uint8_t>(c, (size_t)std::max<int64_t>(ntot, 1));
+    mark_keep_dev(c, nb, n.data(), eoffs.data(), dE, nkeep, etrunc, deps, d_keep, k, &nk, &et);
+    if (E && ntot) QS_CUDA(cudaMemcpyAsync(hE.data(), dE, ntot * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (keep && ntot) QS_CUDA(cudaMemcpyAsync(hk.data(), d_keep, ntot, cudaMemcpyDeviceToHost, c->stream));
     auto part = [&](bool kept) {
       auto T = std::make_unique<qs_tensor>();
       T->ctx = c;
@@ -850,9 +1063,12 @@ void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double
       return T;
     };
     std::unique_ptr<qs_tensor> tk = part(true), td = part(false);
+    QS_CUDA(cudaStreamSynchronize(c->stream));  // host copies of E / keep
     dev_free(c, U);
     dev_free(c, dE);
+    dev_free(c, d_keep);
     U = dE = nullptr;
+    d_keep = nullptr;
     if (E && ntot) std::memcpy(E, hE.data(), ntot * 8);
     if (keep && ntot) std::memcpy(keep, hk.data(), ntot);
     if (nkeep_out) *nkeep_out = nk;
@@ -860,8 +1076,10 @@ void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double
     AK = std::move(tk);
     AD = std::move(td);
   } catch (...) {
+    cudaStreamSynchronize(c->stream);
     if (U) dev_free(c, U);
     if (dE) dev_free(c, dE);
+    if (d_keep) dev_free(c, d_keep);
     throw;
   }
 }
@@ -886,6 +1104,23 @@ qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double et
   eigqs_core(&ctx->c, H, nkeep, etrunc, deps, tk, td, E, keep, nkeep_out, etrunc_out);
   *AK = tk.release();
   *AD = td.release();
+  QS_API_END
+}
+
+qs_status qs_mark_keep_dev(qs_ctx *ctx, int64_t nblk, const int64_t *n, const double *E, int64_t nkeep,
+                           double etrunc, double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
+  QS_API_BEGIN
+  if (!ctx || nblk < 0 || (nblk > 0 && (!n || !E || !keep))) fail(QS_ERR_ARG, "null argument");
+  std::vector<int64_t> eoffs((size_t)nblk);
+  int64_t tot = 0;
+  for (int64_t i = 0; i < nblk; ++i) {
+    if (n[i] < 0) fail(QS_ERR_ARG, "negative block size");
+    eoffs[i] = tot;
+    tot += n[i];
+  }
+  QS_CUDA(cudaSetDevice(ctx->c.device));
+  std::vector<int64_t> k;
+  mark_keep_dev(&ctx->c, nblk, n, eoffs.data(), E, nkeep, etrunc, deps, keep, k, nkeep_out, etrunc_out);
   QS_API_END
 }
 

@@ -5,7 +5,9 @@
 //
 //  * qs_server_submit enqueues a request (FIFO) and records an event on the
 //    submitting context's stream, so the request sees every earlier write to
-//    its operands.
+//    its operands; the results belong to that context (freed on its stream,
+//    after its own later uses).  qs_server_submit_from names the submitting
+//    context (one per client instance); qs_server_submit uses the server's.
 //  * nslots worker threads each own a stream, a scratch arena and an error
 //    word (a qs::Ctx).  A worker takes the head of the queue as soon as the
 //    request's device footprint fits into the HBM budget next to the
@@ -49,6 +51,7 @@ struct Request {
   qs_opts opts{};
   bool has_opts = false;
   cudaEvent_t ready = nullptr;
+  Ctx *owner = nullptr;            // context whose stream orders the request and frees its results
   int64_t footprint = 0;
   clk::time_point t_submit;
   enum State { QUEUED, RUNNING, DONE, FAILED, CANCELLED } state = QUEUED;
@@ -140,7 +143,7 @@ struct qs_server {
                                  r.perm.empty() ? nullptr : r.perm.data(), (int32_t)r.perm.size(),
                                  r.has_opts ? &r.opts : nullptr, nullptr);
           QS_CUDA(cudaStreamSynchronize(slot->stream));
-          T->ctx = &parent->c;  // the caller frees the result on the parent context's stream
+          T->ctx = r.owner;  // the submitter frees the result on its context's stream
           C[k] = T.release();
         } catch (const Error &e) {
           st[k] = e.code;
@@ -163,8 +166,8 @@ struct qs_server {
             r.keep.assign((size_t)std::max<int64_t>(ntot, 1), 0);
             eigqs_core(slot, r.A, r.nkeep, r.etrunc, r.deps, tk, td, r.E.data(), r.keep.data(), &r.nk, &r.et);
             QS_CUDA(cudaStreamSynchronize(slot->stream));
-            tk->ctx = &parent->c;
-            td->ctx = &parent->c;
+            tk->ctx = r.owner;
+            td->ctx = r.owner;
             C[0] = tk.release();
             r.D = td.release();
           } catch (const Error &e) {
@@ -199,7 +202,7 @@ struct qs_server {
                                 pp.data(), np.data(), batch[0]->has_opts ? &batch[0]->opts : nullptr, out);
             QS_CUDA(cudaStreamSynchronize(slot->stream));
             for (int k = 0; k < n; ++k) {
-              out[k]->ctx = &parent->c;
+              out[k]->ctx = batch[k]->owner;
               C[k] = out[k].release();
             }
           } catch (...) {
@@ -280,8 +283,16 @@ void qs_server_destroy(qs_server *s) {
 
 qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const char *ia, const qs_tensor *B, const char *ib,
                            const int32_t *perm, int32_t nperm, const qs_opts *opts, int64_t *ticket) {
+  return qs_server_submit_from(s, nullptr, A, ia, B, ib, perm, nperm, opts, ticket);
+}
+
+qs_status qs_server_submit_from(qs_server *s, qs_ctx *client, const qs_tensor *A, const char *ia,
+                                const qs_tensor *B, const char *ib, const int32_t *perm, int32_t nperm,
+                                const qs_opts *opts, int64_t *ticket) {
   QS_API_BEGIN
   if (!s || !A || !B || !ia || !ib || !ticket) fail(QS_ERR_ARG, "null argument");
+  Ctx *owner = client ? &client->c : &s->parent->c;
+  if (owner->device != s->parent->c.device) fail(QS_ERR_ARG, "the client context is on another device");
   // validate the request on the host now: a malformed request fails here,
   // not in a worker
   (void)parse_ctr_idx(ia);
@@ -301,9 +312,10 @@ qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const char *ia, con
     r->has_opts = true;
   }
   r->footprint = fp;
+  r->owner = owner;
   QS_CUDA(cudaSetDevice(s->parent->c.device));
   QS_CUDA(cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming));
-  QS_CUDA(cudaEventRecord(r->ready, s->parent->c.stream));
+  QS_CUDA(cudaEventRecord(r->ready, owner->stream));
   {
     std::lock_guard<std::mutex> lk(s->mu);
     r->ticket = s->next_ticket++;
@@ -318,8 +330,15 @@ qs_status qs_server_submit(qs_server *s, const qs_tensor *A, const char *ia, con
 
 qs_status qs_server_submit_eig(qs_server *s, const qs_tensor *H, int64_t nkeep, double etrunc, double deps,
                                int64_t *ticket) {
+  return qs_server_submit_eig_from(s, nullptr, H, nkeep, etrunc, deps, ticket);
+}
+
+qs_status qs_server_submit_eig_from(qs_server *s, qs_ctx *client, const qs_tensor *H, int64_t nkeep,
+                                    double etrunc, double deps, int64_t *ticket) {
   QS_API_BEGIN
   if (!s || !H || !ticket) fail(QS_ERR_ARG, "null argument");
+  Ctx *owner = client ? &client->c : &s->parent->c;
+  if (owner->device != s->parent->c.device) fail(QS_ERR_ARG, "the client context is on another device");
   if (H->meta.rank != 2) fail(QS_ERR_SHAPE, "eig request: rank-2 QSpace required (got rank %d)", H->meta.rank);
   const int64_t fp = eigqs_footprint(H->meta);
   if (fp > s->budget)
@@ -332,9 +351,10 @@ qs_status qs_server_submit_eig(qs_server *s, const qs_tensor *H, int64_t nkeep, 
   r->etrunc = etrunc;
   r->deps = deps;
   r->footprint = fp;
+  r->owner = owner;
   QS_CUDA(cudaSetDevice(s->parent->c.device));
   QS_CUDA(cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming));
-  QS_CUDA(cudaEventRecord(r->ready, s->parent->c.stream));
+  QS_CUDA(cudaEventRecord(r->ready, owner->stream));
   {
     std::lock_guard<std::mutex> lk(s->mu);
     r->ticket = s->next_ticket++;

@@ -69,6 +69,27 @@ def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float 
     return [keep[o:o + k].astype(bool) for o, k in zip(offs, n)], nk.value, et.value
 
 
+def mark_keep_dev(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0,
+                  ctx: Context | None = None):
+    """The same truncation with the eigenvalues on the device
+    (qs_mark_keep_dev): the values are uploaded, the flags come back."""
+    import torch
+    ctx = ctx or default_context()
+    n = np.array([len(e) for e in E_blocks], np.int64)
+    E = np.concatenate([np.asarray(e, np.float64) for e in E_blocks]) if E_blocks else np.zeros(0)
+    dev = torch.device("cuda", ctx.device)
+    dE = torch.from_numpy(E.copy()).to(dev)
+    dk = torch.zeros(max(len(E), 1), dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize(dev)
+    nk, et = C.c_int64(), C.c_double()
+    check(ctx.lib.qs_mark_keep_dev(ctx.h, len(n), _ptr(n), C.c_void_p(dE.data_ptr()), int(nkeep), float(etrunc),
+                                   float(deps), C.c_void_p(dk.data_ptr()), C.byref(nk), C.byref(et)))
+    ctx.sync()
+    keep = dk.cpu().numpy()
+    offs = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+    return [keep[o:o + k].astype(bool) for o, k in zip(offs, n)], nk.value, et.value
+
+
 def eigQS(H: QSpace, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0, ctx: Context | None = None):
     """Block eigendecomposition + truncation of a block-diagonal rank-2
     abelian QSpace.  Returns (Etot, I) with Etot the ascending eigenvalues of

@@ -203,9 +203,10 @@ class ServingBackend(DeviceBackend):
     """The iteration with its contractions and its eigQS sent as requests to
     a serving loop (qspace_gb300.serve.Server): the way many NRG runs share
     one GPU.  Uploads, permutations and sums run on the instance's own
-    context, which is synchronised before each request (the server orders a
-    request after its submitter's stream of the server's parent context
-    only).  Request latencies (submit to completion) are recorded per kind."""
+    context; requests are submitted as that context's client
+    (qs_server_submit_from), so each waits for the instance's queued work
+    and its results belong to the instance's context.  Request latencies
+    (submit to completion) are recorded per kind."""
 
     def __init__(self, server, ctx=None, prec: str = "fp64"):
         super().__init__(ctx, prec)
@@ -213,14 +214,12 @@ class ServingBackend(DeviceBackend):
         self.latency = {"contract": [], "eig": []}
 
     def contract(self, A, ia, B, ib):
-        self.ctx.sync()
-        T, ms = self.server.wait(self.server.submit(A, ia, B, ib, prec=self.prec))
+        T, ms = self.server.wait(self.server.submit(A, ia, B, ib, prec=self.prec, client=self.ctx))
         self.latency["contract"].append(ms)
         return T
 
     def eig(self, H, nkeep, deps=0.0):
-        self.ctx.sync()
-        r = self.server.wait_eig(self.server.submit_eig(H, nkeep, 0.0, deps))
+        r = self.server.wait_eig(self.server.submit_eig(H, nkeep, 0.0, deps, client=self.ctx))
         self.latency["eig"].append(r["latency_ms"])
         r["AD"].free()
         return _split_blocks(H, r["E"], r["keep"]) + (r["AK"],)

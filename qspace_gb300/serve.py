@@ -28,14 +28,20 @@ class Server:
         check(self.ctx.lib.qs_server_create(self.ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h
         self._eig_sizes = {}   # ticket -> H of pending eig requests
+        self._owner = {}       # ticket -> context that owns the result
 
     def submit(self, A: Tensor, ia, B: Tensor, ib, perm=None, prec: str = "fp64", nslices: int = 0,
-               tol: float = 1e-12) -> int:
+               tol: float = 1e-12, client: Context | None = None) -> int:
+        """Enqueue contractQS(A, ia, B, ib [,perm]).  With `client` (the
+        submitter's own context) the request is ordered after the client's
+        stream and its result belongs to the client's context
+        (qs_server_submit_from); otherwise to the server's."""
         p, n = _perm_arg(perm)
         o = make_opts(prec, nslices, tol)
         t = C.c_int64()
-        check(self.ctx.lib.qs_server_submit(self.h, A.h, _idx_str(ia), B.h, _idx_str(ib), p, n, C.byref(o),
-                                            C.byref(t)))
+        check(self.ctx.lib.qs_server_submit_from(self.h, client.h if client else None, A.h, _idx_str(ia), B.h,
+                                                 _idx_str(ib), p, n, C.byref(o), C.byref(t)))
+        self._owner[t.value] = client or self.ctx
         return t.value
 
     def poll(self, ticket: int, timeout_ms: int = 0):
@@ -43,11 +49,15 @@ class Server:
         cancelled request."""
         done, lat = C.c_int32(), C.c_double()
         h = C.c_void_p()
-        check(self.ctx.lib.qs_server_poll(self.h, int(ticket), int(timeout_ms), C.byref(done), C.byref(h),
-                                          C.byref(lat)))
+        try:
+            check(self.ctx.lib.qs_server_poll(self.h, int(ticket), int(timeout_ms), C.byref(done), C.byref(h),
+                                              C.byref(lat)))
+        except QSError:
+            self._owner.pop(ticket, None)
+            raise
         if not done.value:
             return False, None, None
-        return True, Tensor(self.ctx, h), lat.value
+        return True, Tensor(self._owner.pop(ticket, self.ctx), h), lat.value
 
     def wait(self, ticket: int, timeout_s: float = 60.0):
         import time
@@ -59,13 +69,16 @@ class Server:
             if time.monotonic() - t0 > timeout_s:
                 raise QSError(6, f"request {ticket} did not complete in {timeout_s} s")
 
-    def submit_eig(self, H: Tensor, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0) -> int:
+    def submit_eig(self, H: Tensor, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0,
+                   client: Context | None = None) -> int:
         """Enqueue eigQS(H, 'Nkeep', nkeep, 'Etrunc', etrunc) of a device
-        tensor (qs_server_submit_eig).  H must stay alive until the result is
-        collected."""
+        tensor (qs_server_submit_eig_from; `client` as for submit).  H must
+        stay alive until the result is collected."""
         t = C.c_int64()
-        check(self.ctx.lib.qs_server_submit_eig(self.h, H.h, int(nkeep), float(etrunc), float(deps), C.byref(t)))
+        check(self.ctx.lib.qs_server_submit_eig_from(self.h, client.h if client else None, H.h, int(nkeep),
+                                                     float(etrunc), float(deps), C.byref(t)))
         self._eig_sizes[t.value] = H
+        self._owner[t.value] = client or self.ctx
         return t.value
 
     def poll_eig(self, ticket: int, timeout_ms: int = 0):
@@ -90,11 +103,13 @@ class Server:
                                                   C.byref(et), C.byref(lat)))
         except QSError:
             self._eig_sizes.pop(ticket, None)
+            self._owner.pop(ticket, None)
             raise
         if not done.value:
             return False, None
         self._eig_sizes.pop(ticket, None)
-        return True, {"AK": Tensor(self.ctx, ak), "AD": Tensor(self.ctx, ad), "E": E[:ntot],
+        owner = self._owner.pop(ticket, self.ctx)
+        return True, {"AK": Tensor(owner, ak), "AD": Tensor(owner, ad), "E": E[:ntot],
                       "keep": keep[:ntot].astype(bool), "NK": nk.value, "Etrunc": et.value,
                       "latency_ms": lat.value}
 
