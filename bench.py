@@ -284,13 +284,16 @@ def serve_nrg_bench(ctx, prec: str, runs: int = 32, iters: int = 40, rate: float
     errs = []
 
     def run(be, z, rng):
+        n = -1
         try:
             K = initial_space(be, -0.2, 0.6)
             for n in range(iters):
                 time.sleep(rng.exponential(1.0 / rate))
                 K = nrg_step(K, be, wilson_hopping(n, Lam, z), Lam, nkeep=nk[n], deps=1e-8)
         except Exception as e:  # reported in the row
-            errs.append(repr(e))
+            import traceback
+            errs.append(f"z={z:.3f} iteration {n}: " + "".join(traceback.format_exception(e))[-1500:])
+            print(errs[-1], file=sys.stderr, flush=True)
 
     with Server(nslots=nslots, hbm_budget=96 << 30, ctx=ctx) as srv:
         bes = [ServingBackend(srv, Context(ctx.device), prec) for _ in range(runs)]
@@ -353,7 +356,12 @@ def main():
     torch.cuda.set_device(local)
     if a.serve_nrg:
         ctx = default_context(local)
-        rows = [serve_nrg_bench(ctx, pr, a.nrg_runs, a.nrg_iters, a.nrg_rate) for pr in ("split", "fp64")]
+        rows = []
+        for pr in ("split", "fp64"):
+            rows.append(serve_nrg_bench(ctx, pr, a.nrg_runs, a.nrg_iters, a.nrg_rate))
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+            if rows[-1]["errors"]:
+                break
         print(json.dumps({"serving_nrg": rows}))
         return 0
     pg = None

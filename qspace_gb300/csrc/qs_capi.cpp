@@ -290,12 +290,53 @@ struct Prepared {
   double *dC = nullptr;
   std::vector<void *> tmp;
   std::unique_ptr<qs_tensor> done;  // set when no product is needed
+  // per pair: strided views of operands read in place instead of permuted
+  // (split path; empty when neither operand needed a permutation)
+  std::vector<OperandView> va, vb;
 };
+
+// The view of block `blk` of m whose lines run over `line_legs` and whose
+// depth runs over `k_legs` (first leg fastest): the element order of the
+// permuted copy that permute_to would make, read in place.
+static bool make_view(const QMeta &m, int64_t blk, const std::vector<int> &line_legs, const std::vector<int> &k_legs,
+                      OperandView &v) {
+  v = OperandView{};
+  // legs of size 1 do not move anything; drop them
+  std::vector<int> ll, kl;
+  for (int k : line_legs)
+    if (m.drow(blk)[k] != 1) ll.push_back(k);
+  for (int k : k_legs)
+    if (m.drow(blk)[k] != 1) kl.push_back(k);
+  if ((int)ll.size() > VIEW_LEGS || (int)kl.size() > VIEW_LEGS) return false;
+  int64_t stride[16];
+  int64_t sacc = 1;
+  for (int k = 0; k < m.rank && k < 16; ++k) {
+    stride[k] = sacc;
+    sacc *= m.drow(blk)[k];
+  }
+  v.nl = (int32_t)ll.size();
+  v.nk = (int32_t)kl.size();
+  for (int i = 0; i < v.nl; ++i) {
+    v.ldim[i] = (int32_t)m.drow(blk)[ll[i]];
+    v.lstr[i] = stride[ll[i]];
+  }
+  for (int i = 0; i < v.nk; ++i) {
+    v.kdim[i] = (int32_t)m.drow(blk)[kl[i]];
+    v.kstr[i] = stride[kl[i]];
+  }
+  if (v.nl == 0) {  // a single line: one leg of size 1 keeps the view active
+    v.nl = 1;
+    v.ldim[0] = 1;
+    v.lstr[0] = 0;
+  }
+  return true;
+}
 
 // Plan on the host, then widen/permute the operands as the plan wants and
 // allocate the output (kernels on ctx->stream).
 static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, const QMeta &Bm,
-                    const double *dB, const char *ia, const char *ib, const int32_t *perm, int32_t nperm) {
+                    const double *dB, const char *ia, const char *ib, const int32_t *perm, int32_t nperm,
+                    bool views = false) {
   w.pl = plan_contract(Am, ia, Bm, ib, perm, nperm);
   ContractPlan &pl = w.pl;
   const bool cplx = w.cplx = pl.C.cplx;
@@ -307,7 +348,26 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
     return;
   }
   const int es = cplx ? 2 : 1;
-  auto prep = [&](const QMeta &m, const double *d, const OperandLayout &lay) -> const double * {
+  // The split path reads a permuted operand in place through per-pair
+  // strided views (lines over the kept legs, depth over the contracted legs
+  // in pairing order, the order of permute_to's copy) when every block's legs
+  // fit a view; the FP64 path reads the permuted copy.
+  auto fused = [&](const QMeta &m, bool is_a, std::vector<OperandView> &out) -> bool {
+    const OperandLayout &lay = is_a ? pl.la : pl.lb;
+    if (!views || !lay.permute) return false;
+    const std::vector<int> &lines = is_a ? pl.ika : pl.ikb;
+    const std::vector<int> &ks = is_a ? pl.ica.idx : pl.icb.idx;
+    std::vector<OperandView> v(pl.pairs.size());
+    for (size_t p = 0; p < pl.pairs.size(); ++p)
+      if (!make_view(m, is_a ? pl.pair_ia[p] : pl.pair_ib[p], lines, ks, v[p])) return false;
+    out.swap(v);
+    // the permuted copy would have been conjugated: conjugate on the fly
+    if (lay.conj)
+      for (PairDesc &d : pl.pairs) d.trans |= is_a ? 4 : 8;
+    return true;
+  };
+  const bool fa = fused(Am, true, w.va), fb = fused(Bm, false, w.vb);
+  auto prep = [&](const QMeta &m, const double *d, const OperandLayout &lay, bool in_place) -> const double * {
     const double *cur = d;
     if (cplx && !m.cplx) {
       double *x = dev_alloc<double>(ctx, (size_t)m.nelem * 2);
@@ -315,7 +375,7 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
       launch_widen(ctx, d, x, m.nelem);
       cur = x;
     }
-    if (lay.permute) {
+    if (lay.permute && !in_place) {
       double *o = dev_alloc<double>(ctx, (size_t)m.nelem * es);
       w.tmp.push_back(o);
       std::vector<PermDesc> pd = make_perm_descs(m, lay.perm, lay.conj, m.offs);
@@ -324,8 +384,8 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
     }
     return cur;
   };
-  w.a2 = prep(Am, dA, pl.la);
-  w.b2 = prep(Bm, dB, pl.lb);
+  w.a2 = prep(Am, dA, pl.la, fa);
+  w.b2 = prep(Bm, dB, pl.lb, fb);
   w.dC = dev_alloc<double>(ctx, (size_t)pl.C.nelem * es);
 }
 
@@ -356,13 +416,21 @@ static void run_products(Ctx *ctx, const std::vector<Prepared *> &batch, const q
   std::vector<PairDesc> pairs;
   std::vector<int64_t> grp{0}, c_off;
   std::vector<int32_t> bM, bN;
+  std::vector<OperandView> va, vb;
+  bool any_view = false;
+  for (Prepared *w : batch) any_view = any_view || !w->va.empty() || !w->vb.empty();
   for (Prepared *w : batch) {
     const ContractPlan &pl = w->pl;
     const int64_t da = rel(w->a2, baseA), db = rel(w->b2, baseB), dc = rel(w->dC, baseC);
-    for (PairDesc d : pl.pairs) {
+    for (size_t p = 0; p < pl.pairs.size(); ++p) {
+      PairDesc d = pl.pairs[p];
       d.a_off += da;
       d.b_off += db;
       pairs.push_back(d);
+      if (any_view) {
+        va.push_back(w->va.empty() ? OperandView{} : w->va[p]);
+        vb.push_back(w->vb.empty() ? OperandView{} : w->vb[p]);
+      }
     }
     for (size_t b = 0; b + 1 < pl.grp.size(); ++b) grp.push_back(grp.back() + (pl.grp[b + 1] - pl.grp[b]));
     for (size_t b = 0; b < pl.blk_M.size(); ++b) {
@@ -375,13 +443,15 @@ static void run_products(Ctx *ctx, const std::vector<Prepared *> &batch, const q
   if (prec == QS_PREC_SPLIT) {
     SplitResult sr = run_split(ctx, pairs, grp, bM, bN, c_off, baseA, baseB, baseC, cplx,
                                forced_slices ? forced_slices : (opts ? opts->nslices : 0),
-                               opts && opts->tol > 0 ? opts->tol : 1e-12, nullptr, forced_bits);
+                               opts && opts->tol > 0 ? opts->tol : 1e-12, nullptr, forced_bits, nullptr,
+                               any_view ? &va : nullptr, any_view ? &vb : nullptr);
     if (stats) {
       stats->nslices = sr.nslices;
       stats->digit_bits = sr.bits;
       stats->err_bound = sr.err_bound;
     }
   } else if (prec == QS_PREC_FP64) {
+    if (any_view) fail(QS_ERR_INTERNAL, "FP64 products of operands read through views");
     std::vector<TileDesc> tiles = make_tiles(grp, bM, bN, c_off, gemm_f64_tile_m(), gemm_f64_tile_n());
     PairDesc *dp = dev_upload(ctx, pairs);
     TileDesc *dt = dev_upload(ctx, tiles);
@@ -519,7 +589,7 @@ std::unique_ptr<qs_tensor> contract_core(Ctx *ctx, const QMeta &Am, const double
   Prepared w;
   if (stats) std::memset(stats, 0, sizeof *stats);
   try {
-    prepare(ctx, w, Am, dA, Bm, dB, ia, ib, perm, nperm);
+    prepare(ctx, w, Am, dA, Bm, dB, ia, ib, perm, nperm, opts && opts->prec == QS_PREC_SPLIT);
     if (stats) {
       stats->flops = w.pl.flops;
       stats->bytes = w.pl.bytes;
@@ -552,10 +622,10 @@ void contract_batch_core(Ctx *ctx, int n, const QMeta *const *Am, const double *
                          const qs_opts *opts, std::vector<std::unique_ptr<qs_tensor>> &out) {
   std::vector<Prepared> ws(n);
   try {
+    const bool split = opts && opts->prec == QS_PREC_SPLIT;
     for (int r = 0; r < n; ++r)
       prepare(ctx, ws[r], *Am[r], dA[r], *Bm[r], dB[r], ia[r], ib[r], perm ? perm[r] : nullptr,
-              nperm ? nperm[r] : 0);
-    const bool split = opts && opts->prec == QS_PREC_SPLIT;
+              nperm ? nperm[r] : 0, split);
     std::vector<std::pair<int, int>> plan(n, {0, 0});  // (slices, bits)
     if (split)
       for (int r = 0; r < n; ++r)

@@ -241,6 +241,45 @@ __device__ __forceinline__ void st_pol(uint8_t *a, uint4 v, uint64_t pol) {
                : "memory");
 }
 
+// Element (line, k) of a pair's operand in the role being sliced: plain
+// (lda/ldb, trans) addressing, or the operand's strided view when the
+// contraction reads a permuted operand in place.
+__device__ __forceinline__ int64_t view_part(int n, const int32_t *dim, const int64_t *str, int64_t idx) {
+  int64_t o = 0;
+  int32_t x = (int32_t)idx;  // line and depth indices are < 2^31
+#pragma unroll
+  for (int i = 0; i < VIEW_LEGS; ++i) {
+    if (i < n) {
+      const int32_t d = dim[i];
+      o += (int64_t)(x % d) * str[i];
+      x /= d;
+    }
+  }
+  return o;
+}
+struct OpAddr {
+  int64_t ls, ks;             // plain: line * ls + k * ks
+  const OperandView *v;       // or the view (nl > 0)
+  __device__ __forceinline__ int64_t line(int64_t m) const {
+    return v ? view_part(v->nl, v->ldim, v->lstr, m) : m * ls;
+  }
+  __device__ __forceinline__ int64_t depth(int64_t k) const {
+    return v ? view_part(v->nk, v->kdim, v->kstr, k) : k * ks;
+  }
+};
+// A role: lines are rows of op(A) (contiguous along k when transposed); B
+// role: lines are columns of op(B) (contiguous along k when not transposed).
+__device__ __forceinline__ OpAddr addr_a(const SplitPair &P, const OperandView *views, int p) {
+  const bool ta = P.trans & 1;
+  const OperandView *v = (views && views[p].nl > 0) ? views + p : nullptr;
+  return OpAddr{ta ? (int64_t)P.lda : 1, ta ? 1 : (int64_t)P.lda, v};
+}
+__device__ __forceinline__ OpAddr addr_b(const SplitPair &P, const OperandView *views, int p) {
+  const bool tb = P.trans & 2;
+  const OperandView *v = (views && views[p].nl > 0) ? views + p : nullptr;
+  return OpAddr{tb ? 1 : (int64_t)P.ldb, tb ? (int64_t)P.ldb : 1, v};
+}
+
 // ---------------------------------------------- exponents and slicing, fused
 // One CTA per strip of STRIP real lines of one output block: rows of op(A~)
 // (A role) or columns of op(B~) (B role), over every pair of the block and
@@ -267,9 +306,9 @@ constexpr int STRIP_THREADS = 128;
 // m + k*ld (contig: k + m*ld); X = B role: columns, line n at k + n*ld
 // (contig) or n + k*ld), max over the pairs p0..p1-1 into smax[line].
 template <bool CPLX, bool ROLE_B>
-__device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs, int p0, int p1, int l0, int nl,
-                                             const double *__restrict__ Aarena, const double *__restrict__ Barena,
-                                             int *smax) {
+__device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs, const OperandView *views, int p0,
+                                             int p1, int l0, int nl, const double *__restrict__ Aarena,
+                                             const double *__restrict__ Barena, int *smax) {
   if (threadIdx.x < STRIP) smax[threadIdx.x] = EMPTY_EXP;
   __syncthreads();
   for (int p = p0; p < p1; ++p) {
@@ -277,38 +316,39 @@ __device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs
     // a swapped pair's roles read the other arena
     const double *__restrict__ X = (ROLE_B != (P.swap != 0)) ? Barena : Aarena;
     const int64_t off = ROLE_B ? P.b_off : P.a_off;
-    const int64_t ld = ROLE_B ? P.ldb : P.lda;
-    // lines contiguous along k: rows of a transposed op(A), columns of a plain op(B)
-    const bool contig = ROLE_B ? !(P.trans & 2) : (P.trans & 1);
+    const OpAddr ad = ROLE_B ? addr_b(P, views, p) : addr_a(P, views, p);
+    // lines contiguous along k (unit depth stride): neighbouring lanes take
+    // neighbouring k of one line; else neighbouring lines
+    const bool contig = ad.v ? (ad.v->nk > 0 && ad.v->kstr[0] == 1) : ad.ks == 1;
     constexpr int NPH = STRIP_THREADS / STRIP;
     const int line = contig ? threadIdx.x / NPH : threadIdx.x % STRIP;
     const int ph = contig ? threadIdx.x % NPH : threadIdx.x / STRIP;
     int key = 0;
     if (line < nl) {
       const uint64_t keep = l2_policy_keep();
-      const int64_t m = l0 + line;
-      const int64_t sk = contig ? 1 : ld, base = off + (contig ? m * ld : m);
+      const int64_t base = off + ad.line(l0 + line);
       int k = ph;
       for (; k + 3 * NPH < P.K; k += 4 * NPH) {
+        const int64_t o0 = base + ad.depth(k), o1 = base + ad.depth(k + NPH), o2 = base + ad.depth(k + 2 * NPH),
+                      o3 = base + ad.depth(k + 3 * NPH);
         if (CPLX) {
-          const double2 *x = reinterpret_cast<const double2 *>(X) + base;
-          const double2 v0 = ld_pol(x + k * sk, keep), v1 = ld_pol(x + (k + NPH) * sk, keep),
-                        v2 = ld_pol(x + (k + 2 * NPH) * sk, keep), v3 = ld_pol(x + (k + 3 * NPH) * sk, keep);
+          const double2 *x = reinterpret_cast<const double2 *>(X);
+          const double2 v0 = ld_pol(x + o0, keep), v1 = ld_pol(x + o1, keep), v2 = ld_pol(x + o2, keep),
+                        v3 = ld_pol(x + o3, keep);
           key = max(key, max(max(max(exp_key(v0.x), exp_key(v0.y)), max(exp_key(v1.x), exp_key(v1.y))),
                              max(max(exp_key(v2.x), exp_key(v2.y)), max(exp_key(v3.x), exp_key(v3.y)))));
         } else {
-          const double *x = X + base;
-          key = max(key, max(max(exp_key(ld_pol(x + k * sk, keep)), exp_key(ld_pol(x + (k + NPH) * sk, keep))),
-                             max(exp_key(ld_pol(x + (k + 2 * NPH) * sk, keep)),
-                                 exp_key(ld_pol(x + (k + 3 * NPH) * sk, keep)))));
+          key = max(key, max(max(exp_key(ld_pol(X + o0, keep)), exp_key(ld_pol(X + o1, keep))),
+                             max(exp_key(ld_pol(X + o2, keep)), exp_key(ld_pol(X + o3, keep)))));
         }
       }
       for (; k < P.K; k += NPH) {
+        const int64_t o = base + ad.depth(k);
         if (CPLX) {
-          const double2 v = ld_pol(reinterpret_cast<const double2 *>(X) + base + k * sk, keep);
+          const double2 v = ld_pol(reinterpret_cast<const double2 *>(X) + o, keep);
           key = max(key, max(exp_key(v.x), exp_key(v.y)));
         } else {
-          key = max(key, exp_key(ld_pol(X + base + k * sk, keep)));
+          key = max(key, exp_key(ld_pol(X + o, keep)));
         }
       }
     }
@@ -319,7 +359,7 @@ __device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs
 
 // A role.  Task = (first pair, end pair, first real row r0 of the strip).
 template <bool CPLX, int S, int B>
-__device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int4 tk,
+__device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, const OperandView *views, int4 tk,
                                         const double *__restrict__ Aarena, const double *__restrict__ Barena,
                                         int *__restrict__ E, uint8_t *__restrict__ arena) {
   __shared__ int smax[STRIP];
@@ -328,7 +368,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
   const bool dup = CPLX && Q.dupb == 0;  // two real rows per row of op(A)
   const int l0 = dup ? r0 / 2 : r0;
   const int nl = min(dup ? STRIP / 2 : STRIP, Q.M - l0);
-  strip_maxima<CPLX, false>(pairs, p0, p1, l0, nl, Aarena, Barena, smax);
+  strip_maxima<CPLX, false>(pairs, views, p0, p1, l0, nl, Aarena, Barena, smax);
   if (threadIdx.x < nl) {
     const int e = smax[threadIdx.x];
     if (dup) {
@@ -343,7 +383,8 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
   for (int p = p0; p < p1; ++p) {
     const SplitPair &P = pairs[p];
     const double *__restrict__ A = P.swap ? Barena : Aarena;
-    const bool ta = P.trans & 1, ca = P.trans & 4;
+    const bool ca = P.trans & 4;
+    const OpAddr ad = addr_a(P, views, p);
     const Factor Fa{P.fm, P.fe, P.fneg != 0};
     uint8_t *tiles = arena + P.as_off + (int64_t)mt * P.KB * S * A_DIGIT_BYTES;
     if (dup) {
@@ -353,15 +394,14 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
         const int kb = w / ((STRIP / 2) * KCM), i = w % ((STRIP / 2) * KCM);
         const int ml = i % (STRIP / 2), q = i / (STRIP / 2);
         if (ml >= nl) continue;  // rows past the block feed discarded outputs only: not written
-        const int64_t m = l0 + ml;
+        const int64_t lo = P.a_off + ad.line(l0 + ml);
         const int Ei = smax[ml];
         double2 a[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int k = (kb * TKS + q * 8) / 2 + j;
           a[j] = make_double2(0.0, 0.0);
-          if (k < P.K)
-            a[j] = ld_pol(reinterpret_cast<const double2 *>(A) + P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda), last);
+          if (k < P.K) a[j] = ld_pol(reinterpret_cast<const double2 *>(A) + lo + ad.depth(k), last);
         }
         uint32_t p0w[S][4], p1w[S][4];
 #pragma unroll
@@ -392,7 +432,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
         const int kb = w / (STRIP * KCM), i = w % (STRIP * KCM);
         const int rloc = i % STRIP, q = i / STRIP;
         if (rloc >= nl) continue;
-        const int64_t m = l0 + rloc;
+        const int64_t lo = P.a_off + ad.line(l0 + rloc);
         const int Ei = smax[rloc];
         uint32_t pk[S][4];
         if constexpr (CPLX) {
@@ -401,8 +441,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
           for (int j = 0; j < 4; ++j) {
             const int k = (kb * TKS + q * 8) / 2 + j;
             a[j] = make_double2(0.0, 0.0);
-            if (k < P.K)
-              a[j] = ld_pol(reinterpret_cast<const double2 *>(A) + P.a_off + (ta ? (int64_t)k + m * P.lda : m + (int64_t)k * P.lda), last);
+            if (k < P.K) a[j] = ld_pol(reinterpret_cast<const double2 *>(A) + lo + ad.depth(k), last);
           }
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
@@ -418,7 +457,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
           for (int e = 0; e < 8; ++e) {
             const int kk = kb * TKS + q * 8 + e;
             v[e] = 0.0;
-            if (kk < P.Kr) v[e] = ld_pol(A + P.a_off + (ta ? (int64_t)kk + m * P.lda : m + (int64_t)kk * P.lda), last);
+            if (kk < P.Kr) v[e] = ld_pol(A + lo + ad.depth(kk), last);
           }
 #pragma unroll
           for (int e = 0; e < 8; e += 2) {
@@ -441,7 +480,7 @@ __device__ __forceinline__ void strip_a(const SplitPair *__restrict__ pairs, int
 
 // B role.  Task = (first pair, end pair, first real column c0 of the strip).
 template <bool CPLX, int S, int B>
-__device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int4 tk,
+__device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, const OperandView *views, int4 tk,
                                         const double *__restrict__ Aarena, const double *__restrict__ Barena,
                                         int *__restrict__ F, uint8_t *__restrict__ arena) {
   __shared__ int smax[STRIP];
@@ -450,7 +489,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
   const bool dup = CPLX && Q.dupb != 0;  // two real columns per column of op(B)
   const int l0 = dup ? c0 / 2 : c0;
   const int nl = min(dup ? STRIP / 2 : STRIP, Q.N - l0);
-  strip_maxima<CPLX, true>(pairs, p0, p1, l0, nl, Aarena, Barena, smax);
+  strip_maxima<CPLX, true>(pairs, views, p0, p1, l0, nl, Aarena, Barena, smax);
   if (threadIdx.x < nl) {
     const int e = smax[threadIdx.x];
     if (dup) {
@@ -467,7 +506,8 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
   for (int p = p0; p < p1; ++p) {
     const SplitPair &P = pairs[p];
     const double *__restrict__ Bm = P.swap ? Aarena : Barena;
-    const bool tb = P.trans & 2, cb = P.trans & 8;
+    const bool cb = P.trans & 8;
+    const OpAddr ad = addr_b(P, views, p);
     uint8_t *tiles = arena + P.bs_off + (int64_t)nt * P.KB * S * B_DIGIT_BYTES;
     // item = one real column x 8 real k
     const int items = STRIP * KCM * P.KB;
@@ -479,7 +519,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
       const int Fj = smax[dup ? cloc >> 1 : cloc];
       uint32_t pk[S][4];
       if constexpr (CPLX) {
-        const int64_t n = dup ? l0 + (cloc >> 1) : l0 + cloc;
+        const int64_t lo = P.b_off + ad.line(dup ? l0 + (cloc >> 1) : l0 + cloc);
         double2 x[4];
         // B~ (A-duplicated form): rows 2k, 2k+1 = (Re, Im) of element k; B'
         // (B-duplicated form): the same 4 complex k per 8 real rows
@@ -487,8 +527,7 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
         for (int j = 0; j < 4; ++j) {
           const int k = (kb * TKS + q * 8) / 2 + j;
           x[j] = make_double2(0.0, 0.0);
-          if (k < P.K)
-            x[j] = ld_pol(reinterpret_cast<const double2 *>(Bm) + P.b_off + (tb ? n + (int64_t)k * P.ldb : (int64_t)k + n * P.ldb), last);
+          if (k < P.K) x[j] = ld_pol(reinterpret_cast<const double2 *>(Bm) + lo + ad.depth(k), last);
         }
         const bool odd = dup && (cloc & 1);
 #pragma unroll
@@ -501,13 +540,13 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
             pk[t][j] = dup ? (odd ? pack2(di[t], dr[t]) : pack2(dr[t], -di[t])) : pack2(dr[t], di[t]);
         }
       } else {
-        const int64_t n = l0 + cloc;
+        const int64_t lo = P.b_off + ad.line(l0 + cloc);
         double v[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const int kk = kb * TKS + q * 8 + e;
           v[e] = 0.0;
-          if (kk < P.Kr) v[e] = ld_pol(Bm + P.b_off + (tb ? n + (int64_t)kk * P.ldb : (int64_t)kk + n * P.ldb), last);
+          if (kk < P.Kr) v[e] = ld_pol(Bm + lo + ad.depth(kk), last);
         }
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
@@ -528,27 +567,29 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, int
 
 template <bool CPLX, int S>
 __global__ void __launch_bounds__(STRIP_THREADS)
-strip_a_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks, const double *__restrict__ A,
-               const double *__restrict__ B, int *__restrict__ E, uint8_t *__restrict__ arena, int b) {
+strip_a_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restrict__ views,
+               const int4 *__restrict__ tasks, const double *__restrict__ A, const double *__restrict__ B,
+               int *__restrict__ E, uint8_t *__restrict__ arena, int b) {
   const int4 tk = tasks[blockIdx.x];
   switch (b) {  // the host admits b = 5..8 only
-    case 5: strip_a<CPLX, S, 5>(pairs, tk, A, B, E, arena); break;
-    case 6: strip_a<CPLX, S, 6>(pairs, tk, A, B, E, arena); break;
-    case 7: strip_a<CPLX, S, 7>(pairs, tk, A, B, E, arena); break;
-    default: strip_a<CPLX, S, 8>(pairs, tk, A, B, E, arena); break;
+    case 5: strip_a<CPLX, S, 5>(pairs, views, tk, A, B, E, arena); break;
+    case 6: strip_a<CPLX, S, 6>(pairs, views, tk, A, B, E, arena); break;
+    case 7: strip_a<CPLX, S, 7>(pairs, views, tk, A, B, E, arena); break;
+    default: strip_a<CPLX, S, 8>(pairs, views, tk, A, B, E, arena); break;
   }
 }
 
 template <bool CPLX, int S>
 __global__ void __launch_bounds__(STRIP_THREADS)
-strip_b_kernel(const SplitPair *__restrict__ pairs, const int4 *__restrict__ tasks, const double *__restrict__ A,
-               const double *__restrict__ B, int *__restrict__ F, uint8_t *__restrict__ arena, int b) {
+strip_b_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restrict__ views,
+               const int4 *__restrict__ tasks, const double *__restrict__ A, const double *__restrict__ B,
+               int *__restrict__ F, uint8_t *__restrict__ arena, int b) {
   const int4 tk = tasks[blockIdx.x];
   switch (b) {
-    case 5: strip_b<CPLX, S, 5>(pairs, tk, A, B, F, arena); break;
-    case 6: strip_b<CPLX, S, 6>(pairs, tk, A, B, F, arena); break;
-    case 7: strip_b<CPLX, S, 7>(pairs, tk, A, B, F, arena); break;
-    default: strip_b<CPLX, S, 8>(pairs, tk, A, B, F, arena); break;
+    case 5: strip_b<CPLX, S, 5>(pairs, views, tk, A, B, F, arena); break;
+    case 6: strip_b<CPLX, S, 6>(pairs, views, tk, A, B, F, arena); break;
+    case 7: strip_b<CPLX, S, 7>(pairs, views, tk, A, B, F, arena); break;
+    default: strip_b<CPLX, S, 8>(pairs, views, tk, A, B, F, arena); break;
   }
 }
 
@@ -1002,18 +1043,19 @@ int pick_stages() {
 }
 
 template <int S>
-void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const int4 *d_sa, int nsa, const int4 *d_sb,
-                    int nsb, const SplitTile *d_tiles, int ntiles, const double *A, const double *B, double *C,
-                    int *dE, int *dF, uint8_t *arena, int b, int kchunk, int *err) {
+void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const OperandView *d_va, const OperandView *d_vb,
+                    const int4 *d_sa, int nsa, const int4 *d_sb, int nsb, const SplitTile *d_tiles, int ntiles,
+                    const double *A, const double *B, double *C, int *dE, int *dF, uint8_t *arena, int b,
+                    int kchunk, int *err) {
   if (b < 5 || b > 8 || b * S > 62) fail(QS_ERR_INTERNAL, "split: unsupported digit plan b=%d S=%d", b, S);
   cudaStream_t st = ctx->stream;
   ctx->mark(0);
   if (cplx) {
-    if (nsa) { strip_a_kernel<true, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nsb) { strip_b_kernel<true, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nsa) { strip_a_kernel<true, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_va, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nsb) { strip_b_kernel<true, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
   } else {
-    if (nsa) { strip_a_kernel<false, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nsb) { strip_b_kernel<false, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
+    if (nsa) { strip_a_kernel<false, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_va, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
+    if (nsb) { strip_b_kernel<false, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
   }
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);
@@ -1141,6 +1183,8 @@ struct SplitWork {
   // A role (rows of op(A~)) and of the B role (columns of op(B~))
   std::vector<int4> sa, sb;
   std::vector<SplitTile> tiles;
+  // strided views of the A and B roles per pair (empty: none)
+  std::vector<OperandView> va, vb;
 };
 
 // Their device copies, the exponent arrays and the digit arena.
@@ -1148,6 +1192,7 @@ struct SplitDev {
   SplitPair *pairs = nullptr;
   int4 *sa = nullptr, *sb = nullptr;
   SplitTile *tiles = nullptr;
+  OperandView *va = nullptr, *vb = nullptr;
   int *E = nullptr, *F = nullptr;
   uint8_t *arena = nullptr;
 };
@@ -1215,7 +1260,9 @@ static std::vector<uint8_t> orient_blocks(const std::vector<PairDesc> &pairs, co
 static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::vector<int64_t> &grp,
                               const std::vector<int32_t> &blk_M_in, const std::vector<int32_t> &blk_N_in,
                               const std::vector<int64_t> &c_off, bool cplx, int forced_slices, double tol,
-                              const std::vector<int32_t> *blk_ldc, SplitWork &w, int forced_bits = 0) {
+                              const std::vector<int32_t> *blk_ldc, SplitWork &w, int forced_bits = 0,
+                              const std::vector<OperandView> *va = nullptr,
+                              const std::vector<OperandView> *vb = nullptr) {
   SplitResult res;
   const int64_t nb = (int64_t)blk_M_in.size();
   const int cm = cplx ? 2 : 1;
@@ -1223,6 +1270,25 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
   std::vector<PairDesc> swapped_pairs;
   const std::vector<uint8_t> mode = orient_blocks(pairs_in, grp, blk_M, blk_N, cm, swapped_pairs);
   const std::vector<PairDesc> &pairs = swapped_pairs.empty() ? pairs_in : swapped_pairs;
+  // strided operand views follow their operands into the roles: a block
+  // computed as C^T reads op(B)^T in the A role and op(A)^T in the B role,
+  // whose lines are B's columns resp. A's rows -- the same views, exchanged
+  if ((va && !va->empty()) || (vb && !vb->empty())) {
+    const OperandView none{};
+    w.va.assign(pairs.size(), none);
+    w.vb.assign(pairs.size(), none);
+    for (int64_t g = 0; g < nb; ++g)
+      for (int64_t p = grp[g]; p < grp[g + 1]; ++p) {
+        const OperandView x = (va && !va->empty()) ? (*va)[p] : none, y = (vb && !vb->empty()) ? (*vb)[p] : none;
+        if (mode[g] & 1) {
+          w.va[p] = y;
+          w.vb[p] = x;
+        } else {
+          w.va[p] = x;
+          w.vb[p] = y;
+        }
+      }
+  }
   DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cm, tol, forced_slices, forced_bits);
   const int S = dp.nslices, b = dp.bits;
   const int kchunk = kchunk_of(b, S);
@@ -1378,8 +1444,8 @@ static void launch_split(Ctx *ctx, const SplitWork &w, bool cplx, const SplitDev
   switch (w.S) {
 #define QS_CASE(SS)                                                                                      \
   case SS:                                                                                               \
-    launch_split_s<SS>(ctx, cplx, d.pairs, d.sa, (int)w.sa.size(), d.sb, (int)w.sb.size(), d.tiles,     \
-                       (int)w.tiles.size(), A, B, C, d.E, d.F, d.arena, w.b, w.kchunk, err);             \
+    launch_split_s<SS>(ctx, cplx, d.pairs, d.va, d.vb, d.sa, (int)w.sa.size(), d.sb, (int)w.sb.size(),    \
+                       d.tiles, (int)w.tiles.size(), A, B, C, d.E, d.F, d.arena, w.b, w.kchunk, err);    \
     break;
     QS_CASE(2)
     QS_CASE(3)
@@ -1398,9 +1464,11 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
                       const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                       const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                       bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
-                      int forced_bits, const FactorSource *fs) {
+                      int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
+                      const std::vector<OperandView> *vb) {
   SplitWork w;
-  SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w, forced_bits);
+  SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w, forced_bits,
+                               va, vb);
   if (w.tiles.empty()) return res;
   // device buffers: one allocation for the digit arena (pooled scratch)
   SplitDev d;
@@ -1409,6 +1477,10 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   d.sa = dev_upload(ctx, w.sa);
   d.sb = dev_upload(ctx, w.sb);
   d.tiles = dev_upload(ctx, w.tiles);
+  if (!w.va.empty()) {
+    d.va = dev_upload(ctx, w.va);
+    d.vb = dev_upload(ctx, w.vb);
+  }
   d.E = dev_alloc<int>(ctx, (size_t)w.nE);
   d.F = dev_alloc<int>(ctx, (size_t)w.nF);
   if (fs && !w.sp.empty()) {
@@ -1421,6 +1493,8 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   dev_free(ctx, d.pairs);
   dev_free(ctx, d.sa);
   dev_free(ctx, d.sb);
+  if (d.va) dev_free(ctx, d.va);
+  if (d.vb) dev_free(ctx, d.vb);
   dev_free(ctx, d.tiles);
   dev_free(ctx, d.E);
   dev_free(ctx, d.F);

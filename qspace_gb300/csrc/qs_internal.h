@@ -126,6 +126,19 @@ struct PermDesc {
   int32_t pad_;
 };
 
+// A strided view of one operand block in place of the permuted copy that
+// permute_to makes (Source/QSpace.hh:2824-2866) when the contracted legs of
+// an operand are not contiguous: element (line, k) of the operand as the
+// GEMM reads it -- line = row of op(A) / column of op(B), k = depth -- sits at
+// block offset  sum_i l_i lstr[i] + sum_t k_t kstr[t],  line = sum_i l_i
+// prod_{i'<i} ldim[i'] (first leg fastest), likewise k.  nl = 0: no view.
+constexpr int VIEW_LEGS = 4;
+struct OperandView {
+  int32_t nl, nk;
+  int32_t ldim[VIEW_LEGS], kdim[VIEW_LEGS];
+  int64_t lstr[VIEW_LEGS], kstr[VIEW_LEGS];
+};
+
 // One 32 x 32 tile of a tiled block: tile (ti, tj) of (output leg 0,
 // output leg fast_in_leg) at linear index `rest` of the other legs.
 struct PermTile {
