@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--nrg-runs", type=int, default=32)
     ap.add_argument("--nrg-iters", type=int, default=40)
     ap.add_argument("--nrg-rate", type=float, default=20.0)
+    ap.add_argument("--permute-only", action="store_true",
+                    help="only the permuteQS row (the 257 MB two-site wave function), for profiling")
     return ap.parse_args()
 
 
@@ -315,6 +317,43 @@ def serve_nrg_bench(ctx, prec: str, runs: int = 32, iters: int = 40, rate: float
             "errors": errs[:3]}
 
 
+def permute_bench(ctx, reps: int = 5) -> dict:
+    """permuteQS kernels on a device-resident two-site wave function
+    psi(L, s1, s2, R), U(1)xU(1), bond dimension 8192, complex128 (257 MB,
+    larger than L2): bytes = read + write of every element once; kernel time
+    from the library's CUDA events around the permute launches."""
+    from qspace_gb300 import permute_dev, upload
+    from qspace_gb300.workloads import rank4_psi
+    psi_h = rank4_psi(seed=0, D=8192, complex_data=True)
+    nbytes = 16.0 * sum(x.size for x in psi_h.data)
+    tpsi = upload(psi_h, ctx)
+    del psi_h
+    out = {"workload": "two-site wave function psi(L,s1,s2,R), U(1)xU(1), D=8192, complex128, "
+                       f"{nbytes / 1e6:.0f} MB", "bytes_per_call": 2 * nbytes, "rows": []}
+    _, hbm_pk, hbm_kind = measured_peaks()
+    for perm_, what in (([4, 2, 3, 1], "R,s1,s2,L: blocks transposed (shared-memory tiles)"),
+                        ([1, 4, 2, 3], "L,R,s1,s2: contiguous blocks (output-order lines)")):
+        permute_dev(tpsi, perm_).free()
+        ctx.sync()
+        ctx.set_timing(True)
+        kms, cms = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            tp = permute_dev(tpsi, perm_)
+            kms.append(ctx.phase_ms()[0])
+            ctx.sync()
+            cms.append(1e3 * (time.perf_counter() - t0))
+            tp.free()
+        ctx.set_timing(False)
+        km = statistics.median(kms)
+        gbs = 2 * nbytes / (km * 1e-3) / 1e9
+        out["rows"].append({"perm": perm_, "layout": what, "kernel_ms": km, "GB/s": gbs,
+                            "frac_of_hbm": gbs / hbm_pk, "peak_kind": hbm_kind,
+                            "call_ms": statistics.median(cms)})
+    tpsi.free()
+    return out
+
+
 def run_reference(a, ws, rank):
     """The reference's algorithm on the host cores: one BLAS GEMM per block
     pair, a thread per core (oracle/cpu_baseline.py)."""
@@ -354,6 +393,9 @@ def main():
     from qspace_gb300.workloads import grouped_pairs
 
     torch.cuda.set_device(local)
+    if a.permute_only:
+        print(json.dumps({"permute": permute_bench(default_context(local))}))
+        return 0
     if a.serve_nrg:
         ctx = default_context(local)
         rows = []
@@ -517,6 +559,25 @@ def main():
             pplan.close()
         pms = e0.elapsed_time(e1) / a.plain_steps
         plain = {"value": flops / (pms * 1e-3) / 1e12, "ms_per_step": pms}
+        # FP64 roofline denominator, measured here: cuBLAS DGEMM (torch.matmul
+        # in float64, n = 8192, best of 3 after a warm-up); the plain path's
+        # fraction of it
+        x = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+        y = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+        torch.matmul(x, y)
+        best = None
+        for _ in range(3):
+            e0.record()
+            torch.matmul(x, y)
+            e1.record()
+            torch.cuda.synchronize()
+            t_ = e0.elapsed_time(e1)
+            best = t_ if best is None else min(best, t_)
+        fp64_peak = 2.0 * 8192 ** 3 / (best * 1e-3) / 1e12
+        del x, y
+        plain["fp64_peak_tflops"] = fp64_peak
+        plain["fp64_peak_kind"] = "measured here: cuBLAS DGEMM 8192^3, best of 3"
+        plain["frac_of_fp64_peak"] = plain["value"] / fp64_peak
 
     # ---- fewer digits: 3 and 4 slices (below the 1e-12 target), error stated
     slices = []
@@ -557,39 +618,7 @@ def main():
             rdm[pr + "_ms_p50"] = 1e3 * statistics.median(ts)
 
     # ---- permuteQS kernels on a device-resident two-site wave function
-    # psi(L, s1, s2, R), U(1)xU(1), bond dimension 8192, complex128 (257 MB,
-    # larger than L2): bytes = read + write of every element once
-    permute = None
-    if not a.no_extras:
-        from qspace_gb300 import permute_dev, upload
-        from qspace_gb300.workloads import rank4_psi
-        psi_h = rank4_psi(seed=0, D=8192, complex_data=True)
-        nbytes = 16.0 * sum(x.size for x in psi_h.data)
-        tpsi = upload(psi_h, ctx)
-        del psi_h
-        permute = {"workload": "two-site wave function psi(L,s1,s2,R), U(1)xU(1), D=8192, complex128, "
-                               f"{nbytes / 1e6:.0f} MB", "bytes_per_call": 2 * nbytes, "rows": []}
-        _, hbm_pk, hbm_kind = measured_peaks()
-        for perm_, what in (([4, 2, 3, 1], "R,s1,s2,L: blocks transposed (shared-memory tiles)"),
-                            ([1, 4, 2, 3], "L,R,s1,s2: contiguous blocks (output-order lines)")):
-            permute_dev(tpsi, perm_).free()
-            ctx.sync()
-            ctx.set_timing(True)
-            kms, cms = [], []
-            for _ in range(5):
-                t0 = time.perf_counter()
-                tp = permute_dev(tpsi, perm_)
-                kms.append(ctx.phase_ms()[0])
-                ctx.sync()
-                cms.append(1e3 * (time.perf_counter() - t0))
-                tp.free()
-            ctx.set_timing(False)
-            km = statistics.median(kms)
-            gbs = 2 * nbytes / (km * 1e-3) / 1e9
-            permute["rows"].append({"perm": perm_, "layout": what, "kernel_ms": km, "GB/s": gbs,
-                                    "frac_of_hbm": gbs / hbm_pk, "peak_kind": hbm_kind,
-                                    "call_ms": statistics.median(cms)})
-        tpsi.free()
+    permute = None if a.no_extras else permute_bench(ctx)
 
     # ---- FP64 block eigendecompositions of one NRG step (abelian U(1)xU(1)
     # stand-in for the SU(2)xU(1) Wilson chain): every symmetry block of a

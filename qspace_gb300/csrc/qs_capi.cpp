@@ -361,9 +361,12 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
     for (size_t p = 0; p < pl.pairs.size(); ++p)
       if (!make_view(m, is_a ? pl.pair_ia[p] : pl.pair_ib[p], lines, ks, v[p])) return false;
     out.swap(v);
-    // the permuted copy would have been conjugated: conjugate on the fly
+    // the permuted copy would have been conjugated: conjugate on the fly.
+    // XOR, not OR: the conjugation flag may be set as well (the auto-conj
+    // rule of contract_getIdxSet, after permute_to flipped the copy's itags),
+    // and the two conjugations then cancel, as they do for the copy
     if (lay.conj)
-      for (PairDesc &d : pl.pairs) d.trans |= is_a ? 4 : 8;
+      for (PairDesc &d : pl.pairs) d.trans ^= is_a ? 4 : 8;
     return true;
   };
   const bool fa = fused(Am, true, w.va), fb = fused(Bm, false, w.vb);
