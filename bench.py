@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--nrg-runs", type=int, default=32)
     ap.add_argument("--nrg-iters", type=int, default=40)
     ap.add_argument("--nrg-rate", type=float, default=20.0)
+    ap.add_argument("--nrg-slots", type=int, default=8)
+    ap.add_argument("--nrg-precs", default="split,fp64")
     ap.add_argument("--permute-only", action="store_true",
                     help="only the permuteQS row (the 257 MB two-site wave function), for profiling")
     return ap.parse_args()
@@ -399,8 +401,8 @@ def main():
     if a.serve_nrg:
         ctx = default_context(local)
         rows = []
-        for pr in ("split", "fp64"):
-            rows.append(serve_nrg_bench(ctx, pr, a.nrg_runs, a.nrg_iters, a.nrg_rate))
+        for pr in a.nrg_precs.split(","):
+            rows.append(serve_nrg_bench(ctx, pr, a.nrg_runs, a.nrg_iters, a.nrg_rate, a.nrg_slots))
             print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
             if rows[-1]["errors"]:
                 break
