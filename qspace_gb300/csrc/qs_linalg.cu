@@ -306,6 +306,30 @@ __global__ void merge_runs_kernel(const double *__restrict__ v, const int64_t *_
   }
 }
 
+// flag = 1 when any of p[0..n) is not finite (NaN or infinite)
+__global__ void nonfinite_kernel(const double *__restrict__ p, int64_t n, int *flag) {
+  int bad = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(p[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+// Host check that a device array holds finite values only (one pass, one
+// synchronisation).
+bool all_finite(Ctx *ctx, const double *p, int64_t n) {
+  if (n <= 0) return true;
+  int *d = dev_alloc<int>(ctx, 1);
+  int h = 0;
+  QS_CUDA(cudaMemsetAsync(d, 0, sizeof(int), ctx->stream));
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)std::max(ctx->num_sms, 1) * 8);
+  nonfinite_kernel<<<grid, 256, 0, ctx->stream>>>(p, n, d);
+  QS_LAUNCHED(ctx);
+  QS_CUDA(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, d);
+  return h == 0;
+}
+
 __global__ void iota_kernel(int64_t *p, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = i;
@@ -373,6 +397,9 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
   if (N == 0) return;
   cudaStream_t st = ctx->stream;
   const int grid = (int)std::min<int64_t>((N + 255) / 256, (int64_t)std::max(ctx->num_sms, 1) * 8);
+  // the stable order needs comparable values: a NaN level is an error, as a
+  // failed LAPACK call is for the reference
+  if (!all_finite(ctx, dE, N)) fail(QS_ERR_NUMERIC, "markSet: non-finite eigenvalues");
   int64_t Nkeep = (nkeep_in < 0 || nkeep_in > N) ? N : nkeep_in;
   int64_t l = 0;
   std::vector<void *> tmp;
@@ -1014,12 +1041,17 @@ void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double
   int64_t nk = 0;
   double et = 0;
   try {
+    if (!all_finite(c, H->d, m.nelem * es)) fail(QS_ERR_NUMERIC, "eigQS: H holds non-finite entries");
     eig_blocks(c, nb, n.data(), m.offs.data(), eoffs.data(), H->d, dE, U, m.cplx);
     // markSet on the device: the eigenvalues stay there; the host gets the
     // kept count of every block (a prefix: its lowest levels)
     std::vector<int64_t> k;
     d_keep = dev_alloc<uint8_t>(c, (size_t)std::max<int64_t>(ntot, 1));
     mark_keep_dev(c, nb, n.data(), eoffs.data(), dE, nkeep, etrunc, deps, d_keep, k, &nk, &et);
+    for (int64_t i = 0; i < nb; ++i)
+      if (k[i] < 0 || k[i] > n[i])
+        fail(QS_ERR_INTERNAL, "eigQS: block %lld keeps %lld of %lld states", (long long)i, (long long)k[i],
+             (long long)n[i]);
     if (E && ntot) QS_CUDA(cudaMemcpyAsync(hE.data(), dE, ntot * 8, cudaMemcpyDeviceToHost, c->stream));
     if (keep && ntot) QS_CUDA(cudaMemcpyAsync(hk.data(), d_keep, ntot, cudaMemcpyDeviceToHost, c->stream));
     auto part = [&](bool kept) {
