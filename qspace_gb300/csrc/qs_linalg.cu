@@ -330,6 +330,29 @@ bool all_finite(Ctx *ctx, const double *p, int64_t n) {
   return h == 0;
 }
 
+// flag = 1 + the first element index found out of ascending order inside a
+// run of bnd (first run boundary 0, last N)
+__global__ void runs_ascending_kernel(const double *__restrict__ v, const int64_t *__restrict__ bnd, int nruns,
+                                      unsigned long long *flag) {
+  for (int r = blockIdx.x; r < nruns; r += gridDim.x)
+    for (int64_t i = bnd[r] + 1 + threadIdx.x; i < bnd[r + 1]; i += blockDim.x)
+      if (v[i] < v[i - 1]) atomicMin(flag, (unsigned long long)i);
+}
+
+// cnt[P[i]] += 1 for every i; afterwards any cnt != 1 marks a broken order
+__global__ void count_targets_kernel(const int64_t *__restrict__ P, int64_t N, int *__restrict__ cnt,
+                                     unsigned long long *bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = P[i];
+    if (t < 0 || t >= N) atomicMin(bad, (unsigned long long)i);
+    else atomicAdd(&cnt[t], 1);
+  }
+}
+__global__ void check_counts_kernel(const int *__restrict__ cnt, int64_t N, unsigned long long *bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    if (cnt[i] != 1) atomicMin(bad, (unsigned long long)i);
+}
+
 __global__ void iota_kernel(int64_t *p, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = i;
@@ -424,6 +447,19 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
         if (n[b] > 0) bnd.push_back(eoffs[b]);
       bnd.push_back(N);
       int64_t *d_bnd = static_cast<int64_t *>(alloc(bnd.size() * 8));
+      unsigned long long *d_bad = static_cast<unsigned long long *>(alloc(8));
+      const unsigned long long none = ~0ull;
+      unsigned long long bad = none;
+      // the merge needs every block's levels in ascending order (the solvers
+      // return them so); a block that is not is an error, not a wrong cut
+      QS_CUDA(cudaMemcpyAsync(d_bnd, bnd.data(), bnd.size() * 8, cudaMemcpyHostToDevice, st));
+      QS_CUDA(cudaMemcpyAsync(d_bad, &none, 8, cudaMemcpyHostToDevice, st));
+      runs_ascending_kernel<<<(int)std::min<size_t>(bnd.size() - 1, 4096), 128, 0, st>>>(v0, d_bnd,
+                                                                                         (int)(bnd.size() - 1), d_bad);
+      QS_LAUNCHED(ctx);
+      QS_CUDA(cudaMemcpyAsync(&bad, d_bad, 8, cudaMemcpyDeviceToHost, st));
+      QS_CUDA(cudaStreamSynchronize(st));
+      if (bad != none) fail(QS_ERR_NUMERIC, "markSet: eigenvalue %llu is below its predecessor in its block", bad);
       while (bnd.size() > 2) {
         if (bnd.size() - 1 > 0x7fffffff) fail(QS_ERR_SHAPE, "markSet: too many blocks");
         QS_CUDA(cudaMemcpyAsync(d_bnd, bnd.data(), bnd.size() * 8, cudaMemcpyHostToDevice, st));
@@ -435,6 +471,19 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
         for (size_t r = 0; r + 1 < bnd.size(); r += 2) nb.push_back(bnd[r]);
         nb.push_back(N);
         bnd.swap(nb);  // the next round's boundary upload is stream-ordered after this merge
+      }
+      // the merged order must be a permutation of 0..N-1
+      {
+        int *d_cnt = static_cast<int *>(alloc(N * 4));
+        QS_CUDA(cudaMemsetAsync(d_cnt, 0, (size_t)N * 4, st));
+        QS_CUDA(cudaMemcpyAsync(d_bad, &none, 8, cudaMemcpyHostToDevice, st));
+        count_targets_kernel<<<grid, 256, 0, st>>>(i0, N, d_cnt, d_bad);
+        QS_LAUNCHED(ctx);
+        check_counts_kernel<<<grid, 256, 0, st>>>(d_cnt, N, d_bad);
+        QS_LAUNCHED(ctx);
+        QS_CUDA(cudaMemcpyAsync(&bad, d_bad, 8, cudaMemcpyDeviceToHost, st));
+        QS_CUDA(cudaStreamSynchronize(st));
+        if (bad != none) fail(QS_ERR_INTERNAL, "markSet: merged order is not a permutation (at %llu)", bad);
       }
       // v0 = sorted levels, i0 = their global indices; averaged levels in v1
       unsigned long long *d_l = static_cast<unsigned long long *>(alloc(8));
