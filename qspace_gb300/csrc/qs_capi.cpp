@@ -685,7 +685,13 @@ static std::unique_ptr<qs_tensor> upload(Ctx *ctx, const qs_qspace_view *v) {
   T->meta = m;
   const size_t n = (size_t)m.nelem * (m.cplx ? 2 : 1);
   T->d = dev_alloc<double>(ctx, n);
-  if (n) QS_CUDA(cudaMemcpyAsync(T->d, v->data, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  if (n) {
+    QS_CUDA(cudaMemcpyAsync(T->d, v->data, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    // the caller may release its host buffer when the call returns, and a copy
+    // from pageable memory may still read it later (the GPU can read host
+    // memory directly): wait until the copy has read it
+    QS_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
   return T;
 }
 

@@ -1539,6 +1539,10 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
   put(d.sb, w.sb.data(), w.sb.size() * sizeof(int4));
   put(d.tiles, w.tiles.data(), w.tiles.size() * sizeof(SplitTile));
   launch_split(ctx, w, cplx, d, A, B, C, err);
+  // the work lists are copied from pageable host memory, which the GPU may
+  // read when the copies execute rather than when they are queued: keep them
+  // alive until then
+  QS_CUDA(cudaStreamSynchronize(ctx->stream));
   return res;
 }
 

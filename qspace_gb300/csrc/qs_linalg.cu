@@ -446,14 +446,22 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
       for (int64_t b = 0; b < nblk; ++b)
         if (n[b] > 0) bnd.push_back(eoffs[b]);
       bnd.push_back(N);
-      int64_t *d_bnd = static_cast<int64_t *>(alloc(bnd.size() * 8));
+      // Host arrays reach the device through the context's page-locked
+      // staging ring (dev_upload), never by a copy from pageable memory: such
+      // a copy may read its source after the call returns, when the source
+      // of an earlier round is already gone.
+      auto upload = [&](const std::vector<int64_t> &h) {
+        int64_t *d = dev_upload(ctx, h);
+        tmp.push_back(d);
+        return d;
+      };
+      int64_t *d_bnd = upload(bnd);
       unsigned long long *d_bad = static_cast<unsigned long long *>(alloc(8));
       const unsigned long long none = ~0ull;
       unsigned long long bad = none;
       // the merge needs every block's levels in ascending order (the solvers
       // return them so); a block that is not is an error, not a wrong cut
-      QS_CUDA(cudaMemcpyAsync(d_bnd, bnd.data(), bnd.size() * 8, cudaMemcpyHostToDevice, st));
-      QS_CUDA(cudaMemcpyAsync(d_bad, &none, 8, cudaMemcpyHostToDevice, st));
+      QS_CUDA(cudaMemsetAsync(d_bad, 0xFF, 8, st));
       runs_ascending_kernel<<<(int)std::min<size_t>(bnd.size() - 1, 4096), 128, 0, st>>>(v0, d_bnd,
                                                                                          (int)(bnd.size() - 1), d_bad);
       QS_LAUNCHED(ctx);
@@ -462,7 +470,7 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
       if (bad != none) fail(QS_ERR_NUMERIC, "markSet: eigenvalue %llu is below its predecessor in its block", bad);
       while (bnd.size() > 2) {
         if (bnd.size() - 1 > 0x7fffffff) fail(QS_ERR_SHAPE, "markSet: too many blocks");
-        QS_CUDA(cudaMemcpyAsync(d_bnd, bnd.data(), bnd.size() * 8, cudaMemcpyHostToDevice, st));
+        d_bnd = upload(bnd);
         merge_runs_kernel<<<grid, 256, 0, st>>>(v0, i0, v1, i1, d_bnd, (int)(bnd.size() - 1), N);
         QS_LAUNCHED(ctx);
         std::swap(v0, v1);
@@ -470,13 +478,13 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
         std::vector<int64_t> nb;
         for (size_t r = 0; r + 1 < bnd.size(); r += 2) nb.push_back(bnd[r]);
         nb.push_back(N);
-        bnd.swap(nb);  // the next round's boundary upload is stream-ordered after this merge
+        bnd.swap(nb);
       }
       // the merged order must be a permutation of 0..N-1
       {
         int *d_cnt = static_cast<int *>(alloc(N * 4));
         QS_CUDA(cudaMemsetAsync(d_cnt, 0, (size_t)N * 4, st));
-        QS_CUDA(cudaMemcpyAsync(d_bad, &none, 8, cudaMemcpyHostToDevice, st));
+        QS_CUDA(cudaMemsetAsync(d_bad, 0xFF, 8, st));
         count_targets_kernel<<<grid, 256, 0, st>>>(i0, N, d_cnt, d_bad);
         QS_LAUNCHED(ctx);
         check_counts_kernel<<<grid, 256, 0, st>>>(d_cnt, N, d_bad);
@@ -486,9 +494,8 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
         if (bad != none) fail(QS_ERR_INTERNAL, "markSet: merged order is not a permutation (at %llu)", bad);
       }
       // v0 = sorted levels, i0 = their global indices; averaged levels in v1
-      unsigned long long *d_l = static_cast<unsigned long long *>(alloc(8));
       const unsigned long long lN = (unsigned long long)N;
-      QS_CUDA(cudaMemcpyAsync(d_l, &lN, 8, cudaMemcpyHostToDevice, st));
+      unsigned long long *d_l = reinterpret_cast<unsigned long long *>(upload({(int64_t)N}));
       average_clusters_kernel<<<grid, 256, 0, st>>>(v0, v1, N, deps);
       QS_LAUNCHED(ctx);
       if (etrunc > 0) {
@@ -539,10 +546,11 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
         *etrunc_out = (l < N) ? sl - ends[0] : 0.0;
       }
     }
-    int64_t *d_n = static_cast<int64_t *>(alloc(nblk * 8)), *d_eo = static_cast<int64_t *>(alloc(nblk * 8));
+    int64_t *d_n = dev_upload(ctx, std::vector<int64_t>(n, n + nblk));
+    tmp.push_back(d_n);
+    int64_t *d_eo = dev_upload(ctx, std::vector<int64_t>(eoffs, eoffs + nblk));
+    tmp.push_back(d_eo);
     int64_t *d_k = static_cast<int64_t *>(alloc(nblk * 8));
-    QS_CUDA(cudaMemcpyAsync(d_n, n, nblk * 8, cudaMemcpyHostToDevice, st));
-    QS_CUDA(cudaMemcpyAsync(d_eo, eoffs, nblk * 8, cudaMemcpyHostToDevice, st));
     count_kept_kernel<<<(int)std::min<int64_t>((nblk + 127) / 128, 1024), 128, 0, st>>>(d_keep, d_eo, d_n, nblk, d_k);
     QS_LAUNCHED(ctx);
     QS_CUDA(cudaMemcpyAsync(kcount.data(), d_k, nblk * 8, cudaMemcpyDeviceToHost, st));
