@@ -61,6 +61,13 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the slice-count, RDM-latency and serving rows")
     ap.add_argument("--serve-rates", default="500,5000", help="offered requests/s of the serving rows")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-nrg", action="store_true",
+                    help="only the NRG z-shift serving workload (32 runs, kept 256->4096 over 40 iterations)")
+    ap.add_argument("--nrg-runs", type=int, default=32)
+    ap.add_argument("--nrg-iters", type=int, default=40)
+    ap.add_argument("--nrg-rate", type=float, default=20.0)
+    ap.add_argument("--nrg-slots", type=int, default=8)
+    ap.add_argument("--nrg-precs", default="split,fp64")
     ap.add_argument("--permute-only", action="store_true",
                     help="only the permuteQS row (the 257 MB two-site wave function), for profiling")
     return ap.parse_args()
@@ -259,6 +266,59 @@ def serve_bench(ctx, prec: str, rate: float, seconds: float, seed: int = 0) -> d
             "tflops": done_flops / wall / 1e12}
 
 
+def serve_nrg_bench(ctx, prec: str, runs: int = 32, iters: int = 40, rate: float = 20.0, nslots: int = 8,
+                    seed: int = 0) -> dict:
+    """Serving loop under the NRG z-shift workload: `runs` Wilson-chain NRG
+    runs at z = k/runs (k = 0..runs-1) of the spinful U(1)xU(1) chain
+    (Lambda 2.5), kept states growing geometrically 256 -> 4096 over `iters`
+    iterations.  Each run is a host thread that sends every iteration's
+    contractions and its block eigendecomposition (eigQS with truncation) as
+    requests to one serving loop; each run starts its next iteration after
+    an exponential pause of mean 1/rate (Poisson arrivals of iterations at
+    `rate` per run per second).  Returns requests/s and p50/p99 latency per
+    request kind, and the wall time."""
+    import threading
+
+    import numpy as np
+    from qspace_gb300.nrg import ServingBackend, initial_space, kept_schedule, step as nrg_step, wilson_hopping
+    from qspace_gb300.qspace import Context
+    from qspace_gb300.serve import Server
+    Lam = 2.5
+    nk = kept_schedule(iters)
+    errs = []
+
+    def run(be, z, rng):
+        n = -1
+        try:
+            K = initial_space(be, -0.2, 0.6)
+            for n in range(iters):
+                time.sleep(rng.exponential(1.0 / rate))
+                K = nrg_step(K, be, wilson_hopping(n, Lam, z), Lam, nkeep=nk[n], deps=1e-8)
+        except Exception as e:  # reported in the row
+            import traceback
+            errs.append(f"z={z:.3f} iteration {n}: " + "".join(traceback.format_exception(e))[-1500:])
+            print(errs[-1], file=sys.stderr, flush=True)
+
+    with Server(nslots=nslots, hbm_budget=96 << 30, ctx=ctx) as srv:
+        bes = [ServingBackend(srv, Context(ctx.device), prec) for _ in range(runs)]
+        th = [threading.Thread(target=run, args=(be, k / runs, np.random.default_rng(seed + k)))
+              for k, be in enumerate(bes)]
+        t0 = time.perf_counter()
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        wall = time.perf_counter() - t0
+    lc = [x for be in bes for x in be.latency["contract"]]
+    le = [x for be in bes for x in be.latency["eig"]]
+    return {"prec": prec, "runs": runs, "iterations": iters, "kept": f"{nk[0]}->{nk[-1]}",
+            "iteration_rate_per_run": rate, "slots": nslots, "wall_s": wall,
+            "requests": len(lc) + len(le), "requests_per_s": (len(lc) + len(le)) / wall,
+            "contract_p50_ms": percentile(lc, 0.5), "contract_p99_ms": percentile(lc, 0.99),
+            "eig_p50_ms": percentile(le, 0.5), "eig_p99_ms": percentile(le, 0.99),
+            "errors": errs[:3]}
+
+
 def permute_bench(ctx, reps: int = 5) -> dict:
     """permuteQS kernels on a device-resident two-site wave function
     psi(L, s1, s2, R), U(1)xU(1), bond dimension 8192, complex128 (257 MB,
@@ -337,6 +397,16 @@ def main():
     torch.cuda.set_device(local)
     if a.permute_only:
         print(json.dumps({"permute": permute_bench(default_context(local))}))
+        return 0
+    if a.serve_nrg:
+        ctx = default_context(local)
+        rows = []
+        for pr in a.nrg_precs.split(","):
+            rows.append(serve_nrg_bench(ctx, pr, a.nrg_runs, a.nrg_iters, a.nrg_rate, a.nrg_slots))
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+            if rows[-1]["errors"]:
+                break
+        print(json.dumps({"serving_nrg": rows}))
         return 0
     pg = None
     if ws > 1:

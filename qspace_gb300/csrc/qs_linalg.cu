@@ -21,6 +21,7 @@
 #include <thread>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -339,6 +340,55 @@ __global__ void runs_ascending_kernel(const double *__restrict__ v, const int64_
       if (v[i] < v[i - 1]) atomicMin(flag, (unsigned long long)i);
 }
 
+// Stable insertion sort of every run of (v, idx) by v.  Runs that a solver
+// returned ascending up to rounding (degenerate levels a unit in the last
+// place apart, in either order) take a few steps; the merged order is then
+// the stable ascending order of all levels, whatever the input.
+__global__ void sort_runs_kernel(double *__restrict__ v, int64_t *__restrict__ idx, const int64_t *__restrict__ bnd,
+                                 int nruns) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nruns; r += gridDim.x * blockDim.x) {
+    const int64_t a = bnd[r], b = bnd[r + 1];
+    for (int64_t i = a + 1; i < b; ++i) {
+      const double x = v[i];
+      if (!(x < v[i - 1])) continue;
+      const int64_t xi = idx[i];
+      int64_t j = i;
+      while (j > a && v[j - 1] > x) {
+        v[j] = v[j - 1];
+        idx[j] = idx[j - 1];
+        --j;
+      }
+      v[j] = x;
+      idx[j] = xi;
+    }
+  }
+}
+
+// The eigenvalues of every block made non-decreasing: a level below its
+// predecessor by at most rel * max|E| of the block (rounding of degenerate
+// levels) takes the predecessor's value, so that each block's lowest levels
+// are its first eigenvectors.  A larger inversion is not rounding: 1 + its
+// index goes to *bad and the level is left as it is.
+__global__ void monotone_blocks_kernel(double *__restrict__ E, const int64_t *__restrict__ bnd, int nruns, double rel,
+                                       unsigned long long *bad) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nruns; r += gridDim.x * blockDim.x) {
+    const int64_t a = bnd[r], b = bnd[r + 1];
+    if (b - a < 2) continue;
+    const double tol = rel * fmax(fabs(E[a]), fabs(E[b - 1]));
+    double m = E[a];
+    for (int64_t i = a + 1; i < b; ++i) {
+      const double x = E[i];
+      if (x >= m) {
+        m = x;
+      } else if (m - x <= tol) {
+        E[i] = m;
+      } else {
+        atomicMin(bad, (unsigned long long)i);
+      }
+    }
+  }
+}
+
 // cnt[P[i]] += 1 for every i; afterwards any cnt != 1 marks a broken order
 __global__ void count_targets_kernel(const int64_t *__restrict__ P, int64_t N, int *__restrict__ cnt,
                                      unsigned long long *bad) {
@@ -459,15 +509,19 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
       unsigned long long *d_bad = static_cast<unsigned long long *>(alloc(8));
       const unsigned long long none = ~0ull;
       unsigned long long bad = none;
-      // the merge needs every block's levels in ascending order (the solvers
-      // return them so); a block that is not is an error, not a wrong cut
+      // the merge needs every block's levels in ascending order: blocks that
+      // are not (the caller's levels in any order, or a solver's degenerate
+      // levels a rounding apart) are sorted first
       QS_CUDA(cudaMemsetAsync(d_bad, 0xFF, 8, st));
-      runs_ascending_kernel<<<(int)std::min<size_t>(bnd.size() - 1, 4096), 128, 0, st>>>(v0, d_bnd,
-                                                                                         (int)(bnd.size() - 1), d_bad);
+      const int nruns = (int)(bnd.size() - 1);
+      runs_ascending_kernel<<<(int)std::min(nruns, 4096), 128, 0, st>>>(v0, d_bnd, nruns, d_bad);
       QS_LAUNCHED(ctx);
       QS_CUDA(cudaMemcpyAsync(&bad, d_bad, 8, cudaMemcpyDeviceToHost, st));
       QS_CUDA(cudaStreamSynchronize(st));
-      if (bad != none) fail(QS_ERR_NUMERIC, "markSet: eigenvalue %llu is below its predecessor in its block", bad);
+      if (bad != none) {
+        sort_runs_kernel<<<(nruns + 127) / 128, 128, 0, st>>>(v0, i0, d_bnd, nruns);
+        QS_LAUNCHED(ctx);
+      }
       while (bnd.size() > 2) {
         if (bnd.size() - 1 > 0x7fffffff) fail(QS_ERR_SHAPE, "markSet: too many blocks");
         d_bnd = upload(bnd);
@@ -882,11 +936,15 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
       std::vector<int> hinfo(nb);
       QS_CUDA(cudaMemcpyAsync(hinfo.data(), ib, nb * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       QS_CUDA(cudaStreamSynchronize(ctx->stream));
-      for (int j = 0; j < nb; ++j)
-        if (hinfo[j] < 0) fail(QS_ERR_NUMERIC, "syevjBatched: argument error %d", hinfo[j]);
       for (void *p : {(void *)Ab, (void *)Wb, (void *)ib, (void *)work, (void *)d_so, (void *)d_do, (void *)d_sz,
                       (void *)d_eo, (void *)d_ed, (void *)d_es})
         dev_free(ctx, p);
+      for (int j = 0; j < nb; ++j) {
+        if (hinfo[j] < 0) fail(QS_ERR_NUMERIC, "syevjBatched: argument error %d", hinfo[j]);
+        if (hinfo[j] > 0)
+          fail(QS_ERR_NUMERIC, "eig: block %lld (%d x %d) did not converge in the Jacobi solver (info %d)",
+               (long long)kv.second[j], ni, ni, hinfo[j]);
+      }
     }
     cusolverDnDestroySyevjInfo(params);
   }
@@ -1100,6 +1158,26 @@ void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double
   try {
     if (!all_finite(c, H->d, m.nelem * es)) fail(QS_ERR_NUMERIC, "eigQS: H holds non-finite entries");
     eig_blocks(c, nb, n.data(), m.offs.data(), eoffs.data(), H->d, dE, U, m.cplx);
+    // each block's levels non-decreasing (solvers order degenerate levels
+    // only up to rounding), so that its kept levels are its first columns
+    if (ntot > 0) {
+      std::vector<int64_t> bnd;
+      for (int64_t i = 0; i < nb; ++i)
+        if (n[i] > 0) bnd.push_back(eoffs[i]);
+      bnd.push_back(ntot);
+      int64_t *d_bnd = dev_upload(c, bnd);
+      unsigned long long *d_bad = dev_alloc<unsigned long long>(c, 1);
+      QS_CUDA(cudaMemsetAsync(d_bad, 0xFF, 8, c->stream));
+      const int nruns = (int)(bnd.size() - 1);
+      monotone_blocks_kernel<<<(nruns + 127) / 128, 128, 0, c->stream>>>(dE, d_bnd, nruns, 64 * DBL_EPSILON, d_bad);
+      QS_LAUNCHED(c);
+      unsigned long long bad = 0;
+      QS_CUDA(cudaMemcpyAsync(&bad, d_bad, 8, cudaMemcpyDeviceToHost, c->stream));
+      QS_CUDA(cudaStreamSynchronize(c->stream));
+      dev_free(c, d_bnd);
+      dev_free(c, d_bad);
+      if (bad != ~0ull) fail(QS_ERR_NUMERIC, "eigQS: the solver returned level %llu below its predecessor", bad);
+    }
     // markSet on the device: the eigenvalues stay there; the host gets the
     // kept count of every block (a prefix: its lowest levels)
     std::vector<int64_t> k;

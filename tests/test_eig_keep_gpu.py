@@ -66,3 +66,25 @@ def test_large_spectrum(ctx):
     E = [np.sort(np.round(rng.standard_normal(int(k)) * 3, 4)) for k in sizes]
     for args in ((4096, 0.0, 1e-8), (4096, 0.0, 0.0), (8000, 1.0, 0.0), (2000, 0.0, 1e-6)):
         _same(E, args, ctx)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_blocks_out_of_order(ctx, seed):
+    """Levels of a block need not come ascending: degenerate levels a unit in
+    the last place apart in either order (as solvers return them) and blocks
+    in arbitrary order give the same flags as the host's stable sort."""
+    rng = np.random.default_rng(100 + seed)
+    E = []
+    for _ in range(int(rng.integers(2, 120))):
+        k = int(rng.integers(0, 80))
+        e = np.sort(np.round(rng.standard_normal(k) * 1e7, 0))
+        for i in range(1, k):                      # swap neighbours a rounding apart
+            if rng.random() < 0.3:
+                e[i] = np.nextafter(e[i - 1], -np.inf)
+        if seed == 2:
+            rng.shuffle(e)                          # any order at all
+        E.append(e)
+    N = sum(len(e) for e in E)
+    for nkeep in (1, N // 3, N // 2, N - 1):
+        for deps in (0.0, 1e-12, 1e-6):
+            _same(E, (nkeep, 0.0, deps), ctx)

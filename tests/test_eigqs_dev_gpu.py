@@ -79,3 +79,43 @@ def test_eigqs_dev_rejects_off_diagonal(ctx):
     with pytest.raises(QSError) as e:
         eigQS_dev(T)
     assert e.value.code == 3
+
+
+@pytest.mark.parametrize("deps", [0.0, 1e-10])
+def test_eigqs_dev_degenerate_levels(ctx, deps):
+    """Blocks with exactly degenerate multiplets at a large scale (the NRG
+    Hamiltonian before rescaling): the solver returns degenerate levels only
+    up to rounding, in either order.  Each block's levels come back
+    non-decreasing, its kept states are its first columns, and they are
+    eigenvectors of their levels."""
+    rng = np.random.default_rng(21)
+    sizes = [650, 380, 24, 9, 200, 130]
+    data = []
+    for n in sizes:
+        lv = np.round(rng.standard_normal(-(-n // 6)) * 4e7, 3)
+        d = np.sort(np.repeat(lv, 6)[:n])           # sextets (one partial)
+        Qm, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        data.append((Qm * d) @ Qm.T)
+    labels = np.arange(len(sizes), dtype=np.int32).reshape(-1, 1)
+    H = QSpace([labels.copy(), labels.copy()], [(x + x.T) / 2 for x in data])
+    T = upload(H, ctx)
+    N = sum(sizes)
+    for nkeep in (N // 4, N // 2 + 1, N - 7):
+        Etot, I = eigQS_dev(T, Nkeep=nkeep, deps=deps)
+        ak = _blocks(I["AK"].download())
+        o = 0
+        for i, (d, n) in enumerate(zip(H.data, sizes)):
+            e = I["E"][o:o + n]
+            assert np.all(np.diff(e) >= 0)
+            flags = I["keep"][o:o + n]
+            k = int(flags.sum())
+            assert np.all(flags[:k]) and not np.any(flags[k:])
+            if k:
+                U = ak[(i,)]
+                assert U.shape == (n, k)
+                r = d @ U - U * e[None, :k]
+                assert np.max(np.abs(r)) <= 1e-9 * np.abs(e).max()
+            o += n
+        for t in (I["AK"], I["AD"]):
+            t.free()
+    T.free()
