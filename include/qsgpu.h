@@ -385,6 +385,15 @@ QS_EXPORT qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E
                        double deps, uint8_t *keep, int64_t *nkeep_out,
                        double *etrunc_out);
 
+/* markSet's degeneracy averaging alone (Source/gathered.cc:1847-1866): the
+ * levels of all blocks (n[i] back to back in E, host arrays) in stable
+ * ascending order, clusters of consecutive levels closer than
+ * deps * (max - min) replaced by their mean, written to E_out in E's order
+ * (E_out may be E).  deps <= 0 copies E.  eigQS reports these levels when
+ * deps > 0. */
+QS_EXPORT qs_status qs_average_levels(int64_t nblk, const int64_t *n, const double *E, double deps,
+                       double *E_out);
+
 /* qs_mark_keep with the eigenvalues on the device (E: device array, blocks'
  * ascending eigenvalues back to back; n: host array of block sizes) and the
  * 0/1 flags written to the device array `keep`; NK and Etrunc as
@@ -405,7 +414,11 @@ QS_EXPORT qs_status qs_mark_keep_dev(qs_ctx *ctx, int64_t nblk, const int64_t *n
  * block sizes) = ascending eigenvalues per block in H's block order, keep =
  * 0/1 per eigenvalue, NK as qs_mark_keep reports it (not always the kept
  * count: count the kept states from `keep` or from *AK's blocks) and the
- * truncation energy. */
+ * truncation energy.  With deps > 0 the eigenvalues in E are the averaged
+ * ones, as markSet writes them back for the reference's eigQS (clusters of
+ * levels closer than deps times the spectral width share their mean;
+ * qs_average_levels); a block's levels that the solver returned a rounding
+ * out of order (degenerate levels) are made non-decreasing. */
 QS_EXPORT qs_status qs_eigQS_dev(qs_ctx *ctx, const qs_tensor *H, int64_t nkeep, double etrunc,
                        double deps, qs_tensor **AK, qs_tensor **AD, double *E,
                        uint8_t *keep, int64_t *nkeep_out, double *etrunc_out);

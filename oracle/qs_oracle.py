@@ -564,6 +564,31 @@ def flops_of_contract(A: dict, ia, B: dict, ib) -> int:
 # truncation (markSet) and the Gram-Schmidt step
 # --------------------------------------------------------------------------
 
+def average_levels(E_blocks: list, deps: float) -> list:
+    """markSet's degeneracy averaging (Source/gathered.cc:1847-1866): all
+    levels in stable ascending order, each run of consecutive levels closer
+    than deps * |max - min| replaced by its mean, written back per block in
+    the input order (E.permute(x, iP) and the memcpy into E0 there) -- the
+    levels eigQS reports when deps > 0."""
+    sizes = [len(e) for e in E_blocks]
+    E = np.concatenate([np.asarray(e, float) for e in E_blocks]) if E_blocks else np.zeros(0)
+    N = len(E)
+    if N == 0 or not deps > 0:
+        return [np.asarray(e, float).copy() for e in E_blocks]
+    P = np.argsort(E, kind="stable")
+    s = E[P].copy()
+    eps = deps * abs(s[-1] - s[0])
+    i0 = 0
+    for i in range(1, N + 1):
+        if i == N or abs(s[i] - s[i - 1]) > eps:
+            if i - i0 > 1:
+                s[i0:i] = np.mean(s[i0:i])
+            i0 = i
+    x = np.empty(N)
+    x[P] = s
+    return [x[o:o + n] for o, n in zip(np.cumsum([0] + sizes[:-1]), sizes)]
+
+
 def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0):
     """Kept-eigenvalue mask per block; restates markSet for ascending order
     (Source/gathered.cc:1822-2040) with eigQS's option handling

@@ -242,3 +242,38 @@ def permuteQS(A: dict, perm, conj: bool = False) -> dict:
     finally:
         for a in args:
             lib.mxDestroyArray(a)
+
+
+def plusQS(A: dict, B: dict, f: float = 1.0) -> dict:
+    """The reference's plusQS(A, B [,f]) = A + f B."""
+    lib = _fake()
+    args = [to_mx(A), to_mx(B), _arg(float(f))]
+    try:
+        out = call("plusQS", args, 1)[0]
+        res = from_mx(out) if out else {"Q": [], "data": [], "info": {}}
+        if out:
+            lib.mxDestroyArray(out)
+        return res
+    finally:
+        for a in args:
+            lib.mxDestroyArray(a)
+
+
+def eigQS(H: dict, **opts) -> tuple:
+    """The reference's [Etot, I] = eigQS(H, 'Nkeep', .., 'deps', .., 'Etrunc', ..):
+    returns (Etot, {'AK','AD','EK','ED': QSpace dicts, 'NK': int})."""
+    lib = _fake()
+    args = [to_mx(H)]
+    for k, v in opts.items():
+        args += [_mx_string(k), _arg(v)]
+    try:
+        Etot, I = call("eigQS", args, 2)
+        res = {k: from_mx(lib.mxGetField(I, 0, k.encode())) for k in ("AK", "AD", "EK", "ED")}
+        res["NK"] = int(_np_of(lib.mxGetField(I, 0, b"NK")).ravel()[0])
+        e = _np_of(Etot).copy()
+        lib.mxDestroyArray(Etot)
+        lib.mxDestroyArray(I)
+        return e, res
+    finally:
+        for a in args:
+            lib.mxDestroyArray(a)

@@ -141,6 +141,7 @@ SIGNATURES = {
                                 C.c_void_p, C.c_void_p, C.c_int32]),
     "qs_mark_keep": (C.c_int, [C.c_int64, c_int64_p, c_double_p, c_double_p, C.c_int64, C.c_double,
                                C.c_double, C.POINTER(C.c_uint8), c_int64_p, c_double_p]),
+    "qs_average_levels": (C.c_int, [C.c_int64, c_int64_p, c_double_p, C.c_double, c_double_p]),
     "qs_mark_keep_dev": (C.c_int, [C.c_void_p, C.c_int64, c_int64_p, C.c_void_p, C.c_int64, C.c_double,
                                    C.c_double, C.c_void_p, c_int64_p, c_double_p]),
     "qs_svd_blocks": (C.c_int, [C.c_void_p, C.c_int64, c_int64_p, c_int64_p, c_int64_p, c_int64_p,

@@ -191,8 +191,11 @@ __global__ void scale_kernel(double *__restrict__ v, int64_t n, const double *__
 // *nkeep_out is the reference's NK output: the number kept, except with
 // Etrunc > 0 and deps = 0, where markSet leaves it at min(Nkeep, N) (only its
 // gap-search branch writes the cut back); `keep` holds the kept states.
+// With e_avg the levels after the degeneracy averaging go there, in E's
+// order: markSet writes them back into the blocks' eigenvalue vectors, so
+// eigQS reports averaged levels when deps > 0 (Source/gathered.cc:1851-1866).
 void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nkeep_in, double etrunc,
-                    double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out) {
+                    double deps, uint8_t *keep, int64_t *nkeep_out, double *etrunc_out, double *e_avg) {
   int64_t N = 0;
   for (int64_t i = 0; i < nblk; ++i) N += n[i];
   std::fill(keep, keep + N, 0);
@@ -222,6 +225,8 @@ void mark_keep_host(int64_t nblk, const int64_t *n, const double *E, int64_t nke
       }
     }
   }
+  if (e_avg)
+    for (int64_t i = 0; i < N; ++i) e_avg[P[i]] = s[i];
   int64_t Nkeep = (nkeep_in < 0 || nkeep_in > N) ? N : nkeep_in;
   if (Nkeep == 0) return;
   if (Nkeep >= N && etrunc <= 0) {
@@ -441,6 +446,13 @@ __global__ void first_above_kernel(const double *__restrict__ a, int64_t N, doub
     if (a[l] >= x) atomicMin(lcut, (unsigned long long)l);
 }
 
+// out[P[i]] = v[i]: sorted levels back to block order
+__global__ void scatter_levels_kernel(const int64_t *__restrict__ P, const double *__restrict__ v, int64_t N,
+                                      double *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    out[P[i]] = v[i];
+}
+
 __global__ void scatter_keep_kernel(const int64_t *__restrict__ P, int64_t N, int64_t l, uint8_t *__restrict__ keep) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
     keep[P[i]] = i < l ? 1 : 0;
@@ -461,7 +473,7 @@ __global__ void count_kept_kernel(const uint8_t *__restrict__ keep, const int64_
 // receives the flags and kcount (host) the kept levels per block.
 void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoffs, const double *dE,
                    int64_t nkeep_in, double etrunc, double deps, uint8_t *d_keep, std::vector<int64_t> &kcount,
-                   int64_t *nkeep_out, double *etrunc_out) {
+                   int64_t *nkeep_out, double *etrunc_out, double *dE_avg) {
   int64_t N = 0;
   for (int64_t i = 0; i < nblk; ++i) N += n[i];
   kcount.assign((size_t)std::max<int64_t>(nblk, 0), 0);
@@ -482,10 +494,16 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
     return p;
   };
   try {
-    if (Nkeep == 0 || (Nkeep >= N && etrunc <= 0)) {
+    // markSet averages the degenerate clusters before it looks at Nkeep:
+    // with dE_avg the averaged levels go back there (block order) even when
+    // every level is kept
+    const bool shortcut = Nkeep == 0 || (Nkeep >= N && etrunc <= 0);
+    const bool avg_out = dE_avg && deps > 0;
+    if (shortcut) {
       l = Nkeep == 0 ? 0 : N;
       QS_CUDA(cudaMemsetAsync(d_keep, l ? 1 : 0, (size_t)N, st));
-    } else {
+    }
+    if (!shortcut || avg_out) {
       // stable ascending order: log2(nblk) rounds of pairwise run merges
       double *v0 = static_cast<double *>(alloc(N * 8)), *v1 = static_cast<double *>(alloc(N * 8));
       int64_t *i0 = static_cast<int64_t *>(alloc(N * 8)), *i1 = static_cast<int64_t *>(alloc(N * 8));
@@ -552,52 +570,58 @@ void mark_keep_dev(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *eoff
       unsigned long long *d_l = reinterpret_cast<unsigned long long *>(upload({(int64_t)N}));
       average_clusters_kernel<<<grid, 256, 0, st>>>(v0, v1, N, deps);
       QS_LAUNCHED(ctx);
-      if (etrunc > 0) {
-        first_above_kernel<<<grid, 256, 0, st>>>(v1, N, etrunc, d_l);
+      if (avg_out) {
+        scatter_levels_kernel<<<grid, 256, 0, st>>>(i0, v1, N, dE_avg);
         QS_LAUNCHED(ctx);
       }
-      double ends[2];
-      unsigned long long lfirst = lN;
-      QS_CUDA(cudaMemcpyAsync(&ends[0], v1, 8, cudaMemcpyDeviceToHost, st));
-      QS_CUDA(cudaMemcpyAsync(&ends[1], v1 + N - 1, 8, cudaMemcpyDeviceToHost, st));
-      QS_CUDA(cudaMemcpyAsync(&lfirst, d_l, 8, cudaMemcpyDeviceToHost, st));
-      QS_CUDA(cudaStreamSynchronize(st));
-      l = etrunc > 0 ? std::min<int64_t>((int64_t)lfirst, Nkeep) : Nkeep;
-      if (l < N && l > 0 && deps > 0) {
-        // weighted-gap search over the window around the cut (host arithmetic)
-        const int64_t nx = std::max<int64_t>(16, l / 5);
-        const double q = 10.0 / (double)nx;
-        const int64_t NX = (int64_t)(5.0 / q);
-        int64_t i = std::max<int64_t>(1, l - NX);
-        const int64_t i2 = std::min<int64_t>(N, l + NX);
-        std::vector<double> w((size_t)(i2 - i + 1));
-        QS_CUDA(cudaMemcpyAsync(w.data(), v1 + (i - 1), w.size() * 8, cudaMemcpyDeviceToHost, st));
+      if (!shortcut) {
+        if (etrunc > 0) {
+          first_above_kernel<<<grid, 256, 0, st>>>(v1, N, etrunc, d_l);
+          QS_LAUNCHED(ctx);
+        }
+        double ends[2];
+        unsigned long long lfirst = lN;
+        QS_CUDA(cudaMemcpyAsync(&ends[0], v1, 8, cudaMemcpyDeviceToHost, st));
+        QS_CUDA(cudaMemcpyAsync(&ends[1], v1 + N - 1, 8, cudaMemcpyDeviceToHost, st));
+        QS_CUDA(cudaMemcpyAsync(&lfirst, d_l, 8, cudaMemcpyDeviceToHost, st));
         QS_CUDA(cudaStreamSynchronize(st));
-        const int64_t w0 = i - 1;
-        int64_t imax = l;
-        double xmax = 0;
-        for (; i < i2; ++i) {
-          const double t = q * (double)(i - l);
-          const double x = std::exp(-t * t) * std::fabs(w[i - w0] - w[i - 1 - w0]);
-          if (x > xmax) { xmax = x; imax = i; }
-        }
-        if (i == N) {
-          const double t = q * (double)(i - l);
-          const double x = 0.1 * std::exp(-t * t) * std::fabs(ends[1] - ends[0]);
-          if (x > xmax) { xmax = x; imax = i; }
-        }
-        l = imax;
-      }
-      if (l >= N) l = N;
-      scatter_keep_kernel<<<grid, 256, 0, st>>>(i0, N, l, d_keep);
-      QS_LAUNCHED(ctx);
-      if (etrunc_out) {
-        double sl = 0;
-        if (l < N) {
-          QS_CUDA(cudaMemcpyAsync(&sl, v1 + l, 8, cudaMemcpyDeviceToHost, st));
+        l = etrunc > 0 ? std::min<int64_t>((int64_t)lfirst, Nkeep) : Nkeep;
+        if (l < N && l > 0 && deps > 0) {
+          // weighted-gap search over the window around the cut (host arithmetic)
+          const int64_t nx = std::max<int64_t>(16, l / 5);
+          const double q = 10.0 / (double)nx;
+          const int64_t NX = (int64_t)(5.0 / q);
+          int64_t i = std::max<int64_t>(1, l - NX);
+          const int64_t i2 = std::min<int64_t>(N, l + NX);
+          std::vector<double> w((size_t)(i2 - i + 1));
+          QS_CUDA(cudaMemcpyAsync(w.data(), v1 + (i - 1), w.size() * 8, cudaMemcpyDeviceToHost, st));
           QS_CUDA(cudaStreamSynchronize(st));
+          const int64_t w0 = i - 1;
+          int64_t imax = l;
+          double xmax = 0;
+          for (; i < i2; ++i) {
+            const double t = q * (double)(i - l);
+            const double x = std::exp(-t * t) * std::fabs(w[i - w0] - w[i - 1 - w0]);
+            if (x > xmax) { xmax = x; imax = i; }
+          }
+          if (i == N) {
+            const double t = q * (double)(i - l);
+            const double x = 0.1 * std::exp(-t * t) * std::fabs(ends[1] - ends[0]);
+            if (x > xmax) { xmax = x; imax = i; }
+          }
+          l = imax;
         }
-        *etrunc_out = (l < N) ? sl - ends[0] : 0.0;
+        if (l >= N) l = N;
+        scatter_keep_kernel<<<grid, 256, 0, st>>>(i0, N, l, d_keep);
+        QS_LAUNCHED(ctx);
+        if (etrunc_out) {
+          double sl = 0;
+          if (l < N) {
+            QS_CUDA(cudaMemcpyAsync(&sl, v1 + l, 8, cudaMemcpyDeviceToHost, st));
+            QS_CUDA(cudaStreamSynchronize(st));
+          }
+          *etrunc_out = (l < N) ? sl - ends[0] : 0.0;
+        }
       }
     }
     int64_t *d_n = dev_upload(ctx, std::vector<int64_t>(n, n + nblk));
@@ -1115,7 +1139,21 @@ qs_status qs_mark_keep(int64_t nblk, const int64_t *n, const double *E, const do
   QS_API_BEGIN
   if (nblk < 0 || (nblk > 0 && (!n || !E || !keep))) fail(QS_ERR_ARG, "null argument");
   if (qdim_w) fail(QS_ERR_UNSUPPORTED, "multiplet weights: markSet counts every multiplet once; pass NULL");
-  mark_keep_host(nblk, n, E, nkeep, etrunc, deps, keep, nkeep_out, etrunc_out);
+  mark_keep_host(nblk, n, E, nkeep, etrunc, deps, keep, nkeep_out, etrunc_out, nullptr);
+  QS_API_END
+}
+
+qs_status qs_average_levels(int64_t nblk, const int64_t *n, const double *E, double deps, double *E_out) {
+  QS_API_BEGIN
+  if (nblk < 0 || (nblk > 0 && (!n || !E || !E_out))) fail(QS_ERR_ARG, "null argument");
+  int64_t N = 0;
+  for (int64_t i = 0; i < nblk; ++i) {
+    if (n[i] < 0) fail(QS_ERR_ARG, "negative block size");
+    N += n[i];
+  }
+  if (N == 0) return QS_OK;
+  std::vector<uint8_t> keep((size_t)N);
+  mark_keep_host(nblk, n, E, -1, 0.0, deps, keep.data(), nullptr, nullptr, E_out);
   QS_API_END
 }
 
@@ -1182,7 +1220,7 @@ void eigqs_core(Ctx *c, const qs_tensor *H, int64_t nkeep, double etrunc, double
     // kept count of every block (a prefix: its lowest levels)
     std::vector<int64_t> k;
     d_keep = dev_alloc<uint8_t>(c, (size_t)std::max<int64_t>(ntot, 1));
-    mark_keep_dev(c, nb, n.data(), eoffs.data(), dE, nkeep, etrunc, deps, d_keep, k, &nk, &et);
+    mark_keep_dev(c, nb, n.data(), eoffs.data(), dE, nkeep, etrunc, deps, d_keep, k, &nk, &et, dE);
     for (int64_t i = 0; i < nb; ++i)
       if (k[i] < 0 || k[i] > n[i])
         fail(QS_ERR_INTERNAL, "eigQS: block %lld keeps %lld of %lld states", (long long)i, (long long)k[i],
@@ -1287,7 +1325,7 @@ qs_status qs_mark_keep_dev(qs_ctx *ctx, int64_t nblk, const int64_t *n, const do
   }
   QS_CUDA(cudaSetDevice(ctx->c.device));
   std::vector<int64_t> k;
-  mark_keep_dev(&ctx->c, nblk, n, eoffs.data(), E, nkeep, etrunc, deps, keep, k, nkeep_out, etrunc_out);
+  mark_keep_dev(&ctx->c, nblk, n, eoffs.data(), E, nkeep, etrunc, deps, keep, k, nkeep_out, etrunc_out, nullptr);
   QS_API_END
 }
 

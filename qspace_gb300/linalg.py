@@ -69,6 +69,20 @@ def mark_keep(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float 
     return [keep[o:o + k].astype(bool) for o, k in zip(offs, n)], nk.value, et.value
 
 
+def average_levels(E_blocks: list, deps: float) -> list:
+    """markSet's degeneracy averaging (qs_average_levels): clusters of levels
+    closer than deps times the spectral width replaced by their mean, per
+    block in the input order (what eigQS reports when deps > 0)."""
+    lib = _capi.load()
+    n = np.array([len(e) for e in E_blocks], np.int64)
+    E = np.concatenate([np.asarray(e, np.float64) for e in E_blocks]) if E_blocks else np.zeros(0)
+    out = np.zeros(max(len(E), 1), np.float64)
+    check(lib.qs_average_levels(len(n), _ptr(n), E.ctypes.data_as(_capi.c_double_p), float(deps),
+                                out.ctypes.data_as(_capi.c_double_p)))
+    offs = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+    return [out[o:o + k].copy() for o, k in zip(offs, n)]
+
+
 def mark_keep_dev(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: float = 0.0,
                   ctx: Context | None = None):
     """The same truncation with the eigenvalues on the device
@@ -93,7 +107,9 @@ def mark_keep_dev(E_blocks: list, nkeep: int = -1, etrunc: float = 0.0, deps: fl
 def eigQS(H: QSpace, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0, ctx: Context | None = None):
     """Block eigendecomposition + truncation of a block-diagonal rank-2
     abelian QSpace.  Returns (Etot, I) with Etot the ascending eigenvalues of
-    all blocks and I = {'AK','AD','EK','ED','NK'} as in eigQS."""
+    all blocks and I = {'AK','AD','EK','ED','NK'} as in eigQS (with deps > 0
+    the levels after markSet's degeneracy averaging, as the reference
+    reports them)."""
     if H.rank != 2:
         raise ValueError("eigQS: rank-2 QSpace required")
     for i in range(H.nblk):
@@ -102,6 +118,8 @@ def eigQS(H: QSpace, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0, ct
     blocks = [np.asarray(d).reshape(H.block_dims(i)) for i, d in enumerate(H.data)]
     Es, Us = eig_blocks(blocks, ctx)
     keep, nk, _ = mark_keep(Es, Nkeep, Etrunc, deps)
+    if deps > 0:          # markSet writes the averaged levels back (reported by eigQS)
+        Es = average_levels(Es, deps)
     parts = {}
     for tag, sel in (("K", True), ("D", False)):
         Q0, Q1, data, EQ, Ed = [], [], [], [], []

@@ -9,7 +9,8 @@ Writes tests/golden/eig_golden.npz: seeded block-diagonal real symmetric
 rank-2 H (some sectors repeat another's block, so levels are exactly
 degenerate across sectors), the options (Nkeep, Etrunc, deps) and the
 reference's outputs: the kept count NK, the truncation energy Etrunc and the
-kept eigenvalues EK of every sector.  (The reference's NK equals the number
+kept eigenvalues EK of every sector and all levels Etot (ascending; with
+deps > 0 both hold markSet's averaged levels).  (The reference's NK equals the number
 of kept states except with Etrunc > 0 and deps = 0, where it stays
 min(Nkeep, N); EK always holds the kept states.)
 """
@@ -32,16 +33,24 @@ OPTIONS = [
     {"Nkeep": 10}, {"Nkeep": 25}, {"Nkeep": 25, "deps": 1e-8}, {"Nkeep": 40, "deps": 1e-3},
     {"Etrunc": 1.5}, {"Nkeep": 30, "Etrunc": 2.0}, {"Nkeep": 500}, {"Nkeep": 17, "deps": 1e-6},
     {"Etrunc": 0.8, "deps": 1e-6}, {"Nkeep": 60, "Etrunc": 2.5, "deps": 1e-8},
+    # near-degenerate sectors (copies perturbed by ~1e-10): markSet averages
+    # the clusters and eigQS reports the averaged levels
+    {"Nkeep": 25, "deps": 1e-8, "near": 1e-10}, {"Nkeep": 40, "deps": 1e-6, "near": 1e-9},
+    {"Nkeep": 500, "deps": 1e-6, "near": 1e-10}, {"Etrunc": 1.0, "deps": 1e-7, "near": 3e-10},
 ]
 
 
-def hamiltonian(seed: int):
+def hamiltonian(seed: int, near: float = 0.0):
     rng = np.random.default_rng(seed)
     labs = sorted({(int(a), int(b)) for a, b in rng.integers(-3, 4, size=(int(rng.integers(7, 11)), 2))})
     data = []
     for i, _ in enumerate(labs):
         if i and rng.uniform() < 0.35:
-            data.append(data[int(rng.integers(0, i))].copy())     # degenerate with an earlier sector
+            x = data[int(rng.integers(0, i))].copy()     # degenerate with an earlier sector
+            if near:
+                y = rng.standard_normal(x.shape)
+                x = x + near * (y + y.T) / 2               # ... up to ~near
+            data.append(x)
             continue
         n = int(rng.integers(3, 21))
         x = rng.standard_normal((n, n))
@@ -57,16 +66,18 @@ def main():
     z, meta = {}, []
     for c, opts in enumerate(OPTIONS):
         name = f"eig{c}"
-        H = hamiltonian(200 + c)
+        H = hamiltonian(200 + c, opts.get("near", 0.0))
         args = [ref.to_mx(H)]
         for k, v in opts.items():
-            args += [ref._mx_string(k), ref._arg(v)]
+            if k != "near":
+                args += [ref._mx_string(k), ref._arg(v)]
         Etot, I = ref.call("eigQS", args, 2)
         EK = ref.from_mx(lib.mxGetField(I, 0, b"EK"))
         nk = int(ref._np_of(lib.mxGetField(I, 0, b"NK")).ravel()[0])
         et = float(ref._np_of(lib.mxGetField(I, 0, b"Etrunc")).ravel()[0])
         pack(f"{name}_H", H, z)
         pack(f"{name}_EK", EK, z)
+        z[f"{name}_Etot"] = ref._np_of(Etot).ravel().copy()
         meta.append({"name": name, "opts": opts, "NK": nk, "Etrunc": et})
         for x in (Etot, I) + tuple(args):
             lib.mxDestroyArray(x)

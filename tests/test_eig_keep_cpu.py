@@ -1,8 +1,10 @@
 """eigQS's truncation (markSet over all blocks' eigenvalues: Nkeep, Etrunc,
 degeneracy averaging with the weighted-gap cut for deps > 0) against fixtures
 made by the REFERENCE's own eigQS (tests/golden/make_eig_golden.py): the
-oracle's restatement and the library's host implementation (qs_mark_keep)
-keep the same states of every sector as the reference and report the same NK
+oracle's restatement and the library's host implementation (qs_mark_keep,
+qs_average_levels) keep the same states of every sector as the reference,
+report the same levels (averaged over near-degenerate clusters when
+deps > 0, as markSet writes them back) and the same NK
 (with Etrunc > 0 and deps = 0 the reference's NK stays min(Nkeep, N) while
 its kept set EK follows Etrunc)."""
 import json
@@ -12,7 +14,7 @@ import numpy as np
 import pytest
 
 from oracle import qs_oracle as orc
-from qspace_gb300.linalg import mark_keep
+from qspace_gb300.linalg import average_levels, mark_keep
 from tests.golden.golden_io import unpack
 
 G = Path(__file__).resolve().parent / "golden"
@@ -26,7 +28,7 @@ def _cases():
 @pytest.mark.parametrize("impl", ["oracle", "library"])
 def test_eig_truncation_matches_reference(impl):
     z, cases = _cases()
-    assert len(cases) == 10
+    assert len(cases) == 14
     for c in cases:
         H, EK = unpack(f"{c['name']}_H", z), unpack(f"{c['name']}_EK", z)
         E = [np.linalg.eigvalsh(np.asarray(d)) for d in H["data"]]
@@ -34,8 +36,14 @@ def test_eig_truncation_matches_reference(impl):
         args = (int(o.get("Nkeep", -1)), float(o.get("Etrunc", 0.0)), float(o.get("deps", 0.0)))
         if impl == "oracle":
             keep, nk = orc.mark_keep(E, *args)
+            E = orc.average_levels(E, args[2])
         else:
             keep, nk, _ = mark_keep(E, *args)
+            E = average_levels(E, args[2])
+        # the reported levels: averaged over degenerate clusters when deps > 0
+        Etot = np.sort(np.concatenate(E))
+        ref_tot = np.sort(z[f"{c['name']}_Etot"])
+        assert np.max(np.abs(Etot - ref_tot)) <= 1e-13 * np.abs(ref_tot).max(), c["name"]
         assert nk == c["NK"], c
         assert sum(int(np.sum(k)) for k in keep) == sum(np.size(d) for d in EK["data"]), c
         got = {tuple(np.asarray(H["Q"][0][i]).ravel()): E[i][np.asarray(keep[i], bool)] for i in range(len(E))
@@ -44,3 +52,20 @@ def test_eig_truncation_matches_reference(impl):
         assert got.keys() == ref.keys(), c["name"]
         for k in ref:
             assert np.allclose(got[k], ref[k], rtol=1e-12, atol=1e-12), (c["name"], k)
+
+
+def test_average_levels_matches_oracle():
+    """qs_average_levels against the oracle's restatement on random spectra
+    with exact and near degeneracies within and across blocks."""
+    rng = np.random.default_rng(4)
+    for trial in range(20):
+        E = []
+        for _ in range(int(rng.integers(0, 30))):
+            e = np.round(rng.standard_normal(int(rng.integers(0, 25))), 3)
+            e = e + 1e-11 * rng.standard_normal(len(e)) * (trial % 2)
+            E.append(np.sort(e))
+        for deps in (0.0, 1e-9, 1e-6, 1e-3):
+            a, b = average_levels(E, deps), orc.average_levels(E, deps)
+            assert len(a) == len(b)
+            for x, y in zip(a, b):
+                assert np.allclose(x, y, rtol=0, atol=1e-14)

@@ -77,3 +77,12 @@ def test_concurrent_runs_through_the_serving_loop_match_runs_alone(ctx):
         assert Km.nkept == Ka.nkept and sorted(Km.E) == sorted(Ka.E)
         for lab in Ka.E:
             assert np.max(np.abs(Km.E[lab] - Ka.E[lab])) <= 1e-12 * max(1.0, np.abs(Ka.E[lab]).max())
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("split", 1e-11)])
+def test_device_chain_matches_reference_fixture(ctx, prec, tol):
+    """The device iteration against chains run on the reference's own MEX
+    functions (tests/golden/nrg_golden.npz): same truncation in every sector,
+    same levels (averaged over degenerate clusters, as eigQS reports them)."""
+    from tests.test_nrg_cpu import chain_matches_reference
+    chain_matches_reference(lambda: DeviceBackend(ctx, prec), tol)
