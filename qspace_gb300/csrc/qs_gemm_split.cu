@@ -565,11 +565,14 @@ __device__ __forceinline__ void strip_b(const SplitPair *__restrict__ pairs, con
   }
 }
 
-template <bool CPLX, int S>
+// VIEWS = false: no pair of the launch reads its operand through a view, and
+// the view addressing is compiled out
+template <bool CPLX, int S, bool VIEWS>
 __global__ void __launch_bounds__(STRIP_THREADS)
-strip_a_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restrict__ views,
+strip_a_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restrict__ views_in,
                const int4 *__restrict__ tasks, const double *__restrict__ A, const double *__restrict__ B,
                int *__restrict__ E, uint8_t *__restrict__ arena, int b) {
+  const OperandView *views = VIEWS ? views_in : nullptr;
   const int4 tk = tasks[blockIdx.x];
   switch (b) {  // the host admits b = 5..8 only
     case 5: strip_a<CPLX, S, 5>(pairs, views, tk, A, B, E, arena); break;
@@ -579,11 +582,14 @@ strip_a_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restric
   }
 }
 
-template <bool CPLX, int S>
+// VIEWS = false: no pair of the launch reads its operand through a view, and
+// the view addressing is compiled out
+template <bool CPLX, int S, bool VIEWS>
 __global__ void __launch_bounds__(STRIP_THREADS)
-strip_b_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restrict__ views,
+strip_b_kernel(const SplitPair *__restrict__ pairs, const OperandView *__restrict__ views_in,
                const int4 *__restrict__ tasks, const double *__restrict__ A, const double *__restrict__ B,
                int *__restrict__ F, uint8_t *__restrict__ arena, int b) {
+  const OperandView *views = VIEWS ? views_in : nullptr;
   const int4 tk = tasks[blockIdx.x];
   switch (b) {
     case 5: strip_b<CPLX, S, 5>(pairs, views, tk, A, B, F, arena); break;
@@ -1050,13 +1056,21 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const Operand
   if (b < 5 || b > 8 || b * S > 62) fail(QS_ERR_INTERNAL, "split: unsupported digit plan b=%d S=%d", b, S);
   cudaStream_t st = ctx->stream;
   ctx->mark(0);
-  if (cplx) {
-    if (nsa) { strip_a_kernel<true, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_va, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nsb) { strip_b_kernel<true, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
-  } else {
-    if (nsa) { strip_a_kernel<false, S><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_va, d_sa, A, B, dE, arena, b); QS_LAUNCHED(ctx); }
-    if (nsb) { strip_b_kernel<false, S><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b); QS_LAUNCHED(ctx); }
-  }
+  auto strips = [&](auto cx) {
+    constexpr bool CX = decltype(cx)::value;
+    if (nsa) {
+      if (d_va) strip_a_kernel<CX, S, true><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_va, d_sa, A, B, dE, arena, b);
+      else strip_a_kernel<CX, S, false><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, nullptr, d_sa, A, B, dE, arena, b);
+      QS_LAUNCHED(ctx);
+    }
+    if (nsb) {
+      if (d_vb) strip_b_kernel<CX, S, true><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b);
+      else strip_b_kernel<CX, S, false><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, nullptr, d_sb, A, B, dF, arena, b);
+      QS_LAUNCHED(ctx);
+    }
+  };
+  if (cplx) strips(std::true_type{});
+  else strips(std::false_type{});
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);
   QS_CUDA(cudaFuncSetAttribute(gemm_split_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));

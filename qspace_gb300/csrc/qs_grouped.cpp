@@ -182,7 +182,7 @@ void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double
 }
 
 // Host-buffer form.  Large batches are cut at output-block boundaries into
-// chunks of similar input size; chunk i's operands are copied in on one copy
+// chunks of similar input size (the last few smaller); chunk i's operands are copied in on one copy
 // stream while chunk i-1 computes on the context stream and earlier results
 // are copied out on another, so the copies over the host link overlap the
 // products.  Only the part of A and B not yet copied is sent per chunk (one
@@ -215,10 +215,21 @@ static void grouped_host(Ctx *c, const qs_pair_list *pl, const double *A, int64_
       }
       tot += w[b];
     }
+    // the last chunks shrink geometrically (weights 1/2, 1/4, ... of the
+    // others; QS_HOST_TAPER of them, default 2): what remains after the last
+    // copy in -- the last chunk's products and its copy out -- is short
+    const char *e_tp = std::getenv("QS_HOST_TAPER");
+    const int taper = std::min(std::max(e_tp ? std::atoi(e_tp) : 2, 0), std::max(nchunk - 2, 0));
+    std::vector<double> frac(nchunk + 1, 0.0);
+    for (int k = 0; k < nchunk; ++k) {
+      const int t = k - (nchunk - taper) + 1;  // 1.. for the tapered chunks
+      frac[k + 1] = frac[k] + (t > 0 ? std::ldexp(1.0, -t) : 1.0);
+    }
     double acc = 0;
     for (size_t b = 0; b < nb; ++b) {
       acc += w[b];
-      if (cut.size() < (size_t)nchunk && acc >= tot * double(cut.size()) / nchunk && b + 1 < nb) cut.push_back(b + 1);
+      if (cut.size() < (size_t)nchunk && acc >= tot * frac[cut.size()] / frac[nchunk] && b + 1 < nb)
+        cut.push_back(b + 1);
     }
   }
   cut.push_back(nb);
