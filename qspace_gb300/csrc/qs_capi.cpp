@@ -129,10 +129,24 @@ void Ctx::ensure_copy_streams() {
   if (!d2h) QS_CUDA(cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking));
 }
 
+void Ctx::ensure_aux() {
+  if (!aux) QS_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+  if (!aux_fork) QS_CUDA(cudaEventCreateWithFlags(&aux_fork, cudaEventDisableTiming));
+  if (!aux_join) QS_CUDA(cudaEventCreateWithFlags(&aux_join, cudaEventDisableTiming));
+}
+
 void Ctx::destroy_copy_streams() {
   if (h2d) cudaStreamDestroy(h2d);
   if (d2h) cudaStreamDestroy(d2h);
   h2d = d2h = nullptr;
+  if (aux) {
+    cudaStreamSynchronize(aux);
+    cudaStreamDestroy(aux);
+  }
+  if (aux_fork) cudaEventDestroy(aux_fork);
+  if (aux_join) cudaEventDestroy(aux_join);
+  aux = nullptr;
+  aux_fork = aux_join = nullptr;
 }
 
 // A block's permutation on its fewest legs: legs of size 1 dropped, and

@@ -1052,25 +1052,41 @@ template <int S>
 void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const OperandView *d_va, const OperandView *d_vb,
                     const int4 *d_sa, int nsa, const int4 *d_sb, int nsb, const SplitTile *d_tiles, int ntiles,
                     const double *A, const double *B, double *C, int *dE, int *dF, uint8_t *arena, int b,
-                    int kchunk, int *err) {
+                    int kchunk, int *err, bool may_fork) {
   if (b < 5 || b > 8 || b * S > 62) fail(QS_ERR_INTERNAL, "split: unsupported digit plan b=%d S=%d", b, S);
   cudaStream_t st = ctx->stream;
   ctx->mark(0);
+  // the two roles' strips are independent: the B role runs on the
+  // context's second stream beside the A role, so that neither launch's
+  // last partial wave leaves SMs idle; the GEMM waits for both (not on the
+  // allocation-free path, which creates no stream)
+  const bool fork = may_fork && nsa && nsb;
+  cudaStream_t sb = st;
+  if (fork) {
+    ctx->ensure_aux();
+    QS_CUDA(cudaEventRecord(ctx->aux_fork, st));
+    QS_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->aux_fork, 0));
+    sb = ctx->aux;
+  }
   auto strips = [&](auto cx) {
     constexpr bool CX = decltype(cx)::value;
+    if (nsb) {
+      if (d_vb) strip_b_kernel<CX, S, true><<<nsb, STRIP_THREADS, 0, sb>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b);
+      else strip_b_kernel<CX, S, false><<<nsb, STRIP_THREADS, 0, sb>>>(d_pairs, nullptr, d_sb, A, B, dF, arena, b);
+      QS_LAUNCHED(ctx);
+    }
     if (nsa) {
       if (d_va) strip_a_kernel<CX, S, true><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, d_va, d_sa, A, B, dE, arena, b);
       else strip_a_kernel<CX, S, false><<<nsa, STRIP_THREADS, 0, st>>>(d_pairs, nullptr, d_sa, A, B, dE, arena, b);
       QS_LAUNCHED(ctx);
     }
-    if (nsb) {
-      if (d_vb) strip_b_kernel<CX, S, true><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, d_vb, d_sb, A, B, dF, arena, b);
-      else strip_b_kernel<CX, S, false><<<nsb, STRIP_THREADS, 0, st>>>(d_pairs, nullptr, d_sb, A, B, dF, arena, b);
-      QS_LAUNCHED(ctx);
-    }
   };
   if (cplx) strips(std::true_type{});
   else strips(std::false_type{});
+  if (fork) {
+    QS_CUDA(cudaEventRecord(ctx->aux_join, ctx->aux));
+    QS_CUDA(cudaStreamWaitEvent(st, ctx->aux_join, 0));
+  }
   const int nst = pick_stages<S>();
   const size_t sm = smem_bytes<S>(nst);
   QS_CUDA(cudaFuncSetAttribute(gemm_split_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -1454,12 +1470,13 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
 // split product on the context's stream, with every work list, exponent
 // array and the digit arena already on the device.
 static void launch_split(Ctx *ctx, const SplitWork &w, bool cplx, const SplitDev &d, const double *A,
-                         const double *B, double *C, int *err) {
+                         const double *B, double *C, int *err, bool may_fork = true) {
   switch (w.S) {
 #define QS_CASE(SS)                                                                                      \
   case SS:                                                                                               \
     launch_split_s<SS>(ctx, cplx, d.pairs, d.va, d.vb, d.sa, (int)w.sa.size(), d.sb, (int)w.sb.size(),    \
-                       d.tiles, (int)w.tiles.size(), A, B, C, d.E, d.F, d.arena, w.b, w.kchunk, err);    \
+                       d.tiles, (int)w.tiles.size(), A, B, C, d.E, d.F, d.arena, w.b, w.kchunk, err,     \
+                       may_fork);                                                                        \
     break;
     QS_CASE(2)
     QS_CASE(3)
@@ -1552,7 +1569,7 @@ SplitResult run_split_static(Ctx *ctx, const std::vector<PairDesc> &pairs, const
   put(d.sa, w.sa.data(), w.sa.size() * sizeof(int4));
   put(d.sb, w.sb.data(), w.sb.size() * sizeof(int4));
   put(d.tiles, w.tiles.data(), w.tiles.size() * sizeof(SplitTile));
-  launch_split(ctx, w, cplx, d, A, B, C, err);
+  launch_split(ctx, w, cplx, d, A, B, C, err, false);
   // the work lists are copied from pageable host memory, which the GPU may
   // read when the copies execute rather than when they are queued: keep them
   // alive until then

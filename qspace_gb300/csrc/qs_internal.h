@@ -76,6 +76,12 @@ struct Ctx {
   cudaStream_t h2d = nullptr, d2h = nullptr;
   void ensure_copy_streams();
   void destroy_copy_streams();
+  // a second compute stream for independent kernels of one step (forked
+  // from and joined back to `stream` with the two events; created on use,
+  // released with the copy streams)
+  cudaStream_t aux = nullptr;
+  cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
+  void ensure_aux();
   // cuSOLVER handle (created on first use)
   void *solver = nullptr;
   void *solver_lanes = nullptr;  // extra solver streams for concurrent blocks

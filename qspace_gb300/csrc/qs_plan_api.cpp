@@ -134,6 +134,7 @@ void record_graph(qs_grouped_plan *p, const double *A, const double *B, double *
   const int64_t l0 = c->launches;
   c->timing = false;
   cudaGraph_t gr = nullptr;
+  c->ensure_aux();  // the launch forks onto the second stream: created outside the capture
   QS_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   try {
     launch_direct(p, A, B, C);
