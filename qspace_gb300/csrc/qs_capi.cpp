@@ -11,6 +11,7 @@
 #include <numeric>
 
 #include "qs_internal.h"
+#include "qs_grouped.h"
 #include "qs_xcache.h"
 #include "qs_objects.h"
 #include "qs_plan.h"
@@ -366,9 +367,12 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
   // strided views (lines over the kept legs, depth over the contracted legs
   // in pairing order, the order of permute_to's copy) when every block's legs
   // fit a view; the FP64 path reads the permuted copy.
+  // Deep output blocks are cut along their depth (split_deep), which needs
+  // plain operands: such contractions read permuted copies.
+  const bool deep = views && has_deep_blocks(pl.pairs, pl.grp, pl.blk_M, pl.blk_N);
   auto fused = [&](const QMeta &m, bool is_a, std::vector<OperandView> &out) -> bool {
     const OperandLayout &lay = is_a ? pl.la : pl.lb;
-    if (!views || !lay.permute) return false;
+    if (!views || deep || !lay.permute) return false;
     const std::vector<int> &lines = is_a ? pl.ika : pl.ikb;
     const std::vector<int> &ks = is_a ? pl.ica.idx : pl.icb.idx;
     std::vector<OperandView> v(pl.pairs.size());
@@ -469,12 +473,7 @@ static void run_products(Ctx *ctx, const std::vector<Prepared *> &batch, const q
     }
   } else if (prec == QS_PREC_FP64) {
     if (any_view) fail(QS_ERR_INTERNAL, "FP64 products of operands read through views");
-    std::vector<TileDesc> tiles = make_tiles(grp, bM, bN, c_off, gemm_f64_tile_m(), gemm_f64_tile_n());
-    PairDesc *dp = dev_upload(ctx, pairs);
-    TileDesc *dt = dev_upload(ctx, tiles);
-    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), baseA, baseB, baseC, cplx ? 1 : 0);
-    dev_free(ctx, dp);
-    dev_free(ctx, dt);
+    run_f64(ctx, pairs, grp, bM, bN, c_off, nullptr, baseA, baseB, baseC, cplx);
   } else {
     fail(QS_ERR_ARG, "unknown precision mode %d", prec);
   }

@@ -1491,12 +1491,71 @@ static void launch_split(Ctx *ctx, const SplitWork &w, bool cplx, const SplitDev
   }
 }
 
+static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                                   const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                                   const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
+                                   bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
+                                   int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
+                                   const std::vector<OperandView> *vb);
+
+// Deep output blocks (few tiles, a very deep sum) are cut along their depth
+// into parts computed as blocks of their own in a temporary buffer and summed
+// in part order (split_deep); the digit plan is the one of the list as
+// given, so the cut never changes it.  Lists with per-pair factor keys or
+// operand views run as they are.
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                       const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                       const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                       bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
                       int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
                       const std::vector<OperandView> *vb) {
+  DeepSplit ds;
+  const int64_t eb = cplx ? 16 : 8;
+  // blocks with a pair read through a view stay whole
+  std::vector<char> keep;
+  if (va || vb) {
+    keep.assign(blk_M.size(), 0);
+    for (size_t g = 0; g < blk_M.size(); ++g)
+      for (int64_t p = grp[g]; p < grp[g + 1]; ++p)
+        if ((va && (*va)[p].nl > 0) || (vb && (*vb)[p].nl > 0)) keep[g] = 1;
+  }
+  if (!fs && reinterpret_cast<uintptr_t>(C) % eb == 0 &&
+      split_deep(pairs, grp, blk_M, blk_N, c_off, blk_ldc, ds, keep.empty() ? nullptr : &keep)) {
+    const DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cplx ? 2 : 1, tol, forced_slices, forced_bits);
+    double *T = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(ds.temp_elems, 1) * (cplx ? 2 : 1));
+    DeepReduce *d_red = nullptr;
+    // the views follow their pairs (pairs of cut blocks have none)
+    std::vector<OperandView> va2, vb2;
+    for (int32_t q : ds.src) {
+      if (va) va2.push_back((*va)[q]);
+      if (vb) vb2.push_back((*vb)[q]);
+    }
+    try {
+      ds.place((int64_t)(reinterpret_cast<intptr_t>(T) - reinterpret_cast<intptr_t>(C)) / eb);
+      d_red = dev_upload(ctx, ds.red);
+      SplitResult res = run_split_lists(ctx, ds.pairs, ds.grp, ds.bM, ds.bN, ds.coff, A, B, C, cplx, dp.nslices, tol,
+                                        &ds.bldc, dp.bits, nullptr, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
+      launch_reduce_parts(ctx, d_red, (int64_t)ds.red.size(), T, C, cplx);
+      dev_free(ctx, d_red);
+      dev_free(ctx, T);
+      return res;
+    } catch (...) {
+      cudaStreamSynchronize(ctx->stream);
+      if (d_red) dev_free(ctx, d_red);
+      dev_free(ctx, T);
+      throw;
+    }
+  }
+  return run_split_lists(ctx, pairs, grp, blk_M, blk_N, c_off, A, B, C, cplx, forced_slices, tol, blk_ldc,
+                         forced_bits, fs, va, vb);
+}
+
+static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                                   const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
+                                   const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
+                                   bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
+                                   int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
+                                   const std::vector<OperandView> *vb) {
   SplitWork w;
   SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w, forced_bits,
                                va, vb);

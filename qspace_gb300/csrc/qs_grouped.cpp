@@ -94,6 +94,44 @@ GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elem
   return g;
 }
 
+void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+             const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
+             const std::vector<int32_t> *bldc, const double *A, const double *B, double *C, bool cplx,
+             const FactorSource *fs) {
+  DeepSplit ds;
+  const int64_t eb = cplx ? 16 : 8;
+  const bool deep = !fs && reinterpret_cast<uintptr_t>(C) % eb == 0 && split_deep(pairs, grp, bM, bN, coff, bldc, ds);
+  double *T = nullptr;
+  PairDesc *dp = nullptr;
+  TileDesc *dt = nullptr;
+  DeepReduce *dr = nullptr;
+  try {
+    if (deep) {
+      T = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(ds.temp_elems, 1) * (cplx ? 2 : 1));
+      ds.place((int64_t)(reinterpret_cast<intptr_t>(T) - reinterpret_cast<intptr_t>(C)) / eb);
+    }
+    const std::vector<PairDesc> &pp = deep ? ds.pairs : pairs;
+    std::vector<TileDesc> tiles = deep ? make_tiles(ds.grp, ds.bM, ds.bN, ds.coff, gemm_f64_tile_m(),
+                                                    gemm_f64_tile_n(), &ds.bldc)
+                                       : make_tiles(grp, bM, bN, coff, gemm_f64_tile_m(), gemm_f64_tile_n(), bldc);
+    dp = dev_upload(ctx, pp);
+    dt = dev_upload(ctx, tiles);
+    if (fs) launch_resolve_pairdesc(ctx, dp, (int64_t)pp.size(), *fs);
+    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), A, B, C, cplx ? 1 : 0);
+    if (deep) {
+      dr = dev_upload(ctx, ds.red);
+      launch_reduce_parts(ctx, dr, (int64_t)ds.red.size(), T, C, cplx);
+    }
+  } catch (...) {
+    cudaStreamSynchronize(ctx->stream);
+    for (void *p : {(void *)T, (void *)dp, (void *)dt, (void *)dr})
+      if (p) dev_free(ctx, p);
+    throw;
+  }
+  for (void *p : {(void *)T, (void *)dp, (void *)dt, (void *)dr})
+    if (p) dev_free(ctx, p);
+}
+
 // Launches the products of output blocks [b0, b1) of a plan (FP64 or split
 // path).  With `static_scratch` the split path carves its device buffers from
 // that scratch instead of allocating.
@@ -141,13 +179,7 @@ static void grouped_exec(Ctx *ctx, const GroupedPlan &g, size_t b0, size_t b1, c
   } else if (static_scratch) {
     fail(QS_ERR_ARG, "the static-scratch entry point runs the split path only");
   } else if (prec == QS_PREC_FP64) {
-    std::vector<TileDesc> tiles = make_tiles(grp, bM, bN, coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &bldc);
-    PairDesc *dp = dev_upload(ctx, pairs);
-    TileDesc *dt = dev_upload(ctx, tiles);
-    if (fs) launch_resolve_pairdesc(ctx, dp, (int64_t)pairs.size(), *fs);
-    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), A, B, C, g.cplx ? 1 : 0);
-    dev_free(ctx, dp);
-    dev_free(ctx, dt);
+    run_f64(ctx, pairs, grp, bM, bN, coff, &bldc, A, B, C, g.cplx, fs);
   } else {
     fail(QS_ERR_ARG, "unknown precision mode %d", prec);
   }

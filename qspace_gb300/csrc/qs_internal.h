@@ -109,6 +109,46 @@ struct PairDesc {
 };
 static_assert(sizeof(PairDesc) == 48, "PairDesc layout");
 
+// Deep output blocks.  The grouped kernels give each output tile to one CTA
+// for the block's whole summed depth, so a block with few tiles and a very
+// deep sum (a reduced density matrix or an overlap over large bonds) would
+// leave most SMs idle.  Such a block is cut along its depth into parts, each
+// a temporary output block of its own (the pairs' K ranges split where the
+// parts meet), and the parts are summed in a fixed order afterwards.  The
+// decision depends on the block alone, so a block is cut the same way
+// whatever else is in the launch.
+struct DeepReduce {
+  int64_t c_off;   // the block in C (elements)
+  int64_t t_off;   // its first part in the temporary buffer (elements)
+  int32_t M, N, ldc, nparts;  // parts are packed M x N, back to back
+};
+struct DeepSplit {
+  std::vector<PairDesc> pairs;
+  std::vector<int64_t> grp, coff;   // coff of part blocks: temporary-buffer offsets
+  std::vector<int32_t> bM, bN, bldc;
+  std::vector<char> part;           // block is a part (its coff is in the temporary buffer)
+  std::vector<int32_t> src;         // pair of the input list each pair came from
+  std::vector<DeepReduce> red;
+  int64_t temp_elems = 0;
+  // shifts the part blocks' offsets by the temporary buffer's element
+  // offset from C
+  void place(int64_t shift) {
+    for (size_t b = 0; b < coff.size(); ++b)
+      if (part[b]) coff[b] += shift;
+  }
+};
+// Whether any block of the list is deep enough to be cut.
+bool has_deep_blocks(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                     const std::vector<int32_t> &bM, const std::vector<int32_t> &bN);
+// Cuts the deep blocks (except those marked in `keep`); false (and `out`
+// untouched) when there are none.
+bool split_deep(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                const std::vector<int32_t> &bM, const std::vector<int32_t> &bN,
+                const std::vector<int64_t> &coff, const std::vector<int32_t> *bldc, DeepSplit &out,
+                const std::vector<char> *keep = nullptr);
+// C block = sum of its parts in part order (FP64 or complex128 elements).
+void launch_reduce_parts(Ctx *ctx, const DeepReduce *d_red, int64_t nred, const double *T, double *C, bool cplx);
+
 // One output tile of one output block: the pairs [p0, p1) all write block c.
 struct TileDesc {
   int64_t c_off;
