@@ -5,6 +5,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <unordered_map>
 #include <unordered_set>
 #include <mutex>
 #include <new>
@@ -347,6 +348,24 @@ static bool make_view(const QMeta &m, int64_t blk, const std::vector<int> &line_
   return true;
 }
 
+// The offsets sum_i l_i str[i] of the n-leg index space dim (first leg
+// fastest) appended to `tab` (one entry for n = 0).
+static void append_offsets(int n, const int32_t *dim, const int64_t *str, std::vector<int64_t> &tab) {
+  int64_t count = 1;
+  for (int i = 0; i < n; ++i) count *= dim[i];
+  int32_t idx[VIEW_LEGS] = {0, 0, 0, 0};
+  int64_t off = 0;
+  for (int64_t e = 0; e < count; ++e) {
+    tab.push_back(off);
+    for (int i = 0; i < n; ++i) {  // odometer step
+      off += str[i];
+      if (++idx[i] < dim[i]) break;
+      off -= str[i] * dim[i];
+      idx[i] = 0;
+    }
+  }
+}
+
 // Plan on the host, then widen/permute the operands as the plan wants and
 // allocate the output (kernels on ctx->stream).
 static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, const QMeta &Bm,
@@ -370,15 +389,39 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
   // Deep output blocks are cut along their depth (split_deep), which needs
   // plain operands: such contractions read permuted copies.
   const bool deep = views && has_deep_blocks(pl.pairs, pl.grp, pl.blk_M, pl.blk_N);
+  // the views' offset tables, one pair of tables per operand block (every
+  // pair reading the block shares them): all in one upload
+  std::vector<int64_t> vtab;
+  std::vector<std::pair<int64_t, int64_t>> toff_a, toff_b;  // per pair: (line, depth) table starts
   auto fused = [&](const QMeta &m, bool is_a, std::vector<OperandView> &out) -> bool {
     const OperandLayout &lay = is_a ? pl.la : pl.lb;
     if (!views || deep || !lay.permute) return false;
     const std::vector<int> &lines = is_a ? pl.ika : pl.ikb;
     const std::vector<int> &ks = is_a ? pl.ica.idx : pl.icb.idx;
     std::vector<OperandView> v(pl.pairs.size());
-    for (size_t p = 0; p < pl.pairs.size(); ++p)
-      if (!make_view(m, is_a ? pl.pair_ia[p] : pl.pair_ib[p], lines, ks, v[p])) return false;
+    std::vector<std::pair<int64_t, int64_t>> toff(pl.pairs.size());
+    std::unordered_map<int64_t, size_t> first;  // block -> first pair that reads it
+    const size_t tab0 = vtab.size();
+    for (size_t p = 0; p < pl.pairs.size(); ++p) {
+      const int64_t blk = is_a ? pl.pair_ia[p] : pl.pair_ib[p];
+      auto it = first.find(blk);
+      if (it != first.end()) {
+        v[p] = v[it->second];
+        toff[p] = toff[it->second];
+        continue;
+      }
+      if (!make_view(m, blk, lines, ks, v[p])) {
+        vtab.resize(tab0);
+        return false;
+      }
+      toff[p] = {(int64_t)vtab.size(), 0};
+      append_offsets(v[p].nl, v[p].ldim, v[p].lstr, vtab);
+      toff[p].second = (int64_t)vtab.size();
+      append_offsets(v[p].nk, v[p].kdim, v[p].kstr, vtab);
+      first.emplace(blk, p);
+    }
     out.swap(v);
+    (is_a ? toff_a : toff_b).swap(toff);
     // the permuted copy would have been conjugated: conjugate on the fly.
     // XOR, not OR: the conjugation flag may be set as well (the auto-conj
     // rule of contract_getIdxSet, after permute_to flipped the copy's itags),
@@ -388,6 +431,18 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
     return true;
   };
   const bool fa = fused(Am, true, w.va), fb = fused(Bm, false, w.vb);
+  if (!vtab.empty()) {
+    const int64_t *d_tab = dev_upload(ctx, vtab);
+    w.tmp.push_back(const_cast<int64_t *>(d_tab));
+    for (size_t p = 0; p < w.va.size(); ++p) {
+      w.va[p].ltab = d_tab + toff_a[p].first;
+      w.va[p].ktab = d_tab + toff_a[p].second;
+    }
+    for (size_t p = 0; p < w.vb.size(); ++p) {
+      w.vb[p].ltab = d_tab + toff_b[p].first;
+      w.vb[p].ktab = d_tab + toff_b[p].second;
+    }
+  }
   auto prep = [&](const QMeta &m, const double *d, const OperandLayout &lay, bool in_place) -> const double * {
     const double *cur = d;
     if (cplx && !m.cplx) {

@@ -242,42 +242,31 @@ __device__ __forceinline__ void st_pol(uint8_t *a, uint4 v, uint64_t pol) {
 }
 
 // Element (line, k) of a pair's operand in the role being sliced: plain
-// (lda/ldb, trans) addressing, or the operand's strided view when the
-// contraction reads a permuted operand in place.
-__device__ __forceinline__ int64_t view_part(int n, const int32_t *dim, const int64_t *str, int64_t idx) {
-  int64_t o = 0;
-  int32_t x = (int32_t)idx;  // line and depth indices are < 2^31
-#pragma unroll
-  for (int i = 0; i < VIEW_LEGS; ++i) {
-    if (i < n) {
-      const int32_t d = dim[i];
-      o += (int64_t)(x % d) * str[i];
-      x /= d;
-    }
-  }
-  return o;
-}
+// (lda/ldb, trans) addressing, or the offset tables of the operand's strided
+// view when the contraction reads a permuted operand in place.
 struct OpAddr {
   int64_t ls, ks;             // plain: line * ls + k * ks
-  const OperandView *v;       // or the view (nl > 0)
-  __device__ __forceinline__ int64_t line(int64_t m) const {
-    return v ? view_part(v->nl, v->ldim, v->lstr, m) : m * ls;
-  }
-  __device__ __forceinline__ int64_t depth(int64_t k) const {
-    return v ? view_part(v->nk, v->kdim, v->kstr, k) : k * ks;
-  }
+  const int64_t *lt, *kt;     // or the view's tables (nullptr: plain)
+  bool kunit;                 // unit depth stride (neighbouring k adjacent)
+  __device__ __forceinline__ int64_t line(int64_t m) const { return lt ? lt[m] : m * ls; }
+  __device__ __forceinline__ int64_t depth(int64_t k) const { return kt ? kt[k] : k * ks; }
 };
 // A role: lines are rows of op(A) (contiguous along k when transposed); B
 // role: lines are columns of op(B) (contiguous along k when not transposed).
+__device__ __forceinline__ OpAddr view_addr(const OperandView *views, int p, int64_t ls, int64_t ks) {
+  if (views && views[p].nl > 0) {
+    const OperandView &v = views[p];
+    return OpAddr{0, 0, v.ltab, v.ktab, v.nk > 0 && v.kstr[0] == 1};
+  }
+  return OpAddr{ls, ks, nullptr, nullptr, ks == 1};
+}
 __device__ __forceinline__ OpAddr addr_a(const SplitPair &P, const OperandView *views, int p) {
   const bool ta = P.trans & 1;
-  const OperandView *v = (views && views[p].nl > 0) ? views + p : nullptr;
-  return OpAddr{ta ? (int64_t)P.lda : 1, ta ? 1 : (int64_t)P.lda, v};
+  return view_addr(views, p, ta ? (int64_t)P.lda : 1, ta ? 1 : (int64_t)P.lda);
 }
 __device__ __forceinline__ OpAddr addr_b(const SplitPair &P, const OperandView *views, int p) {
   const bool tb = P.trans & 2;
-  const OperandView *v = (views && views[p].nl > 0) ? views + p : nullptr;
-  return OpAddr{tb ? 1 : (int64_t)P.ldb, tb ? (int64_t)P.ldb : 1, v};
+  return view_addr(views, p, tb ? 1 : (int64_t)P.ldb, tb ? (int64_t)P.ldb : 1);
 }
 
 // ---------------------------------------------- exponents and slicing, fused
@@ -319,7 +308,7 @@ __device__ __forceinline__ void strip_maxima(const SplitPair *__restrict__ pairs
     const OpAddr ad = ROLE_B ? addr_b(P, views, p) : addr_a(P, views, p);
     // lines contiguous along k (unit depth stride): neighbouring lanes take
     // neighbouring k of one line; else neighbouring lines
-    const bool contig = ad.v ? (ad.v->nk > 0 && ad.v->kstr[0] == 1) : ad.ks == 1;
+    const bool contig = ad.kunit;
     constexpr int NPH = STRIP_THREADS / STRIP;
     const int line = contig ? threadIdx.x / NPH : threadIdx.x % STRIP;
     const int ph = contig ? threadIdx.x % NPH : threadIdx.x / STRIP;

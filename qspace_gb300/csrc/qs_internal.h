@@ -178,11 +178,15 @@ struct PermDesc {
 // GEMM reads it -- line = row of op(A) / column of op(B), k = depth -- sits at
 // block offset  sum_i l_i lstr[i] + sum_t k_t kstr[t],  line = sum_i l_i
 // prod_{i'<i} ldim[i'] (first leg fastest), likewise k.  nl = 0: no view.
+// The kernels read the offsets from tables built on the host once per
+// operand block: ltab[line] = sum_i l_i lstr[i], ktab[k] likewise (device
+// pointers; the host fills them in after the tables are uploaded).
 constexpr int VIEW_LEGS = 4;
 struct OperandView {
   int32_t nl, nk;
   int32_t ldim[VIEW_LEGS], kdim[VIEW_LEGS];
   int64_t lstr[VIEW_LEGS], kstr[VIEW_LEGS];
+  const int64_t *ltab, *ktab;
 };
 
 // One 32 x 32 tile of a tiled block: tile (ti, tj) of (output leg 0,
