@@ -350,8 +350,11 @@ QS_EXPORT qs_status qs_xcache_get(qs_xcache *cache, int64_t n, const uint64_t *k
 QS_EXPORT qs_status qs_xcache_count(const qs_xcache *cache, int64_t *n);
 /* qs_grouped_gemm with the factor of pair p looked up under the key
  * fkeys[2p], fkeys[2p+1] (host array); pairs->afac is ignored and may be
- * NULL.  The call waits for its products.  A key missing from the table
- * fails it with QS_ERR_ARG; the products of that pair then used factor 0. */
+ * NULL.  The keys are looked up on the device, the factors come back (8
+ * bytes per pair) and the product runs as qs_grouped_gemm with them, so it
+ * gives the same bits as the listed-factor call.  The call waits for its
+ * products.  A key missing from the table fails it with QS_ERR_ARG; the
+ * products of that pair then used factor 0. */
 QS_EXPORT qs_status qs_grouped_gemm_keyed(qs_ctx *ctx, const qs_pair_list *pairs, const uint64_t *fkeys,
                                           const qs_xcache *cache, const double *A, const double *B,
                                           double *C, const qs_opts *opts, qs_stats *stats);

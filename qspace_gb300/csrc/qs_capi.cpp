@@ -388,7 +388,16 @@ static void prepare(Ctx *ctx, Prepared &w, const QMeta &Am, const double *dA, co
   // fit a view; the FP64 path reads the permuted copy.
   // Deep output blocks are cut along their depth (split_deep), which needs
   // plain operands: such contractions read permuted copies.
-  const bool deep = views && has_deep_blocks(pl.pairs, pl.grp, pl.blk_M, pl.blk_N);
+  bool deep = views && has_deep_blocks(pl.pairs, pl.grp, pl.blk_M, pl.blk_N);
+  // likewise contractions whose blocks are all shallow (computed directly
+  // from plain operands)
+  if (views && !deep) {
+    bool all_shallow = true;
+    for (size_t b = 0; b + 1 < pl.grp.size() && all_shallow; ++b)
+      all_shallow = is_shallow(pl.pairs, pl.grp[b], pl.grp[b + 1]) &&
+                    shallow_direct_wins(pl.pairs, pl.grp[b], pl.grp[b + 1], pl.blk_M[b], pl.blk_N[b], w.cplx);
+    deep = all_shallow;
+  }
   // the views' offset tables, one pair of tables per operand block (every
   // pair reading the block shares them): all in one upload
   std::vector<int64_t> vtab;

@@ -11,6 +11,7 @@
 // by one kernel in a fixed order, so the result does not depend on how the
 // work was scheduled.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <vector>
 
@@ -47,7 +48,170 @@ __global__ void reduce_parts_kernel(const DeepReduce *__restrict__ red, const do
   }
 }
 
+// One thread per output element of a shallow block: C(i, j) = sum over the
+// block's pairs, in order, of afac sum_k op(A)(i, k) op(B)(k, j).
+struct ShallowTask {
+  int64_t c_off;
+  int32_t p0, p1, M, N, ldc, pad_;
+  int64_t e0, e1;   // elements of this task (column-major over M x N)
+};
+
+template <bool CPLX>
+__global__ void shallow_kernel(const ShallowTask *__restrict__ tasks, const PairDesc *__restrict__ pairs,
+                               const double *__restrict__ A, const double *__restrict__ B, double *__restrict__ C) {
+  const ShallowTask t = tasks[blockIdx.x];
+  for (int64_t e = t.e0 + threadIdx.x; e < t.e1; e += blockDim.x) {
+    const int64_t i = e % t.M, j = e / t.M;
+    double re = 0.0, im = 0.0;
+    for (int p = t.p0; p < t.p1; ++p) {
+      const PairDesc P = pairs[p];
+      const bool ta = P.trans & 1, tb = P.trans & 2, ca = P.trans & 4, cb = P.trans & 8;
+      double sr = 0.0, si = 0.0;
+      for (int k = 0; k < P.K; ++k) {
+        const int64_t ia = P.a_off + (ta ? k + i * (int64_t)P.lda : i + k * (int64_t)P.lda);
+        const int64_t ib = P.b_off + (tb ? j + k * (int64_t)P.ldb : k + j * (int64_t)P.ldb);
+        if (CPLX) {
+          const double ar = A[2 * ia], ai = ca ? -A[2 * ia + 1] : A[2 * ia + 1];
+          const double br = B[2 * ib], bi = cb ? -B[2 * ib + 1] : B[2 * ib + 1];
+          sr += ar * br - ai * bi;
+          si += ar * bi + ai * br;
+        } else {
+          sr += A[ia] * B[ib];
+        }
+      }
+      re += P.afac * sr;
+      im += P.afac * si;
+    }
+    const int64_t o = t.c_off + i + j * (int64_t)t.ldc;
+    if (CPLX) {
+      C[2 * o] = re;
+      C[2 * o + 1] = im;
+    } else {
+      C[o] = re;
+    }
+  }
+}
+
 }  // namespace
+
+bool is_shallow(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1) {
+  int64_t depth = 0;
+  for (int64_t p = p0; p < p1; ++p) depth += std::max<int32_t>(pairs[p].K, 0);
+  return depth <= SHALLOW_K;
+}
+
+bool shallow_direct_wins(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1, int32_t M, int32_t N,
+                         bool cplx) {
+  int64_t depth = 0;
+  for (int64_t p = p0; p < p1; ++p) depth += std::max<int32_t>(pairs[p].K, 0);
+  const double m = M, n = N, cm = cplx ? 2.0 : 1.0;
+  // direct: FP64 multiply-adds at ~1 TFLOP/s and the output written once
+  const double direct = (cplx ? 8.0 : 2.0) * m * n * (double)depth / 1.0e12 + 8.0 * cm * m * n / 5.0e12;
+  // tiled: 128 x 32 tiles of the real form, either orientation, ~3000 cycles
+  // each (one k-block and the epilogue) spread over 152 SMs at 2 GHz
+  auto tiles = [](double r, double c) { return std::ceil(r / 128.0) * std::ceil(c / 32.0); };
+  const double t = std::min(tiles(cm * m, n), tiles(cm * n, m));
+  const double tiled = t * 3000.0 / (152.0 * 2.0e9);
+  return direct < tiled;
+}
+
+static std::vector<ShallowTask> shallow_tasks(const std::vector<int64_t> &grp, const std::vector<int32_t> &bM,
+                                              const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
+                                              const std::vector<int32_t> *bldc, const std::vector<int64_t> &blocks) {
+  constexpr int64_t CHUNK = 8192;  // elements per CTA
+  std::vector<ShallowTask> tasks;
+  for (int64_t b : blocks) {
+    const int64_t n = (int64_t)bM[b] * bN[b];
+    for (int64_t e0 = 0; e0 < n; e0 += CHUNK) {
+      ShallowTask t{};
+      t.c_off = coff[b];
+      t.p0 = (int32_t)grp[b];
+      t.p1 = (int32_t)grp[b + 1];
+      t.M = bM[b];
+      t.N = bN[b];
+      t.ldc = bldc ? (*bldc)[b] : std::max(bM[b], 1);
+      t.e0 = e0;
+      t.e1 = std::min(n, e0 + CHUNK);
+      tasks.push_back(t);
+    }
+  }
+  if (tasks.size() > 0x7fffffff) fail(QS_ERR_SHAPE, "shallow products: too many tasks");
+  return tasks;
+}
+
+void run_shallow(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                 const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
+                 const std::vector<int32_t> *bldc, const std::vector<int64_t> &blocks, const double *A,
+                 const double *B, double *C, bool cplx) {
+  const std::vector<ShallowTask> tasks = shallow_tasks(grp, bM, bN, coff, bldc, blocks);
+  if (tasks.empty()) return;
+  ShallowTask *dt = dev_upload(ctx, tasks);
+  PairDesc *dp = dev_upload(ctx, pairs);
+  if (cplx) shallow_kernel<true><<<(unsigned)tasks.size(), 256, 0, ctx->stream>>>(dt, dp, A, B, C);
+  else shallow_kernel<false><<<(unsigned)tasks.size(), 256, 0, ctx->stream>>>(dt, dp, A, B, C);
+  QS_LAUNCHED(ctx);
+  dev_free(ctx, dt);
+  dev_free(ctx, dp);
+}
+
+ShallowPlan shallow_prepare(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                            const std::vector<int32_t> &bM, const std::vector<int32_t> &bN,
+                            const std::vector<int64_t> &coff, const std::vector<int32_t> *bldc,
+                            const std::vector<int64_t> &blocks, bool cplx) {
+  const std::vector<ShallowTask> tasks = shallow_tasks(grp, bM, bN, coff, bldc, blocks);
+  ShallowPlan sp;
+  sp.cplx = cplx;
+  sp.ntasks = (int64_t)tasks.size();
+  if (tasks.empty()) return sp;
+  try {
+    QS_CUDA(cudaMalloc(&sp.tasks, tasks.size() * sizeof(ShallowTask)));
+    QS_CUDA(cudaMemcpy(sp.tasks, tasks.data(), tasks.size() * sizeof(ShallowTask), cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMalloc(&sp.pairs, std::max<size_t>(pairs.size(), 1) * sizeof(PairDesc)));
+    if (!pairs.empty())
+      QS_CUDA(cudaMemcpy(sp.pairs, pairs.data(), pairs.size() * sizeof(PairDesc), cudaMemcpyHostToDevice));
+  } catch (...) {
+    shallow_release(sp);
+    throw;
+  }
+  return sp;
+}
+
+void shallow_launch(Ctx *ctx, const ShallowPlan &sp, const double *A, const double *B, double *C) {
+  if (!sp.ntasks) return;
+  const ShallowTask *dt = static_cast<const ShallowTask *>(sp.tasks);
+  const PairDesc *dp = static_cast<const PairDesc *>(sp.pairs);
+  if (sp.cplx) shallow_kernel<true><<<(unsigned)sp.ntasks, 256, 0, ctx->stream>>>(dt, dp, A, B, C);
+  else shallow_kernel<false><<<(unsigned)sp.ntasks, 256, 0, ctx->stream>>>(dt, dp, A, B, C);
+  QS_LAUNCHED(ctx);
+}
+
+void shallow_release(ShallowPlan &sp) {
+  if (sp.tasks) cudaFree(sp.tasks);
+  if (sp.pairs) cudaFree(sp.pairs);
+  sp.tasks = sp.pairs = nullptr;
+  sp.ntasks = 0;
+}
+
+BlockList select_blocks(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                        const std::vector<int32_t> &bM, const std::vector<int32_t> &bN,
+                        const std::vector<int64_t> &coff, const std::vector<int32_t> *bldc,
+                        const std::vector<char> &sel) {
+  BlockList L;
+  L.grp.push_back(0);
+  for (size_t b = 0; b < bM.size(); ++b) {
+    if (!sel[b]) continue;
+    for (int64_t p = grp[b]; p < grp[b + 1]; ++p) {
+      L.pairs.push_back(pairs[p]);
+      L.src.push_back((int32_t)p);
+    }
+    L.grp.push_back((int64_t)L.pairs.size());
+    L.bM.push_back(bM[b]);
+    L.bN.push_back(bN[b]);
+    L.bldc.push_back(bldc ? (*bldc)[b] : std::max(bM[b], 1));
+    L.coff.push_back(coff[b]);
+  }
+  return L;
+}
 
 bool has_deep_blocks(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                      const std::vector<int32_t> &bM, const std::vector<int32_t> &bN) {

@@ -1487,27 +1487,59 @@ static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs,
                                    int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
                                    const std::vector<OperandView> *vb);
 
-// Deep output blocks (few tiles, a very deep sum) are cut along their depth
-// into parts computed as blocks of their own in a temporary buffer and summed
-// in part order (split_deep); the digit plan is the one of the list as
-// given, so the cut never changes it.  Lists with per-pair factor keys or
-// operand views run as they are.
+// Shallow output blocks (summed depth <= SHALLOW_K) are computed directly in
+// FP64 (run_shallow); deep ones (few tiles, a very deep sum) are cut along
+// their depth into parts computed as blocks of their own in a temporary
+// buffer and summed in part order (split_deep).  Both decisions depend on the
+// block alone, and the digit plan is the one of the list as given, so a
+// block gives the same bits whatever else is in the launch.  Blocks with a
+// pair read through a view, and lists with per-pair factor keys, run as
+// they are.
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                       const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                       const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                       bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
                       int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
                       const std::vector<OperandView> *vb) {
-  DeepSplit ds;
+  const size_t nb = blk_M.size();
   const int64_t eb = cplx ? 16 : 8;
-  // blocks with a pair read through a view stay whole
+  // blocks with a pair read through a view stay as they are
   std::vector<char> keep;
   if (va || vb) {
-    keep.assign(blk_M.size(), 0);
-    for (size_t g = 0; g < blk_M.size(); ++g)
+    keep.assign(nb, 0);
+    for (size_t g = 0; g < nb; ++g)
       for (int64_t p = grp[g]; p < grp[g + 1]; ++p)
         if ((va && (*va)[p].nl > 0) || (vb && (*vb)[p].nl > 0)) keep[g] = 1;
   }
+  std::vector<char> shallow(nb, 0), rest(nb, 1);
+  std::vector<int64_t> shallow_ids;
+  if (!fs)
+    for (size_t g = 0; g < nb; ++g)
+      if (!(keep.size() && keep[g]) && is_shallow(pairs, grp[g], grp[g + 1]) &&
+          shallow_direct_wins(pairs, grp[g], grp[g + 1], blk_M[g], blk_N[g], cplx)) {
+        shallow[g] = 1;
+        rest[g] = 0;
+        shallow_ids.push_back((int64_t)g);
+      }
+  if (!shallow_ids.empty()) {
+    const DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cplx ? 2 : 1, tol, forced_slices, forced_bits);
+    run_shallow(ctx, pairs, grp, blk_M, blk_N, c_off, blk_ldc, shallow_ids, A, B, C, cplx);
+    SplitResult res;
+    res.nslices = dp.nslices;
+    res.bits = dp.bits;
+    res.err_bound = dp.err_bound;
+    if (shallow_ids.size() == nb) return res;
+    const BlockList R = select_blocks(pairs, grp, blk_M, blk_N, c_off, blk_ldc, rest);
+    std::vector<OperandView> va2, vb2;
+    for (int32_t q : R.src) {
+      if (va) va2.push_back((*va)[q]);
+      if (vb) vb2.push_back((*vb)[q]);
+    }
+    SplitResult r2 = run_split(ctx, R.pairs, R.grp, R.bM, R.bN, R.coff, A, B, C, cplx, dp.nslices, tol, &R.bldc,
+                               dp.bits, nullptr, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
+    return r2.nslices ? r2 : res;
+  }
+  DeepSplit ds;
   if (!fs && reinterpret_cast<uintptr_t>(C) % eb == 0 &&
       split_deep(pairs, grp, blk_M, blk_N, c_off, blk_ldc, ds, keep.empty() ? nullptr : &keep)) {
     const DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cplx ? 2 : 1, tol, forced_slices, forced_bits);

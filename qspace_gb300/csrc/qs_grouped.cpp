@@ -98,6 +98,23 @@ void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int
              const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
              const std::vector<int32_t> *bldc, const double *A, const double *B, double *C, bool cplx,
              const FactorSource *fs) {
+  // shallow blocks directly (run_shallow), the rest through the tiles
+  if (!fs) {
+    std::vector<char> rest(bM.size(), 1);
+    std::vector<int64_t> ids;
+    for (size_t b = 0; b < bM.size(); ++b)
+      if (is_shallow(pairs, grp[b], grp[b + 1])) {
+        rest[b] = 0;
+        ids.push_back((int64_t)b);
+      }
+    if (!ids.empty()) {
+      run_shallow(ctx, pairs, grp, bM, bN, coff, bldc, ids, A, B, C, cplx);
+      if (ids.size() == bM.size()) return;
+      const BlockList R = select_blocks(pairs, grp, bM, bN, coff, bldc, rest);
+      run_f64(ctx, R.pairs, R.grp, R.bM, R.bN, R.coff, &R.bldc, A, B, C, cplx, nullptr);
+      return;
+    }
+  }
   DeepSplit ds;
   const int64_t eb = cplx ? 16 : 8;
   const bool deep = !fs && reinterpret_cast<uintptr_t>(C) % eb == 0 && split_deep(pairs, grp, bM, bN, coff, bldc, ds);

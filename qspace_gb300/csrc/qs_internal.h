@@ -149,6 +149,51 @@ bool split_deep(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &
 // C block = sum of its parts in part order (FP64 or complex128 elements).
 void launch_reduce_parts(Ctx *ctx, const DeepReduce *d_red, int64_t nred, const double *T, double *C, bool cplx);
 
+// Shallow output blocks: a summed depth of at most SHALLOW_K (applying a
+// site operator over a leg of dimension 1 or 2, an outer product).  Tiled
+// products would pad the depth to a full k-block and pay the epilogue per
+// tile; these blocks are computed directly, one thread per output element,
+// in FP64 (exact products, summed in pair and k order).
+constexpr int64_t SHALLOW_K = 8;
+bool is_shallow(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1);
+// Whether the direct FP64 computation of a shallow block is estimated to be
+// faster than the tiled split-precision one: FP64 rate against the tiles'
+// padding (a block with one short side, e.g. M = 1, fills 1 of 32 or 128
+// lines of every tile).  Used by the split path; the FP64 path computes every
+// shallow block directly.
+bool shallow_direct_wins(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1, int32_t M, int32_t N,
+                         bool cplx);
+// Runs the listed blocks (indices into grp / bM / ...) directly.
+void run_shallow(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                 const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
+                 const std::vector<int32_t> *bldc, const std::vector<int64_t> &blocks, const double *A,
+                 const double *B, double *C, bool cplx);
+// The same with the work list prepared once on device memory owned by the
+// caller (reusable plans): prepare, launch any number of times, release.
+struct ShallowPlan {
+  void *tasks = nullptr, *pairs = nullptr;
+  int64_t ntasks = 0;
+  bool cplx = false;
+};
+ShallowPlan shallow_prepare(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                            const std::vector<int32_t> &bM, const std::vector<int32_t> &bN,
+                            const std::vector<int64_t> &coff, const std::vector<int32_t> *bldc,
+                            const std::vector<int64_t> &blocks, bool cplx);
+void shallow_launch(Ctx *ctx, const ShallowPlan &sp, const double *A, const double *B, double *C);
+void shallow_release(ShallowPlan &sp);
+// The blocks of a list with sel[b] set, as a list of their own (with the
+// pairs' index in the input list in `src`).
+struct BlockList {
+  std::vector<PairDesc> pairs;
+  std::vector<int64_t> grp, coff;
+  std::vector<int32_t> bM, bN, bldc;
+  std::vector<int32_t> src;
+};
+BlockList select_blocks(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+                        const std::vector<int32_t> &bM, const std::vector<int32_t> &bN,
+                        const std::vector<int64_t> &coff, const std::vector<int32_t> *bldc,
+                        const std::vector<char> &sel);
+
 // One output tile of one output block: the pairs [p0, p1) all write block c.
 struct TileDesc {
   int64_t c_off;

@@ -58,6 +58,10 @@ struct qs_grouped_plan {
   PairDesc *d_pairs = nullptr;  // FP64 path
   TileDesc *d_tiles = nullptr;
   int64_t ntiles = 0;
+  // shallow output blocks run directly (as in the one-shot calls); `main`
+  // holds the other blocks (all of them when none is shallow)
+  ShallowPlan shallow;
+  GroupedPlan main;
   cudaGraphExec_t exec = nullptr;
   const double *gA = nullptr, *gB = nullptr;
   double *gC = nullptr;
@@ -67,6 +71,8 @@ struct qs_grouped_plan {
 namespace {
 
 void launch_direct(qs_grouped_plan *p, const double *A, const double *B, double *C) {
+  shallow_launch(p->ctx, p->shallow, A, B, C);
+  if (p->main.pairs.empty()) return;
   if (p->o.prec == QS_PREC_SPLIT)
     split_plan_launch(p->ctx, p->split, A, B, C);
   else
@@ -74,8 +80,45 @@ void launch_direct(qs_grouped_plan *p, const double *A, const double *B, double 
 }
 
 SplitPlanHandle *make_split(qs_grouped_plan *p, int bits, SplitResult *r) {
+  const GroupedPlan &g = p->main;
+  int ns = p->o.nslices;
+  if (!bits && p->shallow.ntasks) {
+    // the digit plan of the whole list, as the one-shot call takes it
+    const DigitPlan dp = choose_digits_for(p->g.pairs, p->g.grp, p->g.bM, p->g.bN, p->g.cplx ? 2 : 1, p->o.tol,
+                                           p->o.nslices, 0);
+    bits = dp.bits;
+    ns = dp.nslices;
+  }
+  return split_plan_create(g.pairs, g.grp, g.bM, g.bN, g.coff, g.bldc, g.cplx, ns, p->o.tol, bits, r);
+}
+
+// Splits the plan's blocks into shallow ones (prepared for the direct
+// kernel) and the others (`main`), with the one-shot calls' rule.
+void split_shallow(qs_grouped_plan *p) {
   const GroupedPlan &g = p->g;
-  return split_plan_create(g.pairs, g.grp, g.bM, g.bN, g.coff, g.bldc, g.cplx, p->o.nslices, p->o.tol, bits, r);
+  std::vector<char> rest(g.bM.size(), 1);
+  std::vector<int64_t> ids;
+  const bool split = p->o.prec == QS_PREC_SPLIT;
+  for (size_t b = 0; b < g.bM.size(); ++b)
+    if (is_shallow(g.pairs, g.grp[b], g.grp[b + 1]) &&
+        (!split || shallow_direct_wins(g.pairs, g.grp[b], g.grp[b + 1], g.bM[b], g.bN[b], g.cplx))) {
+      rest[b] = 0;
+      ids.push_back((int64_t)b);
+    }
+  if (ids.empty()) {
+    p->main = g;
+    return;
+  }
+  p->shallow = shallow_prepare(g.pairs, g.grp, g.bM, g.bN, g.coff, &g.bldc, ids, g.cplx);
+  BlockList R = select_blocks(g.pairs, g.grp, g.bM, g.bN, g.coff, &g.bldc, rest);
+  GroupedPlan &m = p->main;
+  m.cplx = g.cplx;
+  m.pairs = std::move(R.pairs);
+  m.grp = std::move(R.grp);
+  m.bM = std::move(R.bM);
+  m.bN = std::move(R.bN);
+  m.bldc = std::move(R.bldc);
+  m.coff = std::move(R.coff);
 }
 
 // Times every feasible digit width on the caller's operands (one warm-up and
@@ -188,6 +231,7 @@ qs_status qs_grouped_plan_create(qs_ctx *ctx, const qs_pair_list *pairs, const q
   p->o = opts ? *opts : qs_opts{QS_PREC_FP64, 0, 1e-12, 0};
   if (!(p->o.tol > 0)) p->o.tol = 1e-12;
   p->g = grouped_plan(pairs, -1, -1, -1);
+  if (p->o.prec == QS_PREC_SPLIT || p->o.prec == QS_PREC_FP64) split_shallow(p.get());
   if (p->o.prec == QS_PREC_SPLIT) {
     p->sig = signature(p->g, p->o);
     int bits = 0;
@@ -195,18 +239,26 @@ qs_status qs_grouped_plan_create(qs_ctx *ctx, const qs_pair_list *pairs, const q
       std::lock_guard<std::mutex> lk(g_tune_mu);
       auto it = g_tuned.find(p->sig);
       if (it == g_tuned.end())
-        p->tune_pending = true;
+        p->tune_pending = !p->main.pairs.empty();
       else
         bits = it->second;
     }
-    if (!p->tune_pending && !p->g.pairs.empty()) p->split = make_split(p.get(), bits, &p->sr);
+    if (!p->tune_pending && !p->main.pairs.empty()) p->split = make_split(p.get(), bits, &p->sr);
+    if (p->main.pairs.empty()) {  // every block shallow: the digit plan is reported only
+      const DigitPlan dp = choose_digits_for(p->g.pairs, p->g.grp, p->g.bM, p->g.bN, p->g.cplx ? 2 : 1, p->o.tol,
+                                             p->o.nslices, 0);
+      p->sr.nslices = dp.nslices;
+      p->sr.bits = dp.bits;
+      p->sr.err_bound = dp.err_bound;
+    }
   } else if (p->o.prec == QS_PREC_FP64) {
-    if (!p->g.pairs.empty()) {
+    if (!p->main.pairs.empty()) {
+      const GroupedPlan &m = p->main;
       std::vector<TileDesc> tiles =
-          make_tiles(p->g.grp, p->g.bM, p->g.bN, p->g.coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &p->g.bldc);
+          make_tiles(m.grp, m.bM, m.bN, m.coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &m.bldc);
       p->ntiles = (int64_t)tiles.size();
-      QS_CUDA(cudaMalloc(&p->d_pairs, p->g.pairs.size() * sizeof(PairDesc)));
-      QS_CUDA(cudaMemcpy(p->d_pairs, p->g.pairs.data(), p->g.pairs.size() * sizeof(PairDesc),
+      QS_CUDA(cudaMalloc(&p->d_pairs, m.pairs.size() * sizeof(PairDesc)));
+      QS_CUDA(cudaMemcpy(p->d_pairs, m.pairs.data(), m.pairs.size() * sizeof(PairDesc),
                          cudaMemcpyHostToDevice));
       QS_CUDA(cudaMalloc(&p->d_tiles, std::max<size_t>(tiles.size(), 1) * sizeof(TileDesc)));
       if (!tiles.empty())
@@ -263,6 +315,7 @@ void qs_grouped_plan_destroy(qs_grouped_plan *p) {
   }
   if (p->exec) cudaGraphExecDestroy(p->exec);
   split_plan_destroy(p->split);
+  shallow_release(p->shallow);
   if (p->d_pairs) cudaFree(p->d_pairs);
   if (p->d_tiles) cudaFree(p->d_tiles);
   delete p;

@@ -4,8 +4,9 @@
 //
 // Inserts happen on the host (a mirror of the table, then one upload): they
 // belong to warm-up, like the reference's first contractCGR call per key.
-// Lookups run on the device only, so repeated contractions carry keys and no
-// factor values.
+// Lookups run on the device: repeated contractions carry keys, and the
+// looked-up factors (8 bytes per pair) come back to run the listed-factor
+// product, so keyed and listed products are the same computation.
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -209,25 +210,39 @@ qs_status qs_grouped_gemm_keyed(qs_ctx *ctx, const qs_pair_list *pairs, const ui
     ones.assign((size_t)std::max<int64_t>(n, 1), 1.0);
     pl.afac = ones.data();
   }
+  // The factors are looked up on the device and come back to the host (8
+  // bytes per pair); the product then runs with them as listed factors, so a
+  // keyed product is the same computation as the listed one, whatever route
+  // its blocks take (shallow, deep, tiled).
   std::vector<uint64_t> k(fkeys, fkeys + 2 * n);
-  uint64_t *dk = dev_upload(c, k);
-  int *dmiss = dev_alloc<int>(c, 1);
-  int miss = 0;
-  try {
-    QS_CUDA(cudaMemsetAsync(dmiss, 0, sizeof(int), c->stream));
-    FactorSource fs{dk, view_of(cache), dmiss};
-    grouped_run(c, &pl, A, B, C, opts, stats, -1, -1, -1, nullptr, 0, nullptr, &fs);
-    QS_CUDA(cudaMemcpyAsync(&miss, dmiss, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    QS_CUDA(cudaStreamSynchronize(c->stream));
-  } catch (...) {
-    cudaStreamSynchronize(c->stream);
+  std::vector<double> vals((size_t)std::max<int64_t>(n, 1), 0.0);
+  std::vector<int32_t> found((size_t)std::max<int64_t>(n, 1), 1);
+  if (n) {
+    uint64_t *dk = dev_upload(c, k);
+    double *dv = dev_alloc<double>(c, (size_t)n);
+    int32_t *df = dev_alloc<int32_t>(c, (size_t)n);
+    try {
+      const int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
+      xcache_get_kernel<<<grid, 256, 0, c->stream>>>(view_of(cache), dk, n, dv, df);
+      QS_LAUNCHED(c);
+      QS_CUDA(cudaMemcpyAsync(vals.data(), dv, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+      QS_CUDA(cudaMemcpyAsync(found.data(), df, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+      QS_CUDA(cudaStreamSynchronize(c->stream));
+    } catch (...) {
+      cudaStreamSynchronize(c->stream);
+      dev_free(c, dk);
+      dev_free(c, dv);
+      dev_free(c, df);
+      throw;
+    }
     dev_free(c, dk);
-    dev_free(c, dmiss);
-    throw;
+    dev_free(c, dv);
+    dev_free(c, df);
   }
-  dev_free(c, dk);
-  dev_free(c, dmiss);
-  if (miss) fail(QS_ERR_ARG, "a pair's factor key is not in the table (its products used factor 0)");
+  pl.afac = vals.data();
+  grouped_run(c, &pl, A, B, C, opts, stats, -1, -1, -1);
+  for (int64_t i = 0; i < n; ++i)
+    if (!found[i]) fail(QS_ERR_ARG, "a pair's factor key is not in the table (its products used factor 0)");
   QS_API_END
 }
 

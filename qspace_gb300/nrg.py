@@ -80,8 +80,39 @@ def initial_space(backend, eps: float = 0.0, U: float = 0.0) -> KeptSpace:
     return KeptSpace(1, E, {s: backend.put(c) for s, c in ops.items()}, nkept=4, ntotal=4)
 
 
+class Packed:
+    """A QSpace in packed form: labels q (nblk, rank, 2), dims (nblk, rank)
+    and the blocks column-major back to back in buf -- built with whole-array
+    numpy operations (the product basis of a large kept space has thousands
+    of blocks) and uploaded in one piece where the backend can."""
+
+    def __init__(self, q, dims, buf):
+        self.q, self.dims, self.buf = q, dims, buf
+
+    def qspace(self) -> QSpace:
+        n, r = self.dims.shape
+        sizes = np.prod(self.dims, axis=1)
+        parts = np.split(self.buf, np.cumsum(sizes)[:-1]) if n else []
+        data = [x.reshape(tuple(self.dims[i]), order="F") for i, x in enumerate(parts)]
+        return QSpace([np.ascontiguousarray(self.q[:, k, :]) for k in range(r)], data, {})
+
+
+def _put(backend, P: Packed):
+    put_packed = getattr(backend, "put_packed", None)
+    return put_packed(P) if put_packed else backend.put(P.qspace())
+
+
+def _scatter_ones(nblk_rows, first, cols0, rows, offs):
+    """Linear indices of entries (i, off + i) of column-major blocks with
+    `rows` rows: block b contributes nblk_rows[b] entries, its block starts
+    at offs[b] and its diagonal at column cols0[b]."""
+    blk = np.repeat(np.arange(len(nblk_rows)), nblk_rows)
+    i = np.arange(int(np.sum(nblk_rows))) - np.repeat(first, nblk_rows)
+    return offs[blk] + i + (cols0[blk] + i) * rows[blk]
+
+
 def _fusion(K: KeptSpace):
-    """A4 and A4Z = Z_K A4 (host QSpaces), and the combined sectors."""
+    """A4 and A4Z = Z_K A4 (packed), and the combined sectors."""
     sectors = sorted(K.E)
     off, D = {}, {}
     for s in SITE_LABELS:
@@ -89,33 +120,45 @@ def _fusion(K: KeptSpace):
             qn = (qk[0] + s[0], qk[1] + s[1])
             off[(qk, s)] = D.get(qn, 0)
             D[qn] = D.get(qn, 0) + len(K.E[qk])
-    Q = [[], [], []]
-    data, dataz = [], []
+    lab, d, dn, o, sign = [], [], [], [], []
     for s in SITE_LABELS:
         for qk in sectors:
             qn = (qk[0] + s[0], qk[1] + s[1])
-            d = len(K.E[qk])
-            blk = np.zeros((d, 1, D[qn]))
-            blk[:, 0, off[(qk, s)]:off[(qk, s)] + d] = np.eye(d)
-            Q[0].append(qk)
-            Q[1].append(s)
-            Q[2].append(qn)
-            data.append(blk)
-            dataz.append(parity(qk, K.nsites) * blk)
-    Qa = [np.array(x, np.int32) for x in Q]
-    return QSpace(Qa, data, {}), QSpace([q.copy() for q in Qa], dataz, {}), D, off
+            lab.append((qk, s, qn))
+            d.append(len(K.E[qk]))
+            dn.append(D[qn])
+            o.append(off[(qk, s)])
+            sign.append(parity(qk, K.nsites))
+    d, dn, o = (np.array(x, np.int64) for x in (d, dn, o))
+    q = np.array(lab, np.int32).reshape(len(lab), 3, 2)
+    dims = np.stack([d, np.ones_like(d), dn], axis=1)
+    sizes = d * dn
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    idx = _scatter_ones(d, np.concatenate([[0], np.cumsum(d)[:-1]]), o, d, offs)
+    buf = np.zeros(int(sizes.sum()))
+    bufz = np.zeros_like(buf)
+    buf[idx] = 1.0
+    bufz[idx] = np.repeat(np.array(sign, np.float64), d)
+    return Packed(q, dims, buf), Packed(q.copy(), dims.copy(), bufz), D, off
 
 
-def _diag_product(K: KeptSpace, D: dict, off: dict, f: float) -> QSpace:
+def _diag_product(K: KeptSpace, D: dict, off: dict, f: float) -> Packed:
     """f (E_K x 1) in the product basis: one diagonal block per combined
     sector, E_K placed on the slice of each (K sector, site state)."""
-    diag = {qn: np.zeros(d) for qn, d in D.items()}
+    diag = {qn: np.zeros(dd) for qn, dd in D.items()}
     for (qk, s), o in off.items():
         qn = (qk[0] + s[0], qk[1] + s[1])
         diag[qn][o:o + len(K.E[qk])] = f * K.E[qk]
     labs = sorted(diag)
-    Q = np.array(labs, np.int32)
-    return QSpace([Q, Q.copy()], [np.diag(diag[l]) for l in labs], {})
+    n = np.array([D[l] for l in labs], np.int64)
+    q = np.repeat(np.array(labs, np.int32).reshape(len(labs), 1, 2), 2, axis=1)
+    dims = np.stack([n, n], axis=1)
+    sizes = n * n
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    idx = _scatter_ones(n, np.concatenate([[0], np.cumsum(n)[:-1]]), np.zeros_like(n), n, offs)
+    buf = np.zeros(int(sizes.sum()))
+    buf[idx] = np.concatenate([diag[l] for l in labs]) if labs else np.zeros(0)
+    return Packed(q, dims, buf)
 
 
 def step(K: KeptSpace, backend, t: float, Lambda: float, nkeep: int = -1, deps: float = 0.0) -> KeptSpace:
@@ -123,9 +166,9 @@ def step(K: KeptSpace, backend, t: float, Lambda: float, nkeep: int = -1, deps: 
     and truncation to nkeep states (markSet; deps > 0 keeps near-degenerate
     levels together), the new kept space."""
     A4, A4Z, D, off = _fusion(K)
-    a4, a4z = backend.put(A4), backend.put(A4Z)
+    a4, a4z = _put(backend, A4), _put(backend, A4Z)
     c = {s: backend.put(q) for s, q in site_ops().items()}
-    H = backend.put(_diag_product(K, D, off, math.sqrt(Lambda)))
+    H = _put(backend, _diag_product(K, D, off, math.sqrt(Lambda)))
     for s in ("up", "dn"):
         Fd = backend.permute(K.F[s], [2, 1], conj=True)            # f_{N,s}^+ in K
         X1 = backend.contract(Fd, "2", a4z, "1")                   # (K', s, n), Z on K
@@ -161,6 +204,10 @@ class DeviceBackend:
     def put(self, A: QSpace):
         from .qspace import upload
         return upload(A, self.ctx)
+
+    def put_packed(self, P: Packed):
+        from .qspace import upload_packed
+        return upload_packed(P.q, P.dims, P.buf, self.ctx)
 
     def contract(self, A, ia, B, ib):
         from .qspace import contract_dev

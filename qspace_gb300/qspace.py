@@ -414,6 +414,39 @@ def upload(A: QSpace, ctx: Context | None = None) -> Tensor:
     return Tensor(ctx, h, A.info)
 
 
+def upload_packed(q, dims, buf, ctx: Context | None = None, info: dict | None = None) -> Tensor:
+    """Device tensor from the packed form directly (no per-block Python
+    objects): q (nblk, rank, qdim) int32 labels, dims (nblk, rank) int64,
+    buf the blocks column-major back to back (float64 or complex128)."""
+    ctx = ctx or default_context()
+    q = np.ascontiguousarray(q, np.int32)
+    n, r = int(q.shape[0]), int(q.shape[1])
+    qd = int(q.shape[2]) if q.ndim == 3 else 1
+    dims = np.ascontiguousarray(dims, np.int64).reshape(n, r)
+    sizes = np.prod(dims, axis=1) if r else np.ones(n, np.int64)
+    offs = np.zeros(n, np.int64)
+    if n > 1:
+        offs[1:] = np.cumsum(sizes)[:-1]
+    buf = np.ascontiguousarray(buf)
+    if buf.size != int(sizes.sum()):
+        raise ValueError("upload_packed: buffer size does not match the block dimensions")
+    cplx = np.iscomplexobj(buf)
+    v = _capi.QSpaceView()
+    v.rank, v.qdim, v.nblk = r, qd, n
+    v.q = q.ctypes.data_as(_capi.c_int32_p)
+    v.dims = dims.ctypes.data_as(_capi.c_int64_p)
+    v.offs = offs.ctypes.data_as(_capi.c_int64_p)
+    v.data = buf.view(np.float64).ctypes.data_as(_capi.c_double_p)
+    v.is_complex = 1 if cplx else 0
+    tags = (info or {}).get("itags")
+    tb = ",".join(tags).encode() if tags else None
+    v.itags = tb
+    h = C.c_void_p()
+    check(ctx.lib.qs_tensor_upload(ctx.h, C.byref(v), C.byref(h)))
+    ctx.sync()
+    return Tensor(ctx, h, info)
+
+
 def contract_dev(A: Tensor, ia, B: Tensor, ib, perm=None, *, prec: str = "fp64", nslices: int = 0,
                  tol: float = 1e-12, stats: dict | None = None) -> Tensor:
     ctx = A.ctx
