@@ -528,7 +528,7 @@ static void run_products(Ctx *ctx, const std::vector<Prepared *> &batch, const q
   if (prec == QS_PREC_SPLIT) {
     SplitResult sr = run_split(ctx, pairs, grp, bM, bN, c_off, baseA, baseB, baseC, cplx,
                                forced_slices ? forced_slices : (opts ? opts->nslices : 0),
-                               opts && opts->tol > 0 ? opts->tol : 1e-12, nullptr, forced_bits, nullptr,
+                               opts && opts->tol > 0 ? opts->tol : 1e-12, nullptr, forced_bits,
                                any_view ? &va : nullptr, any_view ? &vb : nullptr);
     if (stats) {
       stats->nslices = sr.nslices;

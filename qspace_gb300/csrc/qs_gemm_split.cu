@@ -1089,24 +1089,6 @@ void launch_split_s(Ctx *ctx, bool cplx, const SplitPair *d_pairs, const Operand
 
 }  // namespace
 
-namespace {
-// A pair's CG factor from the device table, folded like the host does for a
-// given factor (make_factor, frexp exponent); a missing key gives factor 0
-// and raises the source's flag.
-__global__ void resolve_split_factors_kernel(SplitPair *__restrict__ sp, int64_t n, FactorSource fs) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double x = 0.0;
-    if (!xview_find(fs.tab, fs.keys[2 * i], fs.keys[2 * i + 1], &x)) atomicExch(fs.missing, 1);
-    const Factor f = make_factor(x);
-    sp[i].fm = f.fm;
-    sp[i].fe = f.fe;
-    sp[i].fneg = f.neg ? 1 : 0;
-    int e = 0;
-    if (x != 1.0 && x != 0.0) frexp(x, &e);
-    sp[i].e_afac = e;
-  }
-}
-}  // namespace
 
 // ---------------------------------------------------------------- host side
 // Largest summed (real) depth that keeps every accumulator group exact:
@@ -1484,7 +1466,7 @@ static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs,
                                    const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                                    const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                                    bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
-                                   int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
+                                   int forced_bits, const std::vector<OperandView> *va,
                                    const std::vector<OperandView> *vb);
 
 // Shallow output blocks (summed depth <= SHALLOW_K) are computed directly in
@@ -1493,13 +1475,12 @@ static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs,
 // buffer and summed in part order (split_deep).  Both decisions depend on the
 // block alone, and the digit plan is the one of the list as given, so a
 // block gives the same bits whatever else is in the launch.  Blocks with a
-// pair read through a view, and lists with per-pair factor keys, run as
-// they are.
+// pair read through a view run as they are.
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                       const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                       const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                       bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
-                      int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
+                      int forced_bits, const std::vector<OperandView> *va,
                       const std::vector<OperandView> *vb) {
   const size_t nb = blk_M.size();
   const int64_t eb = cplx ? 16 : 8;
@@ -1513,14 +1494,13 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
   }
   std::vector<char> shallow(nb, 0), rest(nb, 1);
   std::vector<int64_t> shallow_ids;
-  if (!fs)
-    for (size_t g = 0; g < nb; ++g)
-      if (!(keep.size() && keep[g]) && is_shallow(pairs, grp[g], grp[g + 1]) &&
-          shallow_direct_wins(pairs, grp[g], grp[g + 1], blk_M[g], blk_N[g], cplx)) {
-        shallow[g] = 1;
-        rest[g] = 0;
-        shallow_ids.push_back((int64_t)g);
-      }
+  for (size_t g = 0; g < nb; ++g)
+    if (!(keep.size() && keep[g]) && is_shallow(pairs, grp[g], grp[g + 1]) &&
+        shallow_direct_wins(pairs, grp[g], grp[g + 1], blk_M[g], blk_N[g], cplx)) {
+      shallow[g] = 1;
+      rest[g] = 0;
+      shallow_ids.push_back((int64_t)g);
+    }
   if (!shallow_ids.empty()) {
     const DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cplx ? 2 : 1, tol, forced_slices, forced_bits);
     run_shallow(ctx, pairs, grp, blk_M, blk_N, c_off, blk_ldc, shallow_ids, A, B, C, cplx);
@@ -1536,11 +1516,11 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
       if (vb) vb2.push_back((*vb)[q]);
     }
     SplitResult r2 = run_split(ctx, R.pairs, R.grp, R.bM, R.bN, R.coff, A, B, C, cplx, dp.nslices, tol, &R.bldc,
-                               dp.bits, nullptr, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
+                               dp.bits, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
     return r2.nslices ? r2 : res;
   }
   DeepSplit ds;
-  if (!fs && reinterpret_cast<uintptr_t>(C) % eb == 0 &&
+  if (reinterpret_cast<uintptr_t>(C) % eb == 0 &&
       split_deep(pairs, grp, blk_M, blk_N, c_off, blk_ldc, ds, keep.empty() ? nullptr : &keep)) {
     const DigitPlan dp = choose_digits_for(pairs, grp, blk_M, blk_N, cplx ? 2 : 1, tol, forced_slices, forced_bits);
     double *T = dev_alloc<double>(ctx, (size_t)std::max<int64_t>(ds.temp_elems, 1) * (cplx ? 2 : 1));
@@ -1555,7 +1535,7 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
       ds.place((int64_t)(reinterpret_cast<intptr_t>(T) - reinterpret_cast<intptr_t>(C)) / eb);
       d_red = dev_upload(ctx, ds.red);
       SplitResult res = run_split_lists(ctx, ds.pairs, ds.grp, ds.bM, ds.bN, ds.coff, A, B, C, cplx, dp.nslices, tol,
-                                        &ds.bldc, dp.bits, nullptr, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
+                                        &ds.bldc, dp.bits, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
       launch_reduce_parts(ctx, d_red, (int64_t)ds.red.size(), T, C, cplx);
       dev_free(ctx, d_red);
       dev_free(ctx, T);
@@ -1568,14 +1548,14 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
     }
   }
   return run_split_lists(ctx, pairs, grp, blk_M, blk_N, c_off, A, B, C, cplx, forced_slices, tol, blk_ldc,
-                         forced_bits, fs, va, vb);
+                         forced_bits, va, vb);
 }
 
 static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
                                    const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N,
                                    const std::vector<int64_t> &c_off, const double *A, const double *B, double *C,
                                    bool cplx, int forced_slices, double tol, const std::vector<int32_t> *blk_ldc,
-                                   int forced_bits, const FactorSource *fs, const std::vector<OperandView> *va,
+                                   int forced_bits, const std::vector<OperandView> *va,
                                    const std::vector<OperandView> *vb) {
   SplitWork w;
   SplitResult res = plan_split(pairs, grp, blk_M, blk_N, c_off, cplx, forced_slices, tol, blk_ldc, w, forced_bits,
@@ -1594,12 +1574,6 @@ static SplitResult run_split_lists(Ctx *ctx, const std::vector<PairDesc> &pairs,
   }
   d.E = dev_alloc<int>(ctx, (size_t)w.nE);
   d.F = dev_alloc<int>(ctx, (size_t)w.nF);
-  if (fs && !w.sp.empty()) {
-    const int64_t n = (int64_t)w.sp.size();
-    resolve_split_factors_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, ctx->stream>>>(
-        d.pairs, n, *fs);
-    QS_LAUNCHED(ctx);
-  }
   launch_split(ctx, w, cplx, d, A, B, C, ctx->d_err);
   dev_free(ctx, d.pairs);
   dev_free(ctx, d.sa);

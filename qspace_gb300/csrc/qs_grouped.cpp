@@ -96,28 +96,25 @@ GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elem
 
 void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
              const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
-             const std::vector<int32_t> *bldc, const double *A, const double *B, double *C, bool cplx,
-             const FactorSource *fs) {
+             const std::vector<int32_t> *bldc, const double *A, const double *B, double *C, bool cplx) {
   // shallow blocks directly (run_shallow), the rest through the tiles
-  if (!fs) {
-    std::vector<char> rest(bM.size(), 1);
-    std::vector<int64_t> ids;
-    for (size_t b = 0; b < bM.size(); ++b)
-      if (is_shallow(pairs, grp[b], grp[b + 1])) {
-        rest[b] = 0;
-        ids.push_back((int64_t)b);
-      }
-    if (!ids.empty()) {
-      run_shallow(ctx, pairs, grp, bM, bN, coff, bldc, ids, A, B, C, cplx);
-      if (ids.size() == bM.size()) return;
-      const BlockList R = select_blocks(pairs, grp, bM, bN, coff, bldc, rest);
-      run_f64(ctx, R.pairs, R.grp, R.bM, R.bN, R.coff, &R.bldc, A, B, C, cplx, nullptr);
-      return;
+  std::vector<char> rest(bM.size(), 1);
+  std::vector<int64_t> ids;
+  for (size_t b = 0; b < bM.size(); ++b)
+    if (is_shallow(pairs, grp[b], grp[b + 1])) {
+      rest[b] = 0;
+      ids.push_back((int64_t)b);
     }
+  if (!ids.empty()) {
+    run_shallow(ctx, pairs, grp, bM, bN, coff, bldc, ids, A, B, C, cplx);
+    if (ids.size() == bM.size()) return;
+    const BlockList R = select_blocks(pairs, grp, bM, bN, coff, bldc, rest);
+    run_f64(ctx, R.pairs, R.grp, R.bM, R.bN, R.coff, &R.bldc, A, B, C, cplx);
+    return;
   }
   DeepSplit ds;
   const int64_t eb = cplx ? 16 : 8;
-  const bool deep = !fs && reinterpret_cast<uintptr_t>(C) % eb == 0 && split_deep(pairs, grp, bM, bN, coff, bldc, ds);
+  const bool deep = reinterpret_cast<uintptr_t>(C) % eb == 0 && split_deep(pairs, grp, bM, bN, coff, bldc, ds);
   double *T = nullptr;
   PairDesc *dp = nullptr;
   TileDesc *dt = nullptr;
@@ -133,7 +130,6 @@ void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int
                                        : make_tiles(grp, bM, bN, coff, gemm_f64_tile_m(), gemm_f64_tile_n(), bldc);
     dp = dev_upload(ctx, pp);
     dt = dev_upload(ctx, tiles);
-    if (fs) launch_resolve_pairdesc(ctx, dp, (int64_t)pp.size(), *fs);
     launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), A, B, C, cplx ? 1 : 0);
     if (deep) {
       dr = dev_upload(ctx, ds.red);
@@ -154,17 +150,8 @@ void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int
 // that scratch instead of allocating.
 static void grouped_exec(Ctx *ctx, const GroupedPlan &g, size_t b0, size_t b1, const double *A,
                          const double *B, double *C, const qs_opts *opts, SplitResult *sr_out,
-                         uint8_t *static_scratch, size_t static_cap, int *static_err,
-                         const FactorSource *fs_all = nullptr) {
+                         uint8_t *static_scratch, size_t static_cap, int *static_err) {
   if (b1 <= b0) return;
-  // the keys of this range's pairs
-  FactorSource fs_sub{};
-  const FactorSource *fs = nullptr;
-  if (fs_all) {
-    fs_sub = *fs_all;
-    fs_sub.keys += 2 * g.grp[b0];
-    fs = &fs_sub;
-  }
   const bool whole = b0 == 0 && b1 == g.bM.size();
   std::vector<PairDesc> sub_pairs;
   std::vector<int64_t> sub_grp, sub_coff;
@@ -187,16 +174,15 @@ static void grouped_exec(Ctx *ctx, const GroupedPlan &g, size_t b0, size_t b1, c
   if (prec == QS_PREC_SPLIT) {
     const int ns = opts ? opts->nslices : 0;
     const double tol = opts && opts->tol > 0 ? opts->tol : 1e-12;
-    if (static_scratch && fs) fail(QS_ERR_ARG, "the static-scratch entry point takes its factors from the pair list");
     SplitResult sr = static_scratch
                          ? run_split_static(ctx, pairs, grp, bM, bN, coff, A, B, C, g.cplx, ns, tol, &bldc,
                                             static_scratch, static_cap, static_err)
-                         : run_split(ctx, pairs, grp, bM, bN, coff, A, B, C, g.cplx, ns, tol, &bldc, 0, fs);
+                         : run_split(ctx, pairs, grp, bM, bN, coff, A, B, C, g.cplx, ns, tol, &bldc, 0);
     if (sr_out && sr.err_bound >= sr_out->err_bound) *sr_out = sr;
   } else if (static_scratch) {
     fail(QS_ERR_ARG, "the static-scratch entry point runs the split path only");
   } else if (prec == QS_PREC_FP64) {
-    run_f64(ctx, pairs, grp, bM, bN, coff, &bldc, A, B, C, g.cplx, fs);
+    run_f64(ctx, pairs, grp, bM, bN, coff, &bldc, A, B, C, g.cplx);
   } else {
     fail(QS_ERR_ARG, "unknown precision mode %d", prec);
   }
@@ -219,14 +205,13 @@ static void fill_stats(qs_stats *stats, const GroupedPlan &g, const SplitResult 
 // of it.
 void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
                  const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
-                 int64_t c_elems, uint8_t *static_scratch, size_t static_cap, int *static_err,
-                 const FactorSource *fs) {
+                 int64_t c_elems, uint8_t *static_scratch, size_t static_cap, int *static_err) {
   if (stats) std::memset(stats, 0, sizeof *stats);
   GroupedPlan g = grouped_plan(pl, a_elems, b_elems, c_elems);
   if (g.pairs.empty()) return;
   const int64_t launches0 = ctx->launches;
   SplitResult sr;
-  grouped_exec(ctx, g, 0, g.bM.size(), A, B, C, opts, &sr, static_scratch, static_cap, static_err, fs);
+  grouped_exec(ctx, g, 0, g.bM.size(), A, B, C, opts, &sr, static_scratch, static_cap, static_err);
   fill_stats(stats, g, sr, ctx->launches - launches0);
 }
 

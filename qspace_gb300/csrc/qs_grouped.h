@@ -25,21 +25,18 @@ struct GroupedPlan {
 // access is checked against them.
 GroupedPlan grouped_plan(const qs_pair_list *pl, int64_t a_elems, int64_t b_elems, int64_t c_elems);
 
-struct FactorSource;
-// The plain FP64 grouped product of a list (64 x 64 tiles), with deep output
-// blocks cut along their depth and summed in part order (split_deep) unless
-// the factors come from keys (`fs`).
+// The plain FP64 grouped product of a list (64 x 64 tiles): shallow output
+// blocks computed directly (run_shallow), deep ones cut along their depth and
+// summed in part order (split_deep).
 void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
              const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
-             const std::vector<int32_t> *bldc, const double *A, const double *B, double *C, bool cplx,
-             const FactorSource *fs = nullptr);
+             const std::vector<int32_t> *bldc, const double *A, const double *B, double *C, bool cplx);
 
 // Validates the pair list, then launches the FP64 or the split path on all of
-// it.  With `fs` every pair's factor is looked up on the device (the pair
-// list's afac is ignored).
+// it.
 void grouped_run(Ctx *ctx, const qs_pair_list *pl, const double *A, const double *B, double *C,
                  const qs_opts *opts, qs_stats *stats, int64_t a_elems, int64_t b_elems,
                  int64_t c_elems, uint8_t *static_scratch = nullptr, size_t static_cap = 0,
-                 int *static_err = nullptr, const FactorSource *fs = nullptr);
+                 int *static_err = nullptr);
 
 }  // namespace qs

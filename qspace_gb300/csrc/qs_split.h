@@ -31,18 +31,15 @@ DigitPlan choose_digits_for(const std::vector<PairDesc> &pairs, const std::vecto
                             const std::vector<int32_t> &blk_M, const std::vector<int32_t> &blk_N, int cm,
                             double tol, int forced_slices, int forced_bits = 0);
 
-struct FactorSource;
-// With `fs` every pair's CG factor is looked up on the device before it is
-// folded into the digits (the pairs' afac is ignored).  With va / vb (one per
-// pair; nl = 0 for none) the slicing reads op(A) / op(B) of a pair through
-// its strided view instead of (lda, trans): a permuted operand needs no copy.
+// With va / vb (one per pair; nl = 0 for none) the slicing reads op(A) /
+// op(B) of a pair through its strided view instead of (lda, trans): a
+// permuted operand needs no copy.
 SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs,
                       const std::vector<int64_t> &grp, const std::vector<int32_t> &blk_M,
                       const std::vector<int32_t> &blk_N, const std::vector<int64_t> &c_off,
                       const double *A, const double *B, double *C, bool cplx,
                       int forced_slices, double tol,
                       const std::vector<int32_t> *blk_ldc = nullptr, int forced_bits = 0,
-                      const FactorSource *fs = nullptr,
                       const std::vector<OperandView> *va = nullptr,
                       const std::vector<OperandView> *vb = nullptr);
 

@@ -40,14 +40,6 @@ __global__ void xcache_get_kernel(XView v, const uint64_t *__restrict__ keys, in
   }
 }
 
-__global__ void resolve_pairdesc_kernel(PairDesc *__restrict__ pd, int64_t n, FactorSource fs) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double x = 0.0;
-    if (!xview_find(fs.tab, fs.keys[2 * i], fs.keys[2 * i + 1], &x)) atomicExch(fs.missing, 1);
-    pd[i].afac = x;
-  }
-}
-
 int grid_for(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), 4096); }
 
 XView view_of(const qs_xcache *c) { return XView{c->dkeys, c->dvals, c->cap - 1}; }
@@ -75,12 +67,6 @@ void xcache_orphan_all(Ctx *ctx) {
     c->ctx = nullptr;
   }
   ctx->tables.clear();
-}
-
-void launch_resolve_pairdesc(Ctx *ctx, PairDesc *pd, int64_t n, const FactorSource &fs) {
-  if (n <= 0) return;
-  resolve_pairdesc_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(pd, n, fs);
-  QS_LAUNCHED(ctx);
 }
 
 }  // namespace qs

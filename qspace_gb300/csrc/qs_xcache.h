@@ -49,16 +49,6 @@ __device__ inline bool xview_find(const XView &v, uint64_t a, uint64_t b, double
   return false;
 }
 
-// Factors of one launch: 2 key words per pair (device), the table, and a
-// device flag raised when a key is missing (its pair then gets factor 0).
-struct FactorSource {
-  const uint64_t *keys;
-  XView tab;
-  int *missing;
-};
-
-// qs_xcache.cu: pd[i].afac = factor of key i
-void launch_resolve_pairdesc(Ctx *ctx, PairDesc *pd, int64_t n, const FactorSource &fs);
 // qs_xcache.cu: frees the device memory of every table of a context that is
 // being destroyed; the tables stay valid handles (unusable, destroyable)
 void xcache_orphan_all(Ctx *ctx);
