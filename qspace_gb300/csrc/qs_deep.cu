@@ -21,17 +21,22 @@ namespace qs {
 
 namespace {
 
-// Depth of a part (elements of K, complex or real) and the number of tiles a
-// block should reach.  A tile of 64 x 32 outputs is the unit of the estimate.
+// Depth of a part (elements of K, complex or real) and the parallel work a
+// block should reach: output tiles (64 x 32 outputs as the unit of the
+// estimate) for the products, and strips of 16 lines (each slicing its lines
+// over the whole depth) for the digit preparation of the split path.
 constexpr int64_t KPART = 4096;
 constexpr int64_t TARGET_TILES = 256;
+constexpr int64_t TARGET_STRIPS = 1024;
 
 int64_t parts_of(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1, int32_t M, int32_t N) {
   int64_t depth = 0;
   for (int64_t p = p0; p < p1; ++p) depth += std::max<int32_t>(pairs[p].K, 0);
   if (depth < 2 * KPART) return 1;
   const int64_t tiles = std::max<int64_t>(1, ((int64_t)M + 63) / 64 * (((int64_t)N + 31) / 32));
-  return std::max<int64_t>(1, std::min<int64_t>(depth / KPART, TARGET_TILES / tiles));
+  const int64_t strips = std::max<int64_t>(1, ((int64_t)M + N + 7) / 8);
+  const int64_t want = std::max(TARGET_TILES / tiles, TARGET_STRIPS / strips);
+  return std::max<int64_t>(1, std::min<int64_t>(depth / KPART, want));
 }
 
 __global__ void reduce_parts_kernel(const DeepReduce *__restrict__ red, const double *__restrict__ T,
