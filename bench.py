@@ -619,6 +619,37 @@ def main():
                 ts.append(time.perf_counter() - t0)
             rdm[pr + "_ms_p50"] = 1e3 * statistics.median(ts)
 
+    # ---- contraction shapes the tiled products would pad or serialise:
+    # rho(s, s') = sum over both bonds of A A* for a D = 8192 complex site
+    # tensor (deep output blocks: four 1 x 1 outputs, each summing 1-5 x 10^5
+    # products), and a site operator applied over the site leg of the same
+    # tensor (shallow blocks: a summed depth of 1, M = 1); device-resident
+    # operands, wall time of the library call (it waits for its products)
+    shapes = None
+    if not a.no_extras:
+        from qspace_gb300 import upload
+        from qspace_gb300.nrg import site_ops
+        from qspace_gb300.qspace import contract_dev
+        from qspace_gb300.workloads import mps_site_tensor
+        tA = upload(mps_site_tensor(seed=3, D=8192, complex_data=True), ctx)
+        shapes = {"workload": "site tensor A(L,s,R), U(1)xU(1), D=8192, complex128"}
+        # the site operator acts on A's site leg: c(s', s) A(L, s, R)
+        top = upload(site_ops()["up"], ctx)
+        for name, (X, ia, Y, ib) in (("rdm_13_13*", (tA, "13", tA, "13*")), ("site_op_2_2", (top, "2", tA, "2"))):
+            for pr in ("split", "fp64"):
+                try:
+                    contract_dev(X, ia, Y, ib, prec=pr).free()
+                    ctx.sync()
+                    t0 = time.perf_counter()
+                    for _ in range(5):
+                        contract_dev(X, ia, Y, ib, prec=pr).free()
+                    ctx.sync()
+                    shapes[f"{name}_{pr}_ms"] = 1e3 * (time.perf_counter() - t0) / 5
+                except Exception as ex:  # reported in the row
+                    shapes[f"{name}_{pr}_error"] = str(ex)[:200]
+        tA.free()
+        top.free()
+
     # ---- permuteQS kernels on a device-resident two-site wave function
     permute = None if a.no_extras else permute_bench(ctx)
 
@@ -761,7 +792,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "slices": slices, "rdm_latency": rdm, "permute": permute, "eig": eig, "nrg": nrg, "serving": serving,
+                "slices": slices, "rdm_latency": rdm, "shapes": shapes, "permute": permute, "eig": eig, "nrg": nrg, "serving": serving,
                 "clocks": ck}
         if shard_info is not None:
             line["shard"] = shard_info

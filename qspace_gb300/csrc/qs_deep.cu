@@ -97,7 +97,83 @@ __global__ void shallow_kernel(const ShallowTask *__restrict__ tasks, const Pair
   }
 }
 
+// One CTA per output element of a small block: every thread sums its share
+// of the block's (pair, k) terms in order, then a fixed tree reduces them.
+struct DotTask {
+  int64_t c_off;
+  int32_t p0, p1, M, ldc, i, j;
+};
+constexpr int DOT_THREADS = 256;
+
+template <bool CPLX>
+__global__ void __launch_bounds__(DOT_THREADS)
+dot_kernel(const DotTask *__restrict__ tasks, const PairDesc *__restrict__ pairs, const double *__restrict__ A,
+           const double *__restrict__ B, double *__restrict__ C) {
+  __shared__ double red[2][DOT_THREADS];
+  const DotTask t = tasks[blockIdx.x];
+  double re = 0.0, im = 0.0;
+  for (int p = t.p0; p < t.p1; ++p) {
+    const PairDesc P = pairs[p];
+    const bool ta = P.trans & 1, tb = P.trans & 2, ca = P.trans & 4, cb = P.trans & 8;
+    double sr = 0.0, si = 0.0;
+    for (int k = threadIdx.x; k < P.K; k += DOT_THREADS) {
+      const int64_t ia = P.a_off + (ta ? k + t.i * (int64_t)P.lda : t.i + k * (int64_t)P.lda);
+      const int64_t ib = P.b_off + (tb ? t.j + k * (int64_t)P.ldb : k + t.j * (int64_t)P.ldb);
+      if (CPLX) {
+        const double ar = A[2 * ia], ai = ca ? -A[2 * ia + 1] : A[2 * ia + 1];
+        const double br = B[2 * ib], bi = cb ? -B[2 * ib + 1] : B[2 * ib + 1];
+        sr += ar * br - ai * bi;
+        si += ar * bi + ai * br;
+      } else {
+        sr += A[ia] * B[ib];
+      }
+    }
+    re += P.afac * sr;
+    im += P.afac * si;
+  }
+  red[0][threadIdx.x] = re;
+  red[1][threadIdx.x] = im;
+  __syncthreads();
+  for (int w = DOT_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int64_t o = t.c_off + t.i + t.j * (int64_t)t.ldc;
+    if (CPLX) {
+      C[2 * o] = red[0][0];
+      C[2 * o + 1] = red[1][0];
+    } else {
+      C[o] = red[0][0];
+    }
+  }
+}
+
 }  // namespace
+
+void run_dot(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+             const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
+             const std::vector<int32_t> *bldc, const std::vector<int64_t> &blocks, const double *A,
+             const double *B, double *C, bool cplx) {
+  std::vector<DotTask> tasks;
+  for (int64_t b : blocks)
+    for (int32_t j = 0; j < bN[b]; ++j)
+      for (int32_t i = 0; i < bM[b]; ++i)
+        tasks.push_back(DotTask{coff[b], (int32_t)grp[b], (int32_t)grp[b + 1], bM[b],
+                                bldc ? (*bldc)[b] : std::max(bM[b], 1), i, j});
+  if (tasks.empty()) return;
+  if (tasks.size() > 0x7fffffff) fail(QS_ERR_SHAPE, "small-block products: too many outputs");
+  DotTask *dt = dev_upload(ctx, tasks);
+  PairDesc *dp = dev_upload(ctx, pairs);
+  if (cplx) dot_kernel<true><<<(unsigned)tasks.size(), DOT_THREADS, 0, ctx->stream>>>(dt, dp, A, B, C);
+  else dot_kernel<false><<<(unsigned)tasks.size(), DOT_THREADS, 0, ctx->stream>>>(dt, dp, A, B, C);
+  QS_LAUNCHED(ctx);
+  dev_free(ctx, dt);
+  dev_free(ctx, dp);
+}
 
 bool is_shallow(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1) {
   int64_t depth = 0;

@@ -1534,8 +1534,31 @@ SplitResult run_split(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::v
     try {
       ds.place((int64_t)(reinterpret_cast<intptr_t>(T) - reinterpret_cast<intptr_t>(C)) / eb);
       d_red = dev_upload(ctx, ds.red);
-      SplitResult res = run_split_lists(ctx, ds.pairs, ds.grp, ds.bM, ds.bN, ds.coff, A, B, C, cplx, dp.nslices, tol,
-                                        &ds.bldc, dp.bits, va ? &va2 : nullptr, vb ? &vb2 : nullptr);
+      // parts with a few outputs: one CTA per output element in FP64
+      // (run_dot; the tiles would compute 4096 outputs for each); the rest
+      // through the split path
+      std::vector<char> sel(ds.bM.size(), 1);
+      std::vector<int64_t> small;
+      for (size_t g = 0; g < ds.bM.size(); ++g)
+        if (ds.part[g] && (int64_t)ds.bM[g] * ds.bN[g] <= DOT_OUTPUTS) {
+          sel[g] = 0;
+          small.push_back((int64_t)g);
+        }
+      run_dot(ctx, ds.pairs, ds.grp, ds.bM, ds.bN, ds.coff, &ds.bldc, small, A, B, C, cplx);
+      SplitResult res;
+      res.nslices = dp.nslices;
+      res.bits = dp.bits;
+      res.err_bound = dp.err_bound;
+      if (small.size() < ds.bM.size()) {
+        const BlockList R = select_blocks(ds.pairs, ds.grp, ds.bM, ds.bN, ds.coff, &ds.bldc, sel);
+        std::vector<OperandView> va3, vb3;
+        for (int32_t q : R.src) {
+          if (va) va3.push_back(va2[q]);
+          if (vb) vb3.push_back(vb2[q]);
+        }
+        res = run_split_lists(ctx, R.pairs, R.grp, R.bM, R.bN, R.coff, A, B, C, cplx, dp.nslices, tol, &R.bldc,
+                              dp.bits, va ? &va3 : nullptr, vb ? &vb3 : nullptr);
+      }
       launch_reduce_parts(ctx, d_red, (int64_t)ds.red.size(), T, C, cplx);
       dev_free(ctx, d_red);
       dev_free(ctx, T);

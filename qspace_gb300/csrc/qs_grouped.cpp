@@ -125,12 +125,28 @@ void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int
       ds.place((int64_t)(reinterpret_cast<intptr_t>(T) - reinterpret_cast<intptr_t>(C)) / eb);
     }
     const std::vector<PairDesc> &pp = deep ? ds.pairs : pairs;
-    std::vector<TileDesc> tiles = deep ? make_tiles(ds.grp, ds.bM, ds.bN, ds.coff, gemm_f64_tile_m(),
-                                                    gemm_f64_tile_n(), &ds.bldc)
-                                       : make_tiles(grp, bM, bN, coff, gemm_f64_tile_m(), gemm_f64_tile_n(), bldc);
+    const std::vector<int64_t> &gg = deep ? ds.grp : grp, &cc = deep ? ds.coff : coff;
+    const std::vector<int32_t> &mm = deep ? ds.bM : bM, &nn = deep ? ds.bN : bN;
+    const std::vector<int32_t> *ll = deep ? &ds.bldc : bldc;
+    // parts of deep blocks with a few outputs: one CTA per output element
+    // (run_dot); the others through the 64 x 64 tiles
+    std::vector<int64_t> small;
+    std::vector<TileDesc> tiles;
+    {
+      std::vector<TileDesc> all = make_tiles(gg, mm, nn, cc, gemm_f64_tile_m(), gemm_f64_tile_n(), ll);
+      std::vector<char> is_small(mm.size(), 0);
+      for (size_t b = 0; b < mm.size(); ++b)
+        if (deep && ds.part[b] && (int64_t)mm[b] * nn[b] <= DOT_OUTPUTS) {
+          is_small[b] = 1;
+          small.push_back((int64_t)b);
+        }
+      for (const TileDesc &t : all)
+        if (!is_small[t.cblk]) tiles.push_back(t);
+    }
+    run_dot(ctx, pp, gg, mm, nn, cc, ll, small, A, B, C, cplx);
     dp = dev_upload(ctx, pp);
     dt = dev_upload(ctx, tiles);
-    launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), A, B, C, cplx ? 1 : 0);
+    if (!tiles.empty()) launch_gemm_f64(ctx, dp, dt, (int64_t)tiles.size(), A, B, C, cplx ? 1 : 0);
     if (deep) {
       dr = dev_upload(ctx, ds.red);
       launch_reduce_parts(ctx, dr, (int64_t)ds.red.size(), T, C, cplx);

@@ -168,6 +168,15 @@ void run_shallow(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector
                  const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
                  const std::vector<int32_t> *bldc, const std::vector<int64_t> &blocks, const double *A,
                  const double *B, double *C, bool cplx);
+// Parts of deep output blocks with at most DOT_OUTPUTS elements on the FP64
+// path: one CTA per output element reduces over the part's pairs and depth
+// (a fixed partition and tree order); 64 x 64 tiles would compute 4096
+// outputs for each of them.
+constexpr int64_t DOT_OUTPUTS = 64;
+void run_dot(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
+             const std::vector<int32_t> &bM, const std::vector<int32_t> &bN, const std::vector<int64_t> &coff,
+             const std::vector<int32_t> *bldc, const std::vector<int64_t> &blocks, const double *A,
+             const double *B, double *C, bool cplx);
 // The same with the work list prepared once on device memory owned by the
 // caller (reusable plans): prepare, launch any number of times, release.
 struct ShallowPlan {
