@@ -248,7 +248,14 @@ QS_EXPORT qs_status qs_permute_dev(qs_ctx *ctx, const qs_tensor *A, const int32_
  * K x M), bit 1 transposes B (B stored N x K), bit 2 conjugates A, bit 3
  * conjugates B.  Pairs that share c_blk are summed in array order into the
  * same M x N output block (first pair overwrites).  All pointers are device
- * pointers; element type double or complex128 (is_complex). */
+ * pointers; element type double or complex128 (is_complex).
+ * How a block runs depends on the block alone (so a block gives the same
+ * bits in any batch): a block whose pairs sum at most 8 along K is computed
+ * directly in FP64 (always on the FP64 path; on the split path where the
+ * tiles would mostly be padding, e.g. M = 1); a block with a summed depth of
+ * thousands and few output tiles is cut along its depth into parts summed in
+ * a fixed order (parts of at most 64 outputs reduced in FP64); every other
+ * block runs through the grouped tiles of the chosen precision. */
 typedef struct {
   int64_t npairs;
   const int32_t *M, *N, *K;
@@ -312,6 +319,10 @@ QS_EXPORT void qs_grouped_plan_destroy(qs_grouped_plan *plan);
  *  - All calls in a process share the array of their device: calls that
  *    overlap in time (two host threads, two contexts) race on it and corrupt
  *    each other's results.  Serialise them.
+ *  - Every output block runs through the tiles as it is: blocks that
+ *    qs_grouped_gemm computes directly (a summed depth of at most 8) or cuts
+ *    along their depth (a few outputs over thousands of terms) give the same
+ *    product within the split error bound, not the same bits.
  *  - A, B, C are device pointers as for qs_grouped_gemm; the call returns
  *    after the product is complete: it synchronises the context's stream to
  *    read the error word, so it must not be called while that stream is
