@@ -170,9 +170,9 @@ void run_dot(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int
   PairDesc *dp = dev_upload(ctx, pairs);
   if (cplx) dot_kernel<true><<<(unsigned)tasks.size(), DOT_THREADS, 0, ctx->stream>>>(dt, dp, A, B, C);
   else dot_kernel<false><<<(unsigned)tasks.size(), DOT_THREADS, 0, ctx->stream>>>(dt, dp, A, B, C);
-  QS_LAUNCHED(ctx);
   dev_free(ctx, dt);
   dev_free(ctx, dp);
+  QS_LAUNCHED(ctx);
 }
 
 bool is_shallow(const std::vector<PairDesc> &pairs, int64_t p0, int64_t p1) {
@@ -230,9 +230,10 @@ void run_shallow(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector
   PairDesc *dp = dev_upload(ctx, pairs);
   if (cplx) shallow_kernel<true><<<(unsigned)tasks.size(), 256, 0, ctx->stream>>>(dt, dp, A, B, C);
   else shallow_kernel<false><<<(unsigned)tasks.size(), 256, 0, ctx->stream>>>(dt, dp, A, B, C);
-  QS_LAUNCHED(ctx);
+  // the work lists are released in stream order, also when the launch failed
   dev_free(ctx, dt);
   dev_free(ctx, dp);
+  QS_LAUNCHED(ctx);
 }
 
 ShallowPlan shallow_prepare(const std::vector<PairDesc> &pairs, const std::vector<int64_t> &grp,
