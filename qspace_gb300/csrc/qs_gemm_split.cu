@@ -52,6 +52,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <memory>
+#include <numeric>
 #include <type_traits>
 
 #include "qs_internal.h"
@@ -1422,12 +1423,26 @@ static SplitResult plan_split(const std::vector<PairDesc> &pairs_in, const std::
       }
   }
   // Longest tiles first (by summed depth): the tail of the launch is short.
-  std::stable_sort(tiles.begin(), tiles.end(), [&](const SplitTile &x, const SplitTile &y) {
-    int64_t kx = 0, ky = 0;
-    for (int p = x.p0; p < x.p1; ++p) kx += sp[p].KB;
-    for (int p = y.p0; p < y.p1; ++p) ky += sp[p].KB;
-    return kx > ky;
-  });
+  // The depth is a property of the tile's block: summed once per block, then
+  // a stable sort of the tiles by it.
+  {
+    std::vector<int64_t> depth(tiles.size());
+    for (size_t t = 0; t < tiles.size(); ++t) {
+      if (t > 0 && tiles[t].p0 == tiles[t - 1].p0 && tiles[t].p1 == tiles[t - 1].p1) {
+        depth[t] = depth[t - 1];
+        continue;
+      }
+      int64_t k = 0;
+      for (int p = tiles[t].p0; p < tiles[t].p1; ++p) k += sp[p].KB;
+      depth[t] = k;
+    }
+    std::vector<int64_t> order(tiles.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return depth[x] > depth[y]; });
+    std::vector<SplitTile> sorted(tiles.size());
+    for (size_t t = 0; t < tiles.size(); ++t) sorted[t] = tiles[order[t]];
+    tiles.swap(sorted);
+  }
   if (tiles.empty()) return res;
   if (tiles.size() > 0x7fffffff || sa.size() > 0x7fffffff || sb.size() > 0x7fffffff)
     fail(QS_ERR_SHAPE, "split: launch too large");
