@@ -72,3 +72,38 @@ def chain_matches_reference(backend_of, tol):
 
 def test_oracle_chain_matches_reference_fixture():
     chain_matches_reference(OracleBackend, 1e-12)
+
+
+def test_product_basis_packed_construction():
+    """The packed product basis A4 / A4Z and the diagonal product term, built
+    with whole-array operations, equal the block-by-block construction:
+    identity slices of each (kept sector, site state) inside its combined
+    sector, the fermionic sign on A4Z, E_K on the diagonal."""
+    from qspace_gb300 import nrg
+    rng = np.random.default_rng(7)
+    E = {}
+    for q in range(-3, 4):
+        for s2 in (-1, 1):
+            E[(q, s2)] = np.sort(rng.standard_normal(int(rng.integers(1, 6))))
+    K = nrg.KeptSpace(5, E)
+    A4, A4Z, D, off = nrg._fusion(K)
+    Q, Qz = A4.qspace(), A4Z.qspace()
+    b = 0
+    for s in nrg.SITE_LABELS:
+        for qk in sorted(E):
+            qn = (qk[0] + s[0], qk[1] + s[1])
+            d = len(E[qk])
+            blk = np.zeros((d, 1, D[qn]))
+            blk[:, 0, off[(qk, s)]:off[(qk, s)] + d] = np.eye(d)
+            assert tuple(Q.Q[0][b]) == qk and tuple(Q.Q[1][b]) == s and tuple(Q.Q[2][b]) == qn
+            assert np.array_equal(Q.data[b], blk)
+            assert np.array_equal(Qz.data[b], nrg.parity(qk, K.nsites) * blk)
+            b += 1
+    H = nrg._diag_product(K, D, off, 1.5).qspace()
+    diag = {qn: np.zeros(dd) for qn, dd in D.items()}
+    for (qk, s), o in off.items():
+        qn = (qk[0] + s[0], qk[1] + s[1])
+        diag[qn][o:o + len(E[qk])] = 1.5 * E[qk]
+    for i, lab in enumerate(sorted(diag)):
+        assert tuple(H.Q[0][i]) == lab and tuple(H.Q[1][i]) == lab
+        assert np.array_equal(H.data[i], np.diag(diag[lab]))
