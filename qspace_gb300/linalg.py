@@ -240,3 +240,265 @@ def eigQS_dev(H, Nkeep: int = -1, Etrunc: float = 0.0, deps: float = 0.0):
              "NK": nk.value, "Etrunc": et.value}
     return np.sort(E), parts
 
+
+
+# ------------------------------------------------------------------- svdQS
+# itags are strings, a trailing '*' marking an outgoing (conjugated) leg, as
+# the reference prints them (itag_, Source/wbindex.hh:631-790).
+def _tconj(t: str) -> str:
+    return t[:-1] if t.endswith("*") else t + "*"
+
+
+def _tname(t: str) -> str:
+    return t[:-1] if t.endswith("*") else t
+
+
+def _tdual(t: str) -> str:
+    """itag_::MarkDual (Source/wbindex.cc:1125-1147): toggles a trailing
+    prime on the name; names hold at most 8 characters."""
+    n = _tname(t)
+    n = n[:-1] if n.endswith("'") else n + "'"
+    if len(n) > 8:
+        raise ValueError(f"svdQS: itag '{n}' longer than 8 characters")
+    return n + ("*" if t.endswith("*") else "")
+
+
+def _tset_(t: str, x: str) -> str:
+    """itag_::Set_: an empty tag takes x; else t takes x's direction."""
+    if not _tname(t):
+        return x
+    return _tconj(t) if t.endswith("*") != x.endswith("*") else t
+
+
+def _lexsort(R: np.ndarray) -> np.ndarray:
+    """Stable permutation sorting integer rows lexicographically (first
+    column most significant), as wbMatrix::SortRecs (Source/wbMatrix.cc)."""
+    if R.shape[0] == 0 or R.shape[1] == 0:
+        return np.arange(R.shape[0])
+    return np.lexsort(R.T[::-1])
+
+
+def _groups(R: np.ndarray):
+    """wbMatrix::groupRecs (Source/wbMatrix.cc:1733-1744): the sort
+    permutation and the runs of equal rows -> (unique rows, member lists,
+    group id of every row)."""
+    p = _lexsort(R)
+    uniq, members = [], []
+    gid = np.empty(R.shape[0], np.int64)
+    for i in p:
+        if not uniq or not np.array_equal(R[i], uniq[-1]):
+            uniq.append(R[i])
+            members.append([])
+        members[-1].append(int(i))
+        gid[i] = len(uniq) - 1
+    return uniq, members, gid
+
+
+class _SvdLayout:
+    """Host plan of svdQS: PSI's legs permuted (the split-off legs last), its
+    blocks grouped by the label sum that the SVD conserves, and every group
+    laid out as one dense block matrix (rows: the distinct label records of
+    the first K legs, columns: those of the rest) -- SVD_Data::blockSVD and
+    QBlock::toBlockMatrix (Source/mpsortho.cc:546-613, 31-257)."""
+
+    def __init__(self, PSI: QSpace, idx):
+        r = PSI.rank
+        if PSI.nblk == 0:
+            raise ValueError("svdQS: got empty PSI")
+        I = [int(i) - 1 for i in np.atleast_1d(np.asarray(idx)).ravel()]
+        if not I or len(I) >= r:
+            raise ValueError(f"svdQS: invalid index set (len={len(I)}/{r})")
+        if any(i < 0 or i >= r for i in I) or len(set(I)) != len(I):
+            raise ValueError("svdQS: index out of bounds or not unique")
+        tags = list(PSI.info.get("itags") or [])
+        self.r, self.K = r, r - len(I)
+        self.P = [i for i in range(r) if i not in I] + I          # extend2Perm(.., 'E')
+        K, P = self.K, self.P
+        self.tags = [tags[p] for p in P] if len(tags) == r else []
+        if K != 1:
+            # only ingoing legs may be fused into the outgoing bond; the other
+            # group must point one way (blockSVD, Source/mpsortho.cc:557-573)
+            if not self.tags:
+                raise ValueError("svdQS: got invalid orthonormalization (rank mismatch of itags)")
+            qd = [not t.endswith("*") for t in self.tags]
+            if not all(qd[:K]):
+                raise ValueError("svdQS: got invalid orthonormalization "
+                                 "(only ingoing indices can be fused into outgoing)")
+            if any(q != qd[K] for q in qd[K + 1:]):
+                raise ValueError("svdQS: got invalid orthonormalization (2nd/right group is mixed in+out)")
+        n, qdim = PSI.nblk, PSI.qdim
+        Q = [np.asarray(PSI.Q[p], np.int64).reshape(n, qdim) for p in P]
+        dims = [tuple(PSI.block_dims(i)[p] for p in P) for i in range(n)]
+        self.qdim, self.cplx = qdim, PSI.is_complex
+        Ib = [0] if K == 1 else ([K] if K == r - 1 else list(range(K)))
+        qsum = sum(Q[j] for j in Ib)
+        uq, members, _ = _groups(qsum)
+        self.groups, self.mats = [], []
+        dt = np.complex128 if self.cplx else np.float64
+        for g, blks in zip(uq, members):
+            R1 = np.concatenate([Q[j][blks] for j in range(K)], axis=1)
+            R2 = np.concatenate([Q[j][blks] for j in range(K, r)], axis=1)
+            u1, _, g1 = _groups(R1)
+            u2, _, g2 = _groups(R2)
+            s1 = [None] * len(u1)
+            s2 = [None] * len(u2)
+            seen = set()
+            for b, i1, i2 in zip(blks, g1, g2):
+                if (i1, i2) in seen:
+                    raise ValueError("svdQS: block not unique (degenerate records)")
+                seen.add((i1, i2))
+                for s, i, d in ((s1, i1, dims[b][:K]), (s2, i2, dims[b][K:])):
+                    if s[i] is None:
+                        s[i] = d
+                    elif s[i] != d:
+                        raise ValueError("svdQS: block size mismatch")
+            o1 = np.concatenate([[0], np.cumsum([int(np.prod(d)) for d in s1])]).astype(np.int64)
+            o2 = np.concatenate([[0], np.cumsum([int(np.prod(d)) for d in s2])]).astype(np.int64)
+            M = np.zeros((int(o1[-1]), int(o2[-1])), dt)
+            for b, i1, i2 in zip(blks, g1, g2):
+                blk = np.asarray(PSI.data[b]).reshape(PSI.block_dims(b), order="F").transpose(P)
+                M[o1[i1]:o1[i1 + 1], o2[i2]:o2[i2 + 1]] = blk.reshape((o1[i1 + 1] - o1[i1], -1), order="F")
+            # the label of the new bond: that of the single split-off leg,
+            # else the label sum of U's legs (QBlock::init_bare_refA,
+            # Source/mpsortho.cc:277-296); it equals the group's sum except
+            # for rank 2 with both legs pointing the same way
+            if r - K == 1:
+                if any(not np.array_equal(x, u2[0]) for x in u2):
+                    raise ValueError("svdQS: got inconsistency in block symmetry")
+                g = u2[0]
+            self.groups.append({"q": np.asarray(g), "rows": (u1, s1, o1), "cols": (u2, s2, o2)})
+            self.mats.append(M)
+
+    def finish(self, Us, Ss, Vts, Nkeep=-1, Nkmin=0, stol=None, itag="", permA=None, permB=None):
+        """Truncation (svd_keep) and the U / S / Vd QSpaces with their
+        itags -- SVD_Data::dmrgTruncate (Source/mpsortho.cc:616-905) and
+        the final permutations of svdQS (Source/svdQS.cc:196-233)."""
+        r, K, P, qdim = self.r, self.K, self.P, self.qdim
+        if stol is None:
+            stol = 0.0 if Nkeep > 0 else 1e-8                     # WB_STOL_SVD
+        Nkmin = max(int(Nkmin), 0)
+        S_all = [np.asarray(s, np.float64) for s in Ss]
+        keep, nk, s2t, tot, sfac = svd_keep(S_all, int(Nkeep), Nkmin, float(stol))
+        SM = np.sort(np.concatenate(S_all))[::-1] if S_all else np.zeros(0)
+        # the flag that dmrgTruncate reports (Source/mpsortho.cc:682-735)
+        nk_u = int(Nkeep) if Nkeep >= 0 else 2 ** 32 - 1
+        flag = 0
+        if SM.size and SM[-1] > stol:
+            if SM.size > nk_u and stol:
+                flag += 1
+        elif nk >= nk_u and nk < SM.size:
+            flag += 1
+        if s2t and tot > s2t and abs(sfac - 1) > 0.01:
+            flag += 1
+        info = {"svd": SM, "stol": float(stol), "svd2tr": s2t / tot if tot else 0.0, "sv2tot": tot,
+                "sfac": sfac, "Nkmin": Nkmin, "Nkeep": nk, "Ntot": int(SM.size), "flag": flag, "K": K}
+        # itags of U, S and Vd (Source/mpsortho.cc:737-779)
+        T = self.tags
+        if len(T) != r:
+            raise ValueError("svdQS: got invalid/empty itags")
+        tu = _tname(itag or "")
+        revert, i = False, -1
+        if r - K == 1:
+            i = r - 1
+            tu = _tset_(tu, T[-1])
+            if not tu.endswith("*") and nk:
+                revert = not (r == 2 and T[0].endswith("*") != T[1].endswith("*"))   # iTags::isOp(2,'L')
+        elif K == 1:
+            i = 0
+            tu = _tconj(_tset_(tu, T[0]))
+        elif not T[0].endswith("*"):
+            tu = _tconj(tu)
+        tv = tu
+        if i == 1 and r == 2:
+            tu = _tname(T[0]) + ("*" if tu.endswith("*") else "")        # itag_::tSet
+            if not T[1].endswith("*") and revert:
+                tu = _tdual(tu)
+        tU, tS, tV = T[:K] + [tu], [_tconj(tu), tv], T[K:] + [_tconj(tv)]
+        # blocks: per group of kept values, U rows x new leg, S diagonal, V rows x new leg
+        UQ, Ud, SQ, Sd, VQ, Vd = [], [], [], [], [], []
+        for G, U, s, Vt, kp in zip(self.groups, Us, S_all, Vts, keep):
+            ik = np.flatnonzero(kp)
+            if ik.size == 0:
+                continue
+            g = G["q"]
+            Vc = np.asarray(Vt).T                                  # conj(V): PSI = U S Vc^T
+            for (u, sz, o), X, dst_q, dst_d in ((G["rows"], np.asarray(U), UQ, Ud), (G["cols"], Vc, VQ, Vd)):
+                for j in range(len(u)):
+                    dst_q.append(np.concatenate([u[j], g]))
+                    dst_d.append(X[o[j]:o[j + 1], ik].reshape(tuple(sz[j]) + (ik.size,), order="F"))
+            SQ.append(np.concatenate([g, g]))
+            Sd.append((s[ik] * sfac).reshape(-1, 1))
+
+        # the blocks of one QSpace must not repeat a label record
+        # (QSpace::Append2AndDestroy 'u', Source/mpsortho.cc:806-845)
+        for nm, recs in (("U", UQ), ("S", SQ), ("V", VQ)):
+            if len({tuple(x) for x in recs}) != len(recs):
+                raise ValueError(f"svdQS: {nm}: QIDX must not overlap")
+
+        def mk(recs, data, rank, tags):
+            if not recs:
+                return QSpace([], [], {})
+            R = np.asarray(recs, np.int64).reshape(len(recs), rank, qdim)
+            return QSpace([np.ascontiguousarray(R[:, k, :]).astype(np.int32) for k in range(rank)], data,
+                          {"itags": tags})
+
+        if revert:
+            # U's bond and S's first leg turn into the dual (labels negated,
+            # direction flipped, primed tag); both come back from the
+            # reference's identity contraction sorted by their labels
+            # (Source/mpsortho.cc:867-902, QSpace::initIdentityCG 'z')
+            tU[-1], tS[0] = _tdual(_tconj(tU[-1])), _tdual(_tconj(tS[0]))
+            for recs, data, col in ((UQ, Ud, K * qdim), (SQ, Sd, 0)):
+                for x in recs:
+                    x[col:col + qdim] = -x[col:col + qdim]
+                o = _lexsort(np.asarray(recs, np.int64).reshape(len(recs), -1)) if recs else []
+                recs[:] = [recs[j] for j in o]
+                data[:] = [data[j] for j in o]
+        Uq, Sq, Vq = mk(UQ, Ud, K + 1, tU), mk(SQ, Sd, 2, tS), mk(VQ, Vd, r - K + 1, tV)
+        # svdQS's final permutations: Vd gets its bond first; a single
+        # split-off leg leaves U in PSI's leg order, a single kept leg V
+        iP = list(np.argsort(P))
+        n = r - K + 1
+        pb = [n - 1] + list(range(n - 1))                          # wbperm::initLastTo(0, n)
+        if permB is not None:
+            pb = [pb[j] for j in _perm0(permB)]
+        pa = _perm0(permA) if permA is not None else None
+        if K + 1 == r:
+            pa = [iP[j] for j in pa] if pa is not None else iP
+        elif K == 1:
+            pb = [iP[j] for j in pb]
+        if pa is not None:
+            Uq = _permute(Uq, pa)
+        Vq = _permute(Vq, pb)
+        return Uq, Sq, Vq, info
+
+
+def _perm0(p) -> list:
+    return [int(x) - 1 for x in np.atleast_1d(np.asarray(p)).ravel()]
+
+
+def _permute(A: QSpace, p: list) -> QSpace:
+    """Leg permutation of a host QSpace (new leg i = old leg p[i]); the block
+    order stays (QSpace::Permute, Source/QSpace.hh:2669-2719)."""
+    if A.nblk == 0 or p == list(range(A.rank)):
+        return A
+    tags = A.info.get("itags")
+    data = [np.asarray(d).reshape(A.block_dims(i), order="F").transpose(p) for i, d in enumerate(A.data)]
+    return QSpace([A.Q[j] for j in p], data, {"itags": [tags[j] for j in p]} if tags else {})
+
+
+def svdQS(PSI: QSpace, idx, Nkeep: int = -1, Nkmin: int = 0, stol: float | None = None, itag: str = "",
+          permA=None, permB=None, ctx: Context | None = None):
+    """[U, S, Vd, info] = svdQS(PSI, idx, ...) for abelian QSpaces
+    (Source/svdQS.cc:170-234): the legs ``idx`` (1-based) are split off into
+    Vd, the others stay with U, PSI = U * S * Vd.  The blocks of one
+    conserved label sum form one matrix; all of them are decomposed in one
+    batched SVD on the GPU (qs_svd_blocks_ex), truncated together
+    (qs_svd_keep: Nkeep, Nkmin, stol; stol defaults to 1e-8 without Nkeep)
+    with the kept values rescaled to PSI's norm.  itags, block order and the
+    direction of the new bond follow the reference.  ``info`` holds svd (all
+    singular values, descending), stol, svd2tr, sv2tot, sfac, Nkmin, Nkeep
+    (kept count), Ntot, flag and K."""
+    L = _SvdLayout(PSI, idx)
+    Us, Ss, Vts = svd_blocks(L.mats, ctx)
+    return L.finish(Us, Ss, Vts, Nkeep, Nkmin, stol, itag, permA, permB)

@@ -48,3 +48,70 @@ def assert_qspace_close(C, R, tol: float):
     e = rel_err(C, R)
     assert e <= tol, f"relative error {e:.3e} > {tol:.1e}"
     return e
+
+
+def svd_bond_legs(r: int, idx, permA=None, permB=None):
+    """0-based positions of the new bond in svdQS's U and Vd: Vd gets it
+    first, a single split-off leg leaves U in PSI's leg order, a single kept
+    leg leaves Vd in it (Source/svdQS.cc:209-229), then permA / permB."""
+    I = [int(i) - 1 for i in idx]
+    K = r - len(I)
+    P = [i for i in range(r) if i not in I] + I
+    iP = [int(x) for x in np.argsort(P)]
+    n = r - K + 1
+    pb = [n - 1] + list(range(n - 1))
+    if permB:
+        pb = [pb[j - 1] for j in permB]
+    pa = [j - 1 for j in permA] if permA else None
+    if K + 1 == r:
+        pa = [iP[j] for j in pa] if pa else iP
+    elif K == 1:
+        pb = [iP[j] for j in pb]
+    return (pa.index(K) if pa else K), pb.index(r - K)
+
+
+def _padded(X, i):
+    r = len(X["Q"])
+    d = np.asarray(X["data"][i])
+    return d.reshape((tuple(d.shape) + (1,) * r)[:r] if d.ndim < r else d.shape, order="F")
+
+
+def svd_factors(U, S, V, bu: int, bv: int):
+    """Per block of S: (U rows stacked over U's blocks on that bond label,
+    the singular values, Vd columns side by side over Vd's blocks)."""
+    U, S, V = as_dict(U), as_dict(S), as_dict(V)
+    nU, nS, nV = len(U["data"]), len(S["data"]), len(V["data"])
+    qU = np.asarray(U["Q"][bu]).reshape(nU, -1) if nU else None
+    qV = np.asarray(V["Q"][bv]).reshape(nV, -1) if nV else None
+    out = []
+    for j in range(nS):
+        s = np.asarray(S["data"][j]).ravel()
+        lu = np.asarray(S["Q"][0]).reshape(nS, -1)[j]
+        lv = np.asarray(S["Q"][1]).reshape(nS, -1)[j]
+        ub = [np.moveaxis(_padded(U, i), bu, -1).reshape(-1, s.size, order="F")
+              for i in range(nU) if np.array_equal(qU[i], lu)]
+        vb = [np.moveaxis(_padded(V, i), bv, 0).reshape(s.size, -1, order="F")
+              for i in range(nV) if np.array_equal(qV[i], lv)]
+        out.append((np.vstack(ub), s, np.hstack(vb)))
+    return out
+
+
+def assert_svd_matches(got, refd, idx, opts, tol: float = 1e-11):
+    """svdQS outputs against the reference's: labels, block order, shapes and
+    itags exactly; the singular values and, per bond sector, U diag(S) Vd
+    (free of the singular vectors' phases) within tol; U and Vd isometric."""
+    for g, x in zip(got, refd):
+        assert_same_structure(g, x)
+        assert (as_dict(g)["info"].get("itags") or None) == (as_dict(x)["info"].get("itags") or None)
+    r = len(as_dict(got[0])["Q"]) if as_dict(got[0])["data"] else None
+    if r is None:
+        assert not as_dict(refd[0])["data"]
+        return
+    rank = len(as_dict(got[0])["Q"]) + len(as_dict(got[2])["Q"]) - 2
+    bu, bv = svd_bond_legs(rank, idx, opts.get("permA"), opts.get("permB"))
+    for (gu, gs, gv), (xu, xs, xv) in zip(svd_factors(*got, bu, bv), svd_factors(*refd, bu, bv)):
+        assert np.allclose(gs, xs, rtol=tol, atol=tol * xs.max())
+        smax = xs.max()
+        assert np.abs((gu * gs) @ gv - (xu * xs) @ xv).max() <= tol * smax * 10
+        assert np.abs(gu.conj().T @ gu - np.eye(gs.size)).max() <= tol * 10
+        assert np.abs(gv @ gv.conj().T - np.eye(gs.size)).max() <= tol * 10

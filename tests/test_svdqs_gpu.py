@@ -1,0 +1,72 @@
+"""svdQS end to end with the block SVD on the GPU (qs_svd_blocks_ex) against
+the fixtures made by the REFERENCE's own svdQS, and on larger two-site
+wavefunctions against LAPACK's SVD of the same block matrices."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from qspace_gb300.linalg import _SvdLayout, svdQS
+from qspace_gb300.qspace import QSpace
+from tests.golden.golden_io import unpack
+from tests.helpers import assert_svd_matches
+
+pytestmark = pytest.mark.gpu
+
+G = Path(__file__).resolve().parent / "golden"
+Z = np.load(G / "svdqs_golden.npz")
+CASES = json.loads(str(Z["cases"]))
+
+
+def _opts(o):
+    return dict(Nkeep=o.get("Nkeep", -1), Nkmin=o.get("Nkmin", 0), stol=o.get("stol"), itag=o.get("itag", ""),
+                permA=o.get("permA"), permB=o.get("permB"))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_svdqs_matches_reference(ctx, case):
+    A = QSpace.from_dict(unpack(f"{case['name']}_A", Z))
+    if case.get("error"):
+        with pytest.raises(ValueError):
+            svdQS(A, case["idx"], ctx=ctx, **_opts(case["opts"]))
+        return
+    U, S, V, info = svdQS(A, case["idx"], ctx=ctx, **_opts(case["opts"]))
+    ref = [unpack(f"{case['name']}_{t}", Z) for t in "USV"]
+    assert_svd_matches((U, S, V), ref, case["idx"], case["opts"], tol=1e-11)
+    assert info["Nkeep"] == case["Nkeep"] and info["flag"] == case["flag"]
+    assert abs(info["sfac"] - case["sfac"]) <= 1e-12 * case["sfac"]
+    assert np.allclose(info["svd"], Z[f"{case['name']}_svd"], rtol=1e-12, atol=1e-13)
+
+
+def _two_site(seed, D, cplx):
+    """Rank-4 all-in two-site wavefunction (L, s1, s2, R) with U(1) labels
+    summing to zero: bond sectors q in [-4, 4] of dimension ~D exp(-q^2/8),
+    local labels {-1, 0, 1}."""
+    rng = np.random.default_rng(seed)
+    dq = {q: max(1, int(round(D * np.exp(-q * q / 8.0)))) for q in range(-4, 5)}
+    recs, data = [], []
+    for qL in dq:
+        for s1 in (-1, 0, 1):
+            for s2 in (-1, 0, 1):
+                qR = -(qL + s1 + s2)
+                if qR not in dq:
+                    continue
+                shp = (dq[qL], 1, 1, dq[qR])
+                x = rng.standard_normal(shp)
+                recs.append((qL, s1, s2, qR))
+                data.append(x + 1j * rng.standard_normal(shp) if cplx else x)
+    Q = [np.array([[r[k]] for r in recs], np.int32) for k in range(4)]
+    return QSpace(Q, data, {"itags": ["L", "s1", "s2", "R"]})
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("idx,opts", [([3, 4], {"Nkeep": 200}), ([4], {}), ([2, 3, 4], {"stol": 1e-3})])
+def test_svdqs_two_site_against_lapack(ctx, cplx, idx, opts):
+    A = _two_site(11, 96, cplx)
+    U, S, V, info = svdQS(A, idx, ctx=ctx, **_opts(opts))
+    L = _SvdLayout(A, idx)
+    dec = [np.linalg.svd(M, full_matrices=False) for M in L.mats]
+    ref = L.finish([d[0] for d in dec], [d[1] for d in dec], [d[2] for d in dec], **_opts(opts))
+    assert_svd_matches((U, S, V), [x.to_dict() for x in ref[:3]], idx, opts, tol=1e-11)
+    assert info["Nkeep"] == ref[3]["Nkeep"] and abs(info["sfac"] - ref[3]["sfac"]) <= 1e-12
