@@ -31,7 +31,7 @@ OUT = HERE / "_ref"
 # --source=PATH argument, or else a checkout named "reference" beside this
 # repository's root.
 REF_SRC = Path(os.environ.get("QS_REFERENCE_SOURCE") or (HERE.parent.parent / "reference" / "Source"))
-DEFAULT = ("contractQS", "permuteQS", "eigQS", "svdQS", "getIdentityQS", "plusQS")
+DEFAULT = ("contractQS", "permuteQS", "eigQS", "svdQS", "orthoQS", "getIdentityQS", "plusQS")
 
 
 def reference_present() -> bool:

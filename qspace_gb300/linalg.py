@@ -301,18 +301,23 @@ class _SvdLayout:
     the first K legs, columns: those of the rest) -- SVD_Data::blockSVD and
     QBlock::toBlockMatrix (Source/mpsortho.cc:546-613, 31-257)."""
 
-    def __init__(self, PSI: QSpace, idx):
+    def __init__(self, PSI: QSpace, idx, first=None):
+        """``idx``: the 1-based legs split off behind the others
+        (extend2Perm(.., 'E')); or ``first``: the 1-based legs that lead,
+        in the given order, the others following (extend2Perm)."""
         r = PSI.rank
         if PSI.nblk == 0:
-            raise ValueError("svdQS: got empty PSI")
-        I = [int(i) - 1 for i in np.atleast_1d(np.asarray(idx)).ravel()]
+            raise ValueError("got empty PSI")
+        J = idx if first is None else first
+        I = [int(i) - 1 for i in np.atleast_1d(np.asarray(J)).ravel()]
         if not I or len(I) >= r:
-            raise ValueError(f"svdQS: invalid index set (len={len(I)}/{r})")
+            raise ValueError(f"invalid index set (len={len(I)}/{r})")
         if any(i < 0 or i >= r for i in I) or len(set(I)) != len(I):
-            raise ValueError("svdQS: index out of bounds or not unique")
+            raise ValueError("index out of bounds or not unique")
         tags = list(PSI.info.get("itags") or [])
-        self.r, self.K = r, r - len(I)
-        self.P = [i for i in range(r) if i not in I] + I          # extend2Perm(.., 'E')
+        rest = [i for i in range(r) if i not in I]
+        self.r = r
+        self.P, self.K = (rest + I, r - len(I)) if first is None else (I + rest, len(I))
         K, P = self.K, self.P
         self.tags = [tags[p] for p in P] if len(tags) == r else []
         if K != 1:
@@ -369,11 +374,13 @@ class _SvdLayout:
             self.groups.append({"q": np.asarray(g), "rows": (u1, s1, o1), "cols": (u2, s2, o2)})
             self.mats.append(M)
 
-    def finish(self, Us, Ss, Vts, Nkeep=-1, Nkmin=0, stol=None, itag="", permA=None, permB=None):
-        """Truncation (svd_keep) and the U / S / Vd QSpaces with their
-        itags -- SVD_Data::dmrgTruncate (Source/mpsortho.cc:616-905) and
-        the final permutations of svdQS (Source/svdQS.cc:196-233)."""
-        r, K, P, qdim = self.r, self.K, self.P, self.qdim
+    def decompose(self, Us, Ss, Vts, Nkeep=-1, Nkmin=0, stol=None, itag="", with_s=True):
+        """Truncation (svd_keep) and the QSpaces U (the first K legs and the
+        new bond), S (diagonal, with_s) and V (the other legs and the bond;
+        with_s=False: V times S as one tensor) with their itags, before any
+        final leg permutation -- SVD_Data::dmrgTruncate (Source/mpsortho.cc:
+        616-905) with SQ given (svdQS) or not (orthoQS)."""
+        r, K, qdim = self.r, self.K, self.qdim
         if stol is None:
             stol = 0.0 if Nkeep > 0 else 1e-8                     # WB_STOL_SVD
         Nkmin = max(int(Nkmin), 0)
@@ -409,7 +416,7 @@ class _SvdLayout:
         elif not T[0].endswith("*"):
             tu = _tconj(tu)
         tv = tu
-        if i == 1 and r == 2:
+        if with_s and i == 1 and r == 2:
             tu = _tname(T[0]) + ("*" if tu.endswith("*") else "")        # itag_::tSet
             if not T[1].endswith("*") and revert:
                 tu = _tdual(tu)
@@ -422,6 +429,8 @@ class _SvdLayout:
                 continue
             g = G["q"]
             Vc = np.asarray(Vt).T                                  # conj(V): PSI = U S Vc^T
+            if not with_s:
+                Vc = Vc * (s * sfac)[None, :]                      # Wb::DMatProd(Vc, S)
             for (u, sz, o), X, dst_q, dst_d in ((G["rows"], np.asarray(U), UQ, Ud), (G["cols"], Vc, VQ, Vd)):
                 for j in range(len(u)):
                     dst_q.append(np.concatenate([u[j], g]))
@@ -431,9 +440,9 @@ class _SvdLayout:
 
         # the blocks of one QSpace must not repeat a label record
         # (QSpace::Append2AndDestroy 'u', Source/mpsortho.cc:806-845)
-        for nm, recs in (("U", UQ), ("S", SQ), ("V", VQ)):
+        for nm, recs in (("U", UQ), ("S", SQ if with_s else []), ("V", VQ)):
             if len({tuple(x) for x in recs}) != len(recs):
-                raise ValueError(f"svdQS: {nm}: QIDX must not overlap")
+                raise ValueError(f"{nm}: QIDX must not overlap")
 
         def mk(recs, data, rank, tags):
             if not recs:
@@ -443,45 +452,85 @@ class _SvdLayout:
                           {"itags": tags})
 
         if revert:
-            # U's bond and S's first leg turn into the dual (labels negated,
-            # direction flipped, primed tag); both come back from the
-            # reference's identity contraction sorted by their labels
-            # (Source/mpsortho.cc:867-902, QSpace::initIdentityCG 'z')
-            tU[-1], tS[0] = _tdual(_tconj(tU[-1])), _tdual(_tconj(tS[0]))
-            for recs, data, col in ((UQ, Ud, K * qdim), (SQ, Sd, 0)):
+            # U's bond and S's first leg (without S: V's bond) turn into the
+            # dual (labels negated, direction flipped, primed tag); both come
+            # back from the reference's identity contraction sorted by their
+            # labels (Source/mpsortho.cc:867-902, QSpace::initIdentityCG 'z')
+            tU[-1] = _tdual(_tconj(tU[-1]))
+            if with_s:
+                tS[0] = _tdual(_tconj(tS[0]))
+                other = (SQ, Sd, 0)
+            else:
+                tV[-1] = _tdual(_tconj(tV[-1]))
+                other = (VQ, Vd, (r - K) * qdim)
+            for recs, data, col in ((UQ, Ud, K * qdim), other):
                 for x in recs:
                     x[col:col + qdim] = -x[col:col + qdim]
                 o = _lexsort(np.asarray(recs, np.int64).reshape(len(recs), -1)) if recs else []
                 recs[:] = [recs[j] for j in o]
                 data[:] = [data[j] for j in o]
-        Uq, Sq, Vq = mk(UQ, Ud, K + 1, tU), mk(SQ, Sd, 2, tS), mk(VQ, Vd, r - K + 1, tV)
-        # svdQS's final permutations: Vd gets its bond first; a single
-        # split-off leg leaves U in PSI's leg order, a single kept leg V
+        Sq = mk(SQ, Sd, 2, tS) if with_s else None
+        return mk(UQ, Ud, K + 1, tU), Sq, mk(VQ, Vd, r - K + 1, tV), info
+
+    def finish(self, Us, Ss, Vts, Nkeep=-1, Nkmin=0, stol=None, itag="", permA=None, permB=None):
+        """svdQS's U, S, Vd and info: decompose() and svdQS's final
+        permutations (Source/svdQS.cc:209-229): Vd gets its bond first; a
+        single split-off leg leaves U in PSI's leg order, a single kept leg
+        Vd; then permA / permB."""
+        r, K, P = self.r, self.K, self.P
+        _check_perms(r, permA, permB)
+        Uq, Sq, Vq, info = self.decompose(Us, Ss, Vts, Nkeep, Nkmin, stol, itag, True)
         iP = list(np.argsort(P))
         n = r - K + 1
         pb = [n - 1] + list(range(n - 1))                          # wbperm::initLastTo(0, n)
-        if permB is not None:
-            pb = [pb[j] for j in _perm0(permB)]
-        pa = _perm0(permA) if permA is not None else None
+        if _perm0(permB) is not None:
+            pb = _compose(pb, _perm0(permB))
+        pa = _perm0(permA)
         if K + 1 == r:
-            pa = [iP[j] for j in pa] if pa is not None else iP
+            pa = _compose(iP, pa) if pa is not None else iP
         elif K == 1:
-            pb = [iP[j] for j in pb]
+            pb = _compose(iP, pb)
         if pa is not None:
             Uq = _permute(Uq, pa)
         Vq = _permute(Vq, pb)
         return Uq, Sq, Vq, info
 
 
-def _perm0(p) -> list:
-    return [int(x) - 1 for x in np.atleast_1d(np.asarray(p)).ravel()]
+def _check_perms(r: int, permA, permB):
+    """The MEX's check of the permA / permB options (Source/svdQS.cc:192-193,
+    Source/orthoQS.cc:218-219)."""
+    la = 0 if permA is None else np.size(permA)
+    lb = 0 if permB is None else np.size(permB)
+    if la > r or lb > r or (la and lb and la + lb != r + 2):
+        raise ValueError(f"invalid permutations perm[AB] (lengths {la}, {lb}; rank {r})")
+
+
+def _compose(base: list, p: list) -> list:
+    """wbvector::Permute: entry i becomes base[p[i]] for the first len(p)
+    entries, the others stay (a shorter permutation acts on the leading
+    entries)."""
+    if len(p) > len(base) or any(j >= len(base) for j in p):
+        raise ValueError(f"permutation {[j + 1 for j in p]} out of bounds ({len(base)})")
+    return [base[j] for j in p] + list(base[len(p):])
+
+
+def _perm0(p):
+    """A 1-based permutation option as a 0-based list; None for an identity
+    of any length (the reference skips those)."""
+    if p is None:
+        return None
+    q = [int(x) - 1 for x in np.atleast_1d(np.asarray(p)).ravel()]
+    return None if q == list(range(len(q))) else q
 
 
 def _permute(A: QSpace, p: list) -> QSpace:
     """Leg permutation of a host QSpace (new leg i = old leg p[i]); the block
     order stays (QSpace::Permute, Source/QSpace.hh:2669-2719)."""
-    if A.nblk == 0 or p == list(range(A.rank)):
+    if A.nblk == 0 or p == list(range(len(p))):
         return A
+    if len(p) > A.rank or sorted(p) != list(range(len(p))):
+        raise ValueError(f"permutation {[j + 1 for j in p]} out of bounds (rank {A.rank})")
+    p = list(p) + list(range(len(p), A.rank))                 # a shorter one acts on the leading legs
     tags = A.info.get("itags")
     data = [np.asarray(d).reshape(A.block_dims(i), order="F").transpose(p) for i, d in enumerate(A.data)]
     return QSpace([A.Q[j] for j in p], data, {"itags": [tags[j] for j in p]} if tags else {})
@@ -502,3 +551,102 @@ def svdQS(PSI: QSpace, idx, Nkeep: int = -1, Nkmin: int = 0, stol: float | None 
     L = _SvdLayout(PSI, idx)
     Us, Ss, Vts = svd_blocks(L.mats, ctx)
     return L.finish(Us, Ss, Vts, Nkeep, Nkmin, stol, itag, permA, permB)
+
+
+_LRDIR = {">>": 3, "<<": -3, "LR": 2, "RL": -2, "+": 1, "-": -1}
+
+
+def _nkeep_estimate(L: "_SvdLayout", PSI: QSpace) -> int:
+    """get_Nkeep_estimate (Source/orthoQS.cc:35-52), abelian: the smaller of
+    the products of the total leg dimensions either side of the split."""
+    tot = []
+    for p in L.P:
+        seen = {}
+        for i in range(PSI.nblk):
+            seen.setdefault(tuple(np.asarray(PSI.Q[p][i]).ravel()), PSI.block_dims(i)[p])
+        tot.append(sum(seen.values()))
+    return int(min(np.prod(tot[:L.K]), np.prod(tot[L.K:])))
+
+
+class _OrthoPlan:
+    """Host plan of orthoQS (Source/orthoQS.cc:156-310, usages #1 and #2):
+    which legs lead the SVD, the block matrices (_SvdLayout) and the final
+    leg permutations of A1 and A2."""
+
+    def __init__(self, PSI: QSpace, idx, lrdir=None, permA=None, permB=None):
+        r = PSI.rank
+        I = [int(i) for i in np.atleast_1d(np.asarray(idx)).ravel()]
+        if lrdir is None:
+            if len(I) != 1:
+                raise ValueError("orthoQS: invalid usage #1 (one index required without lrdir)")
+            ldir = None
+        else:
+            # the MEX takes lrdir as a string only (Source/orthoQS.cc:76-79)
+            ldir = _LRDIR.get(lrdir) if isinstance(lrdir, str) else None
+            if not ldir:
+                raise ValueError(f"orthoQS: invalid lrdir {lrdir!r}")
+            if not I or len(I) >= r:
+                raise ValueError(f"orthoQS: invalid index set ({len(I)}/{r})")
+            if abs(ldir) == 3 and (len(I) == 1 or len(I) + 1 == r):
+                I = [i for i in range(1, r + 1) if i not in I]       # ctrIdx::Invert
+                ldir = -ldir
+        # ldir >= 0: the legs I lead (K = len(I)); < 0: they go behind
+        self.L = L = _SvdLayout(PSI, None, first=I) if (ldir is None or ldir >= 0) else _SvdLayout(PSI, I)
+        self.nkeep_est = _nkeep_estimate(L, PSI)
+        K, P = L.K, L.P
+        iP = [int(x) for x in np.argsort(P)]
+        _check_perms(r, permA, permB)
+        pa_u, pb_u = _perm0(permA), _perm0(permB)
+        self.swap = ldir is not None and ldir < 0
+        if ldir is None:
+            pa, pb = None, _compose([r - 1] + list(range(r - 1)), iP)
+        elif ldir >= 0:
+            pb = [r - K] + list(range(r - K))                      # initLastTo(0, r-K+1)
+            if pb_u is not None:
+                pb = _compose(pb, pb_u)
+            pa = pa_u
+            if K + 1 == r:
+                pa = _compose(iP, pa) if pa is not None else iP
+            elif K == 1:
+                pb = _compose(iP, pb)
+        else:
+            n = len(I)
+            pa, pb = pa_u, None
+            if n + 1 == r:
+                pa = _compose([n] + list(range(n)), iP)
+                if pa_u is not None:
+                    pa = _compose(pa, pa_u)
+            elif n == 1:
+                pb = _compose(iP, pb_u) if pb_u is not None else iP
+            if pb is None:
+                pb = [K] + list(range(K))
+                if pb_u is not None:
+                    pb = _compose(pb, pb_u)
+        self.pa, self.pb = pa, pb
+
+    def finish(self, Us, Ss, Vts, Nkeep=-1, Nkmin=0, stol=None, itag=""):
+        if Nkeep is None or Nkeep < 0:
+            Nkeep = self.nkeep_est
+            if stol is None:
+                stol = 1e-8
+        U, _, VS, info = self.L.decompose(Us, Ss, Vts, Nkeep, Nkmin, stol, itag, with_s=False)
+        A1, A2 = (VS, U) if self.swap else (U, VS)
+        if self.pa is not None:
+            A1 = _permute(A1, self.pa)
+        return A1, _permute(A2, self.pb), info
+
+
+def orthoQS(PSI: QSpace, idx, lrdir=None, Nkeep: int = -1, Nkmin: int = 0, stol: float | None = None,
+            itag: str = "", permA=None, permB=None, ctx: Context | None = None):
+    """[A1, A2, info] = orthoQS(PSI, idx [, lrdir], ...) for abelian QSpaces
+    (Source/orthoQS.cc:156-310, usages #1 and #2): PSI = A1 * A2 through a
+    new bond, A1 the isometry.  Without lrdir ``idx`` is one leg, split off
+    into A1 (its leg and the bond); A2 = V S keeps PSI's leg order with the
+    bond in that leg's place.  With lrdir ('>>' 'LR' '+' / '<<' 'RL' '-') the legs ``idx`` go to A1 (>=0) or to A2 (<0; '>>' / '<<' with
+    one leg or all but one take the complement instead and flip the
+    direction), with permA / permB applied as the reference does.  The SVD
+    runs batched on the GPU; Nkeep < 0 keeps up to the smaller dimension
+    either side (stol 1e-8 unless Nkeep is given)."""
+    plan = _OrthoPlan(PSI, idx, lrdir, permA, permB)
+    Us, Ss, Vts = svd_blocks(plan.L.mats, ctx)
+    return plan.finish(Us, Ss, Vts, Nkeep, Nkmin, stol, itag)

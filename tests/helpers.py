@@ -115,3 +115,41 @@ def assert_svd_matches(got, refd, idx, opts, tol: float = 1e-11):
         assert np.abs((gu * gs) @ gv - (xu * xs) @ xv).max() <= tol * smax * 10
         assert np.abs(gu.conj().T @ gu - np.eye(gs.size)).max() <= tol * 10
         assert np.abs(gv @ gv.conj().T - np.eye(gs.size)).max() <= tol * 10
+
+
+def _bond_stack(X, b: int, label, first: bool, nk=None):
+    X = as_dict(X)
+    n = len(X["data"])
+    q = np.asarray(X["Q"][b]).reshape(n, -1)
+    parts = []
+    for i in range(n):
+        if not np.array_equal(q[i], label):
+            continue
+        d = _padded(X, i)
+        k = d.shape[b]
+        parts.append(np.moveaxis(d, b, 0).reshape(k, -1, order="F") if first
+                     else np.moveaxis(d, b, -1).reshape(-1, k, order="F"))
+    return np.hstack(parts) if first else np.vstack(parts)
+
+
+def assert_ortho_matches(got, refd, b1: int, b2: int, tol: float = 1e-11, iso: int = 1):
+    """orthoQS's [A1, A2] against the reference's: labels, block order,
+    shapes and itags exactly; per bond label, A1 A2 contracted over the bond
+    (free of the singular vectors' phases) within tol, and A<iso> (the U
+    factor) isometric.  b1 / b2: the bond's leg in A1 / A2."""
+    for g, x in zip(got, refd):
+        assert_same_structure(g, x)
+        assert (as_dict(g)["info"].get("itags") or None) == (as_dict(x)["info"].get("itags") or None)
+    A1 = as_dict(got[0])
+    if not A1["data"]:
+        return
+    n1 = len(A1["data"])
+    labels = {tuple(x) for x in np.asarray(A1["Q"][b1]).reshape(n1, -1)}
+    for lab in sorted(labels):
+        lab = np.array(lab)
+        gu, xu = _bond_stack(got[0], b1, lab, False), _bond_stack(refd[0], b1, lab, False)
+        gv, xv = _bond_stack(got[1], b2, lab, True), _bond_stack(refd[1], b2, lab, True)
+        scale = max(np.abs(xv).max(), 1.0)
+        assert np.abs(gu @ gv - xu @ xv).max() <= tol * scale * 10
+        W = gu.conj().T @ gu if iso == 1 else gv @ gv.conj().T
+        assert np.abs(W - np.eye(W.shape[0])).max() <= tol * 10

@@ -70,3 +70,29 @@ def test_svdqs_two_site_against_lapack(ctx, cplx, idx, opts):
     ref = L.finish([d[0] for d in dec], [d[1] for d in dec], [d[2] for d in dec], **_opts(opts))
     assert_svd_matches((U, S, V), [x.to_dict() for x in ref[:3]], idx, opts, tol=1e-11)
     assert info["Nkeep"] == ref[3]["Nkeep"] and abs(info["sfac"] - ref[3]["sfac"]) <= 1e-12
+
+
+OCASES = json.loads(str(Z["ortho_cases"]))
+
+
+@pytest.mark.parametrize("case", OCASES, ids=[c["name"] for c in OCASES])
+def test_orthoqs_matches_reference(ctx, case):
+    from qspace_gb300.linalg import _OrthoPlan, orthoQS
+    from tests.helpers import assert_ortho_matches
+    from tests.test_orthoqs_cpu import bonds
+    A = QSpace.from_dict(unpack(f"{case['name']}_A", Z))
+    o = case["opts"]
+    kw = dict(Nkeep=o.get("Nkeep", -1), Nkmin=o.get("Nkmin", 0), stol=o.get("stol"), itag=o.get("itag", ""),
+              permA=o.get("permA"), permB=o.get("permB"), ctx=ctx)
+    if case.get("error"):
+        with pytest.raises(ValueError):
+            orthoQS(A, case["idx"], case["lrdir"], **kw)
+        return
+    A1, A2, info = orthoQS(A, case["idx"], case["lrdir"], **kw)
+    ref = [unpack(f"{case['name']}_{t}", Z) for t in ("A1", "A2")]
+    pl = _OrthoPlan(A, case["idx"], case["lrdir"], o.get("permA"), o.get("permB"))
+    if A1.nblk:
+        assert_ortho_matches((A1, A2), ref, *bonds(pl, A1, A2), tol=1e-11, iso=2 if pl.swap else 1)
+    else:
+        assert not ref[0]["data"]
+    assert info["Nkeep"] == case["Nkeep"] and info["flag"] == case["flag"]
