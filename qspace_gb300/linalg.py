@@ -367,11 +367,12 @@ class _SvdLayout:
             # else the label sum of U's legs (QBlock::init_bare_refA,
             # Source/mpsortho.cc:277-296); it equals the group's sum except
             # for rank 2 with both legs pointing the same way
+            # (a group whose split-off leg carries several labels is refused
+            # once a value of it is kept)
+            mixed = r - K == 1 and any(not np.array_equal(x, u2[0]) for x in u2)
             if r - K == 1:
-                if any(not np.array_equal(x, u2[0]) for x in u2):
-                    raise ValueError("svdQS: got inconsistency in block symmetry")
                 g = u2[0]
-            self.groups.append({"q": np.asarray(g), "rows": (u1, s1, o1), "cols": (u2, s2, o2)})
+            self.groups.append({"q": np.asarray(g), "rows": (u1, s1, o1), "cols": (u2, s2, o2), "mixed": mixed})
             self.mats.append(M)
 
     def decompose(self, Us, Ss, Vts, Nkeep=-1, Nkmin=0, stol=None, itag="", with_s=True):
@@ -427,6 +428,8 @@ class _SvdLayout:
             ik = np.flatnonzero(kp)
             if ik.size == 0:
                 continue
+            if G["mixed"]:
+                raise ValueError("got inconsistency in block symmetry")
             g = G["q"]
             Vc = np.asarray(Vt).T                                  # conj(V): PSI = U S Vc^T
             if not with_s:
@@ -506,12 +509,14 @@ def _check_perms(r: int, permA, permB):
 
 
 def _compose(base: list, p: list) -> list:
-    """wbvector::Permute: entry i becomes base[p[i]] for the first len(p)
-    entries, the others stay (a shorter permutation acts on the leading
-    entries)."""
-    if len(p) > len(base) or any(j >= len(base) for j in p):
-        raise ValueError(f"permutation {[j + 1 for j in p]} out of bounds ({len(base)})")
-    return [base[j] for j in p] + list(base[len(p):])
+    """wbperm::Permute (Source/wbperm.cc:538-588): both extended by the
+    identity to the longer length, entry i becomes base[p[i]] for the first
+    len(p) entries, the others stay."""
+    n = max(len(base), len(p))
+    if sorted(p) != list(range(len(p))):
+        raise ValueError(f"invalid permutation {[j + 1 for j in p]}")
+    ext = list(base) + list(range(len(base), n))
+    return [ext[j] for j in p] + ext[len(p):]
 
 
 def _perm0(p):
