@@ -460,11 +460,14 @@ QS_EXPORT qs_status qs_svd_blocks(qs_ctx *ctx, int64_t nblk, const int64_t *m,
                         double *S, double *Vt);
 
 /* The same for real (is_complex = 0: FP64) or complex (is_complex = 1:
- * interleaved complex128, offsets in complex elements; Vt = V^H) blocks,
- * with the Jacobi sweep limit (0 = 100) and tolerance (<= 0: 1e-15).  A
- * block that does not converge within max_sweeps fails the call with
- * QS_ERR_NUMERIC (wbSVD stops on a LAPACK info != 0,
- * Source/wbarray_blas.cc:1040-1060). */
+ * interleaved complex128, offsets in complex elements; Vt = V^H) blocks.
+ * With max_sweeps = 0 and tol <= 0 blocks of at most 32 x 32 go to the
+ * batched Jacobi solver and larger ones to the polar-decomposition SVD
+ * (cuSOLVER Xgesvdp), spread over concurrent solver streams; a caller that
+ * gives max_sweeps > 0 or tol > 0 gets one Jacobi SVD per block with that
+ * sweep limit (0 = 100) and tolerance (<= 0: 1e-15).  A block that does
+ * not converge fails the call with QS_ERR_NUMERIC (wbSVD stops on a LAPACK
+ * info != 0, Source/wbarray_blas.cc:1040-1060). */
 QS_EXPORT qs_status qs_svd_blocks_ex(qs_ctx *ctx, int64_t nblk, const int64_t *m,
                         const int64_t *n, const int64_t *offs,
                         const int64_t *uoffs, const int64_t *soffs,

@@ -18,6 +18,7 @@
 
 #include <cstdlib>
 #include <exception>
+#include <functional>
 #include <thread>
 
 #include <algorithm>
@@ -988,18 +989,324 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
 }
 
 // -------------------------------------------------------------- svd blocks
-// One Jacobi SVD (gesvdj, FP64 or complex128) per block on the context's
-// stream.  The copy of the block, V and the solver workspace are allocated
-// once for the largest block and reused.  A block that does not converge
-// within max_sweeps (info > 0) fails the call with QS_ERR_NUMERIC, like the
-// reference's wbSVD, which stops on a LAPACK info != 0
+// Block SVDs, three solvers:
+//  * a caller that bounds the Jacobi iteration (max_sweeps or tol given)
+//    gets one Jacobi SVD (gesvdj) per block on the context's stream;
+//  * otherwise blocks of at most 32 x 32 go, grouped by shape, to the
+//    batched Jacobi solver (gesvdjBatched) on the context's stream,
+//  * and the larger ones to the polar-decomposition SVD (Xgesvdp: QDWH
+//    polar factor, then a Hermitian eigensolver), spread over the solver
+//    lanes.  Measured on GB300 for one square FP64 block of n = 354 / 708 /
+//    1416: gesvdj 198 / 577 / 1842 ms, Xgesvd 70 / 226 / 752 ms, Xgesvdp
+//    33 / 82 / 268 ms (LAPACK's dgesdd on 16 Grace cores: 22 / 117 /
+//    395 ms).  Xgesvdp wants M >= N: a wide block is decomposed as A^H.
+// A block that does not converge fails the call with QS_ERR_NUMERIC, like
+// the reference's wbSVD, which stops on a LAPACK info != 0
 // (Source/wbarray_blas.cc:1040-1060).
+constexpr int64_t SVD_BATCHED_MAX = 32;  // gesvdjBatched takes m, n <= 32
+
+// V^T (conjugate transpose for complex) of nb blocks of n x k, block b read
+// at soff[b], written at doff[b] (offsets in elements).
+__global__ void transpose_blocks_kernel(const double *__restrict__ in, double *__restrict__ out,
+                                        const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
+                                        int64_t n, int64_t k, int cplx) {
+  const int64_t b = blockIdx.y;
+  const int es = cplx ? 2 : 1;
+  const double *src = in + soff[b] * es;
+  double *dst = out + doff[b] * es;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * k; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i % n, c = i / n;
+    if (cplx) {
+      const double2 v = reinterpret_cast<const double2 *>(src)[i];
+      reinterpret_cast<double2 *>(dst)[c + r * k] = make_double2(v.x, -v.y);
+    } else {
+      dst[c + r * k] = src[i];
+    }
+  }
+}
+
+// Estimated GB300 time (ms) of one Xgesvdp call on an M x N block (M >= N),
+// real: fitted to 33 / 82 / 268 ms at n = 354 / 708 / 1416 (complex about
+// twice).  Only its ratios matter: it balances the blocks over the lanes.
+static double svdp_ms(int64_t M, int64_t N) {
+  return 5.0 + 2.2e-3 * std::pow((double)M * (double)N * (double)N, 0.55);
+}
+
+static void svd_batched(Ctx *ctx, const std::vector<int64_t> &ids, const int64_t *m, const int64_t *n,
+                        const int64_t *offs, const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs,
+                        const double *A, double *U, double *S, double *Vt, int cplx) {
+  if (ids.empty()) return;
+  const int64_t es = cplx ? 2 : 1;
+  cusolverDnHandle_t h = solver_of(ctx);
+  std::map<std::pair<int64_t, int64_t>, std::vector<int64_t>> byshape;
+  for (int64_t i : ids) byshape[{m[i], n[i]}].push_back(i);
+  gesvdjInfo_t params;
+  QS_SOLVER(cusolverDnCreateGesvdjInfo(&params));
+  struct ParamsGuard {
+    gesvdjInfo_t p;
+    ~ParamsGuard() { cusolverDnDestroyGesvdjInfo(p); }
+  } guard{params};
+  QS_SOLVER(cusolverDnXgesvdjSetTolerance(params, 1e-15));
+  QS_SOLVER(cusolverDnXgesvdjSetMaxSweeps(params, 100));
+  for (auto &kv : byshape) {
+    const int mi = (int)kv.first.first, ni = (int)kv.first.second, k = std::min(mi, ni);
+    const int nb = (int)kv.second.size();
+    // staging: A (m x n), U (m x m), V (n x n), S (k) per block, back to back
+    std::vector<int64_t> so, ao, asz, uo, ud, usz, vo, vd, sso, sd, ssz;
+    for (int j = 0; j < nb; ++j) {
+      const int64_t i = kv.second[j];
+      so.push_back(offs[i]); ao.push_back((int64_t)mi * ni * j); asz.push_back((int64_t)mi * ni);
+      uo.push_back((int64_t)mi * mi * j); ud.push_back(uoffs[i]); usz.push_back((int64_t)mi * k);
+      vo.push_back((int64_t)ni * ni * j); vd.push_back(voffs[i]);
+      sso.push_back((int64_t)k * j); sd.push_back(soffs[i]); ssz.push_back(k);
+    }
+    std::vector<void *> bufs;
+    auto take = [&](void *p) { bufs.push_back(p); return p; };
+    try {
+      double *Ab = (double *)take(dev_alloc<double>(ctx, (size_t)mi * ni * nb * es));
+      double *Ub = (double *)take(dev_alloc<double>(ctx, (size_t)mi * mi * nb * es));
+      double *Vb = (double *)take(dev_alloc<double>(ctx, (size_t)ni * ni * nb * es));
+      double *Sb = (double *)take(dev_alloc<double>(ctx, (size_t)k * nb));
+      int *ib = (int *)take(dev_alloc<int>(ctx, nb));
+      int64_t *t_so = (int64_t *)take(dev_upload(ctx, so)), *t_ao = (int64_t *)take(dev_upload(ctx, ao));
+      int64_t *t_asz = (int64_t *)take(dev_upload(ctx, asz)), *t_uo = (int64_t *)take(dev_upload(ctx, uo));
+      int64_t *t_ud = (int64_t *)take(dev_upload(ctx, ud)), *t_usz = (int64_t *)take(dev_upload(ctx, usz));
+      int64_t *t_vo = (int64_t *)take(dev_upload(ctx, vo)), *t_vd = (int64_t *)take(dev_upload(ctx, vd));
+      int64_t *t_sso = (int64_t *)take(dev_upload(ctx, sso)), *t_sd = (int64_t *)take(dev_upload(ctx, sd));
+      int64_t *t_ssz = (int64_t *)take(dev_upload(ctx, ssz));
+      const dim3 ga((unsigned)std::min<int64_t>(((int64_t)mi * ni * es + 255) / 256, 16), (unsigned)nb);
+      copy_blocks_kernel<<<ga, 256, 0, ctx->stream>>>(A, Ab, t_so, t_ao, t_asz, (int)es);
+      QS_LAUNCHED(ctx);
+      int lwork = 0;
+      if (cplx)
+        QS_SOLVER(cusolverDnZgesvdjBatched_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, mi, ni, (cuDoubleComplex *)Ab, mi,
+                                                      Sb, (cuDoubleComplex *)Ub, mi, (cuDoubleComplex *)Vb, ni,
+                                                      &lwork, params, nb));
+      else
+        QS_SOLVER(cusolverDnDgesvdjBatched_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, mi, ni, Ab, mi, Sb, Ub, mi, Vb,
+                                                      ni, &lwork, params, nb));
+      double *work = (double *)take(dev_alloc<double>(ctx, (size_t)std::max(lwork, 1) * es));
+      if (cplx)
+        QS_SOLVER(cusolverDnZgesvdjBatched(h, CUSOLVER_EIG_MODE_VECTOR, mi, ni, (cuDoubleComplex *)Ab, mi, Sb,
+                                           (cuDoubleComplex *)Ub, mi, (cuDoubleComplex *)Vb, ni,
+                                           (cuDoubleComplex *)work, lwork, ib, params, nb));
+      else
+        QS_SOLVER(cusolverDnDgesvdjBatched(h, CUSOLVER_EIG_MODE_VECTOR, mi, ni, Ab, mi, Sb, Ub, mi, Vb, ni, work,
+                                           lwork, ib, params, nb));
+      ctx->launches++;
+      // the first k columns of U (contiguous m x k), the k values, V^H
+      const dim3 gu((unsigned)std::min<int64_t>(((int64_t)mi * k * es + 255) / 256, 16), (unsigned)nb);
+      copy_blocks_kernel<<<gu, 256, 0, ctx->stream>>>(Ub, U, t_uo, t_ud, t_usz, (int)es);
+      QS_LAUNCHED(ctx);
+      copy_blocks_kernel<<<dim3(1, (unsigned)nb), 64, 0, ctx->stream>>>(Sb, S, t_sso, t_sd, t_ssz, 1);
+      QS_LAUNCHED(ctx);
+      const dim3 gv((unsigned)std::min<int64_t>(((int64_t)ni * k + 255) / 256, 16), (unsigned)nb);
+      transpose_blocks_kernel<<<gv, 256, 0, ctx->stream>>>(Vb, Vt, t_vo, t_vd, ni, k, cplx);
+      QS_LAUNCHED(ctx);
+      std::vector<int> hinfo(nb);
+      QS_CUDA(cudaMemcpyAsync(hinfo.data(), ib, nb * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      QS_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int j = 0; j < nb; ++j) {
+        if (hinfo[j] < 0) fail(QS_ERR_NUMERIC, "svd: block %lld argument error %d", (long long)kv.second[j], hinfo[j]);
+        if (hinfo[j] > 0)
+          fail(QS_ERR_NUMERIC, "svd: block %lld (%d x %d) did not converge in the batched Jacobi solver (info %d)",
+               (long long)kv.second[j], mi, ni, hinfo[j]);
+      }
+    } catch (...) {
+      cudaStreamSynchronize(ctx->stream);
+      for (void *q : bufs) dev_free(ctx, q);
+      throw;
+    }
+    for (void *q : bufs) dev_free(ctx, q);
+  }
+}
+
+// The larger blocks: Xgesvdp, largest first onto the lane with the least
+// estimated work, one host thread per lane (the solver synchronises with
+// its stream inside each call).  `meanwhile` runs on the calling thread
+// while the lanes work.
+static void svd_polar_lanes(Ctx *ctx, const std::vector<int64_t> &ids, const int64_t *m, const int64_t *n,
+                            const int64_t *offs, const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs,
+                            const double *A, double *U, double *S, double *Vt, int cplx,
+                            const std::function<void()> &meanwhile) {
+  if (ids.empty()) {
+    meanwhile();
+    return;
+  }
+  const int64_t es = cplx ? 2 : 1;
+  const cudaDataType dt = cplx ? CUDA_C_64F : CUDA_R_64F;
+  SolverLanes *L = lanes_of(ctx);
+  std::vector<int64_t> order(ids);
+  auto cost = [&](int64_t i) { return svdp_ms(std::max(m[i], n[i]), std::min(m[i], n[i])); };
+  std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return cost(x) > cost(y); });
+  const int nl = (int)std::min<size_t>(NLANES, order.size());
+  std::vector<std::vector<int64_t>> part(nl);
+  std::vector<double> load(nl, 0.0);
+  for (int64_t i : order) {
+    const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    part[l].push_back(i);
+    load[l] += cost(i);
+  }
+  // per lane: the solver's device and host workspaces, a staging copy of the
+  // block (Xgesvdp overwrites its input) and the factor that is transposed
+  std::vector<cusolverDnParams_t> prm(nl, nullptr);
+  std::vector<size_t> wdev(nl, 0), whost(nl, 0);
+  std::vector<double *> work(nl, nullptr), stage(nl, nullptr), tmp(nl, nullptr);
+  std::vector<std::vector<char>> hwork(nl);
+  std::vector<void *> bufs;
+  int *d_info = nullptr;
+  std::vector<int> used;
+  auto release = [&]() {
+    for (int l : used) cudaStreamSynchronize(L->st[l]);
+    for (void *q : bufs) dev_free(ctx, q);
+    bufs.clear();
+    if (d_info) dev_free(ctx, d_info);
+    d_info = nullptr;
+    for (auto *q : prm)
+      if (q) cusolverDnDestroyParams(q);
+    prm.assign(nl, nullptr);
+  };
+  std::vector<double> err(order.size() + 1, 0.0);
+  std::vector<int64_t> slot(order.size());
+  try {
+    int64_t ns = 0;
+    for (int l = 0; l < nl; ++l) {
+      QS_SOLVER(cusolverDnCreateParams(&prm[l]));
+      int64_t sa = 0, st = 0;
+      for (int64_t i : part[l]) {
+        const int64_t M = std::max(m[i], n[i]), N = std::min(m[i], n[i]);
+        size_t wd = 0, wh = 0;
+        QS_SOLVER(cusolverDnXgesvdp_bufferSize(L->h[l], prm[l], CUSOLVER_EIG_MODE_VECTOR, 1, M, N, dt, A, M,
+                                               CUDA_R_64F, S, dt, U, M, dt, Vt, N, dt, &wd, &wh));
+        wdev[l] = std::max(wdev[l], wd);
+        whost[l] = std::max(whost[l], wh);
+        sa = std::max(sa, M * N);
+        st = std::max(st, M * N);      // the transposed factor: N x N (tall) or M x N (wide)
+        slot[ns++] = i;
+      }
+      work[l] = dev_alloc<double>(ctx, (wdev[l] + 7) / 8 + 1);
+      bufs.push_back(work[l]);
+      stage[l] = dev_alloc<double>(ctx, (size_t)sa * es);
+      bufs.push_back(stage[l]);
+      tmp[l] = dev_alloc<double>(ctx, (size_t)st * es);
+      bufs.push_back(tmp[l]);
+      hwork[l].resize(whost[l] + 16);
+    }
+    d_info = dev_alloc<int>(ctx, order.size());
+    QS_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int) * order.size(), ctx->stream));
+    cudaEvent_t fork;
+    QS_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    QS_CUDA(cudaEventRecord(fork, ctx->stream));
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> errs(nl);
+    const int dev = ctx->device;
+    int64_t base = 0;
+    for (int l = 0; l < nl; ++l) {
+      QS_CUDA(cudaStreamWaitEvent(L->st[l], fork, 0));
+      used.push_back(l);
+      th.emplace_back([&, l, base]() {
+        try {
+          QS_CUDA(cudaSetDevice(dev));
+          cudaStream_t sl = L->st[l];
+          for (size_t q = 0; q < part[l].size(); ++q) {
+            const int64_t i = part[l][q];
+            const int64_t mi = m[i], ni = n[i], k = std::min(mi, ni);
+            const bool tall = mi >= ni;
+            const int64_t M = tall ? mi : ni, N = tall ? ni : mi;
+            const int64_t tot = mi * ni;
+            const unsigned g = (unsigned)std::min<int64_t>((tot + 255) / 256, 1024);
+            if (tall) {
+              QS_CUDA(cudaMemcpyAsync(stage[l], A + offs[i] * es, (size_t)(tot * es) * 8, cudaMemcpyDeviceToDevice, sl));
+            } else {
+              transpose_kernel<<<g, 256, 0, sl>>>(A + offs[i] * es, stage[l], mi, ni, cplx);  // A^H
+              QS_CUDA(cudaGetLastError());
+            }
+            // tall: U -> the output, V -> tmp; wide (A^H = U' S V'^H): V' -> U, U' -> tmp
+            double *uo = tall ? U + uoffs[i] * es : tmp[l];
+            double *vo = tall ? tmp[l] : U + uoffs[i] * es;
+            double e = 0.0;
+            QS_SOLVER(cusolverDnXgesvdp(L->h[l], prm[l], CUSOLVER_EIG_MODE_VECTOR, 1, M, N, dt, stage[l], M,
+                                        CUDA_R_64F, S + soffs[i], dt, uo, M, dt, vo, N, dt, work[l], wdev[l],
+                                        hwork[l].data(), whost[l], d_info + base + (int64_t)q, &e));
+            err[base + q] = e;
+            // Vt = (the factor in tmp)^H: n x k -> k x n
+            transpose_kernel<<<(unsigned)std::min<int64_t>((ni * k + 255) / 256, 1024), 256, 0, sl>>>(
+                tmp[l], Vt + voffs[i] * es, ni, k, cplx);
+            QS_CUDA(cudaGetLastError());
+          }
+          QS_CUDA(cudaEventRecord(L->ev[l], sl));
+        } catch (...) {
+          errs[l] = std::current_exception();
+        }
+      });
+      base += (int64_t)part[l].size();
+    }
+    std::exception_ptr mw;
+    try {
+      meanwhile();
+    } catch (...) {
+      mw = std::current_exception();
+    }
+    for (auto &t : th) t.join();
+    if (mw) {
+      cudaEventDestroy(fork);
+      std::rethrow_exception(mw);
+    }
+    cudaEventDestroy(fork);
+    for (size_t q = 0; q < order.size(); ++q) ctx->launches += (m[slot[q]] >= n[slot[q]] ? 2 : 3);
+    for (auto &e : errs)
+      if (e) std::rethrow_exception(e);
+    for (int l : used) QS_CUDA(cudaStreamWaitEvent(ctx->stream, L->ev[l], 0));
+    std::vector<int> info(order.size());
+    QS_CUDA(cudaMemcpyAsync(info.data(), d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QS_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t q = 0; q < order.size(); ++q) {
+      const int64_t i = slot[q];
+      if (info[q] != 0 || !std::isfinite(err[q]))
+        fail(QS_ERR_NUMERIC, "svd: block %lld (%lld x %lld) failed in the polar-decomposition solver (info %d)",
+             (long long)i, (long long)m[i], (long long)n[i], info[q]);
+    }
+  } catch (...) {
+    release();
+    throw;
+  }
+  release();
+}
+
+static void svd_jacobi_each(Ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
+                            const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, const double *A,
+                            double *U, double *S, double *Vt, int cplx, int max_sweeps, double tol);
+
 void svd_blocks(Ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
                 const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, const double *A, double *U,
                 double *S, double *Vt, int cplx, int max_sweeps, double tol) {
   if (nblk <= 0) return;
-  if (max_sweeps <= 0) max_sweeps = 100;
-  if (!(tol > 0)) tol = 1e-15;
+  for (int64_t i = 0; i < nblk; ++i)
+    if (m[i] < 0 || n[i] < 0 || m[i] > INT32_MAX || n[i] > INT32_MAX) fail(QS_ERR_SHAPE, "svd: bad block size");
+  if (max_sweeps > 0 || tol > 0) {
+    if (max_sweeps <= 0) max_sweeps = 100;
+    if (!(tol > 0)) tol = 1e-15;
+    svd_jacobi_each(ctx, nblk, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt, cplx, max_sweeps, tol);
+    return;
+  }
+  std::vector<int64_t> tiny, large;
+  for (int64_t i = 0; i < nblk; ++i) {
+    if (m[i] == 0 || n[i] == 0) continue;
+    (m[i] <= SVD_BATCHED_MAX && n[i] <= SVD_BATCHED_MAX ? tiny : large).push_back(i);
+  }
+  // the batched Jacobi calls run on the context stream while the lanes
+  // work; both write disjoint output slots
+  svd_polar_lanes(ctx, large, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt, cplx, [&]() {
+    svd_batched(ctx, tiny, m, n, offs, uoffs, soffs, voffs, A, U, S, Vt, cplx);
+  });
+}
+
+// One Jacobi SVD (gesvdj) per block on the context's stream with the
+// caller's sweep limit and tolerance; the copy of the block, V and the
+// solver workspace are allocated once for the largest block and reused.
+static void svd_jacobi_each(Ctx *ctx, int64_t nblk, const int64_t *m, const int64_t *n, const int64_t *offs,
+                            const int64_t *uoffs, const int64_t *soffs, const int64_t *voffs, const double *A,
+                            double *U, double *S, double *Vt, int cplx, int max_sweeps, double tol) {
   const int64_t es = cplx ? 2 : 1;  // doubles per element
   cusolverDnHandle_t h = solver_of(ctx);
   gesvdjInfo_t params;

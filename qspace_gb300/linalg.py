@@ -161,9 +161,11 @@ def svd_keep(S_blocks: list, nkeep: int = -1, nkmin: int = 0, stol: float = 0.0)
 
 def svd_blocks(blocks: list, ctx: Context | None = None, max_sweeps: int = 0, tol: float = 0.0):
     """Thin SVD of real or complex blocks on the GPU (qs_svd_blocks_ex):
-    returns lists U, S, Vt with A = U diag(S) Vt.  ``max_sweeps`` / ``tol``
-    bound the Jacobi iteration (0: the library defaults); a block that does
-    not converge raises QSError (QS_ERR_NUMERIC)."""
+    returns lists U, S, Vt with A = U diag(S) Vt.  By default blocks up to
+    32 x 32 use the batched Jacobi solver and larger ones the
+    polar-decomposition SVD on concurrent solver streams; ``max_sweeps`` /
+    ``tol`` > 0 select one Jacobi SVD per block with that bound.  A block
+    that does not converge raises QSError (QS_ERR_NUMERIC)."""
     import torch
     ctx = ctx or default_context()
     cplx = any(np.iscomplexobj(b) for b in blocks)
