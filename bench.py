@@ -702,6 +702,33 @@ def main():
                                        "cores": cb_["cores"], "kind": "port"}
         del dH, dU, dE
 
+    # ---- svdQS of a DMRG two-site state (rank 4, U(1), bond sectors up to
+    # 512, split between the sites, Nkeep 512): the QSpace-level call end to
+    # end (host grouping, the block SVDs on the device, truncation, U/S/Vd)
+    # and LAPACK's SVD (numpy, the host's threads) of the same block matrices
+    svd = None
+    if not a.no_extras:
+        from qspace_gb300.linalg import _SvdLayout, svdQS
+        from qspace_gb300.workloads import two_site_state
+        psi_ = two_site_state(3, 512, False)
+        svdQS(psi_, [3, 4], Nkeep=512, ctx=ctx)
+        sts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            U_, S_, V_, inf_ = svdQS(psi_, [3, 4], Nkeep=512, ctx=ctx)
+            sts.append(time.perf_counter() - t0)
+        mats_ = _SvdLayout(psi_, [3, 4]).mats
+        svd = {"workload": "svdQS of a two-site state: rank 4, U(1), 73 blocks, 11 sector matrices up to "
+                           f"{max(m_.shape[0] for m_ in mats_)}^2, split [3,4], Nkeep 512, FP64",
+               "ms": 1e3 * min(sts), "kept": inf_["Nkeep"], "discarded_weight": inf_["svd2tr"]}
+        if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+            t0 = time.perf_counter()
+            for m_ in mats_:
+                np.linalg.svd(m_, full_matrices=False)
+            svd["cpu_baseline"] = {"ms": 1e3 * (time.perf_counter() - t0), "kind": "LAPACK gesdd (numpy) on the "
+                                   "same sector matrices, as the reference's wbSVD", "cores": os.cpu_count()}
+        del psi_, U_, S_, V_, mats_
+
     # ---- whole Wilson-chain NRG iterations resident on the device: product
     # basis, hopping terms by contractions, plusQS, eigQS with truncation to
     # 4096 kept states (16k product states), new A-tensor and site operators
@@ -792,7 +819,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "slices": slices, "rdm_latency": rdm, "shapes": shapes, "permute": permute, "eig": eig, "nrg": nrg, "serving": serving,
+                "slices": slices, "rdm_latency": rdm, "shapes": shapes, "permute": permute, "eig": eig, "svd": svd, "nrg": nrg, "serving": serving,
                 "clocks": ck}
         if shard_info is not None:
             line["shard"] = shard_info

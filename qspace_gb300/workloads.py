@@ -159,3 +159,25 @@ def nrg_eig_blocks(seed: int = 0, dmax: int = 700, sigma: float = 3.0):
             x = rng.standard_normal((d, d))
             blocks.append(np.asfortranarray(0.5 * (x + x.T)))
     return blocks
+
+
+def two_site_state(seed: int = 0, D: int = 512, complex_data: bool = False) -> QSpace:
+    """Rank-4 all-in two-site wavefunction (L, s1, s2, R) with U(1) labels
+    summing to zero: bond sectors q in [-4, 4] of dimension ~D exp(-q^2/8),
+    local labels {-1, 0, 1} of dimension 1 -- the tensor that svdQS splits
+    between the two sites of a DMRG sweep."""
+    rng = np.random.default_rng(seed)
+    dq = {q: max(1, int(round(D * np.exp(-q * q / 8.0)))) for q in range(-4, 5)}
+    recs, data = [], []
+    for qL in dq:
+        for s1 in (-1, 0, 1):
+            for s2 in (-1, 0, 1):
+                qR = -(qL + s1 + s2)
+                if qR not in dq:
+                    continue
+                shp = (dq[qL], 1, 1, dq[qR])
+                x = rng.standard_normal(shp)
+                recs.append((qL, s1, s2, qR))
+                data.append(x + 1j * rng.standard_normal(shp) if complex_data else x)
+    Q = [np.array([[r[k]] for r in recs], np.int32) for k in range(4)]
+    return QSpace(Q, data, {"itags": ["L", "s1", "s2", "R"]})

@@ -9,6 +9,7 @@ import pytest
 
 from qspace_gb300.linalg import _SvdLayout, svdQS
 from qspace_gb300.qspace import QSpace
+from qspace_gb300.workloads import two_site_state
 from tests.golden.golden_io import unpack
 from tests.helpers import assert_svd_matches
 
@@ -40,24 +41,7 @@ def test_svdqs_matches_reference(ctx, case):
 
 
 def _two_site(seed, D, cplx):
-    """Rank-4 all-in two-site wavefunction (L, s1, s2, R) with U(1) labels
-    summing to zero: bond sectors q in [-4, 4] of dimension ~D exp(-q^2/8),
-    local labels {-1, 0, 1}."""
-    rng = np.random.default_rng(seed)
-    dq = {q: max(1, int(round(D * np.exp(-q * q / 8.0)))) for q in range(-4, 5)}
-    recs, data = [], []
-    for qL in dq:
-        for s1 in (-1, 0, 1):
-            for s2 in (-1, 0, 1):
-                qR = -(qL + s1 + s2)
-                if qR not in dq:
-                    continue
-                shp = (dq[qL], 1, 1, dq[qR])
-                x = rng.standard_normal(shp)
-                recs.append((qL, s1, s2, qR))
-                data.append(x + 1j * rng.standard_normal(shp) if cplx else x)
-    Q = [np.array([[r[k]] for r in recs], np.int32) for k in range(4)]
-    return QSpace(Q, data, {"itags": ["L", "s1", "s2", "R"]})
+    return two_site_state(seed, D, cplx)
 
 
 @pytest.mark.parametrize("cplx", [False, True])
