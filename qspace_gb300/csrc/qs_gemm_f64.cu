@@ -46,6 +46,28 @@ struct Elem<true> {
   __device__ static void store(double *p, int64_t i, T v) { reinterpret_cast<double2 *>(p)[i] = v; }
 };
 
+// One staged K panel into the accumulators, for the NI x NJ leading 16 x 16
+// groups of the tile and the first kn of its KC steps (CTA-uniform bounds).
+template <class E, int NI, int NJ, int KC>
+__device__ __forceinline__ void panel_fma(typename E::T (&acc)[4][4], const typename E::T (*As)[TM + 1],
+                                          const typename E::T (*Bs)[TN + 1], int tx, int ty, int kn) {
+  using T = typename E::T;
+#pragma unroll
+  for (int kk = 0; kk < KC; ++kk) {
+    if (kk < kn) {
+      T a[NI], b[NJ];
+#pragma unroll
+      for (int i = 0; i < NI; ++i) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) b[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < NI; ++i)
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) E::fma(acc[i][j], a[i], b[j]);
+    }
+  }
+}
+
 template <bool CPLX>
 __global__ void __launch_bounds__(256)
 gemm_f64_kernel(const PairDesc *__restrict__ pairs, const TileDesc *__restrict__ tiles,
@@ -59,6 +81,7 @@ gemm_f64_kernel(const PairDesc *__restrict__ pairs, const TileDesc *__restrict__
   const TileDesc t = tiles[blockIdx.x];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
+  const int shape = (min(4, (t.M - t.m0 + 15) / 16) - 1) * 4 + (min(4, (t.N - t.n0 + 15) / 16) - 1);
 
   T acc[4][4];
 #pragma unroll
@@ -98,17 +121,28 @@ gemm_f64_kernel(const PairDesc *__restrict__ pairs, const TileDesc *__restrict__
         Bs[kk][nn] = v;
       }
       __syncthreads();
-#pragma unroll
-      for (int kk = 0; kk < KC; ++kk) {
-        T a[4], b[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = As[kk][tx + 16 * i];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][ty + 16 * j];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) E::fma(acc[i][j], a[i], b[j]);
+      // only the 16-row / 16-column groups of the tile that hold outputs
+      // of the block, and only the pair's own K steps: the FP64 pipe bounds
+      // this kernel, so the padding a 64 x 64 tile carries on small blocks
+      // would cost as much as real work
+      const int kn = min(KC, pd.K - k0);
+      switch (shape) {
+        case 0: panel_fma<E, 1, 1, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 1: panel_fma<E, 1, 2, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 2: panel_fma<E, 1, 3, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 3: panel_fma<E, 1, 4, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 4: panel_fma<E, 2, 1, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 5: panel_fma<E, 2, 2, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 6: panel_fma<E, 2, 3, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 7: panel_fma<E, 2, 4, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 8: panel_fma<E, 3, 1, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 9: panel_fma<E, 3, 2, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 10: panel_fma<E, 3, 3, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 11: panel_fma<E, 3, 4, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 12: panel_fma<E, 4, 1, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 13: panel_fma<E, 4, 2, KC>(acc, As, Bs, tx, ty, kn); break;
+        case 14: panel_fma<E, 4, 3, KC>(acc, As, Bs, tx, ty, kn); break;
+        default: panel_fma<E, 4, 4, KC>(acc, As, Bs, tx, ty, kn); break;
       }
       __syncthreads();
     }
