@@ -789,11 +789,14 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
   // EIG_BUCKET and padded to it (pad_in_kernel): fewer, larger batched
   // calls.  Measured on a 336-block NRG step: 188 ms by exact size, 176 /
   // 159 / 166 ms with buckets of 32 / 64 / 128.
+  // (QS_EIG_BUCKET, 1..1024, overrides the bucket width)
+  const char *eb = std::getenv("QS_EIG_BUCKET");
+  const int64_t bucket = eb ? std::max<int64_t>(1, std::min<int64_t>(1024, std::atoll(eb))) : EIG_BUCKET;
   std::map<int64_t, std::vector<int64_t>> small, bysize;
   for (int64_t i = 0; i < nblk; ++i) {
     if (n[i] == 0) continue;
     if (n[i] <= JACOBI_MAX) small[n[i]].push_back(i);
-    else bysize[(n[i] + EIG_BUCKET - 1) / EIG_BUCKET * EIG_BUCKET].push_back(i);
+    else bysize[(n[i] + bucket - 1) / bucket * bucket].push_back(i);
   }
   // units: (size, blocks); a unit is solved in place when its blocks follow
   // one another in U and E, otherwise through a staging copy
