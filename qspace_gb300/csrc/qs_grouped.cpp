@@ -133,7 +133,7 @@ void run_f64(Ctx *ctx, const std::vector<PairDesc> &pairs, const std::vector<int
     std::vector<int64_t> small;
     std::vector<TileDesc> tiles;
     {
-      std::vector<TileDesc> all = make_tiles(gg, mm, nn, cc, gemm_f64_tile_m(), gemm_f64_tile_n(), ll);
+      std::vector<TileDesc> all = make_tiles(gg, mm, nn, cc, gemm_f64_tile_m(), gemm_f64_tile_n(), ll, &pp);
       std::vector<char> is_small(mm.size(), 0);
       for (size_t b = 0; b < mm.size(); ++b)
         if (deep && ds.part[b] && (int64_t)mm[b] * nn[b] <= DOT_OUTPUTS) {

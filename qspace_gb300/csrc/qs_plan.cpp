@@ -447,7 +447,7 @@ std::vector<TileDesc> make_tiles(const std::vector<int64_t> &grp,
                                  const std::vector<int32_t> &blk_M,
                                  const std::vector<int32_t> &blk_N,
                                  const std::vector<int64_t> &c_off, int tm, int tn,
-                                 const std::vector<int32_t> *blk_ldc) {
+                                 const std::vector<int32_t> *blk_ldc, const std::vector<PairDesc> *pairs) {
   std::vector<TileDesc> tiles;
   const int64_t nb = (int64_t)blk_M.size();
   for (int64_t b = 0; b < nb; ++b) {
@@ -467,8 +467,23 @@ std::vector<TileDesc> make_tiles(const std::vector<int64_t> &grp,
         tiles.push_back(t);
       }
   }
-  // Largest work first: tiles whose block has the deepest summed K go first
-  // so that the tail of the launch is made of short tiles.
+  if (pairs && tiles.size() > 1) {
+    std::vector<int64_t> depth(nb, 0);
+    for (int64_t b = 0; b < nb; ++b)
+      for (int64_t p = grp[b]; p < grp[b + 1]; ++p) depth[b] += std::max((*pairs)[p].K, 0);
+    auto work = [&](const TileDesc &t) {
+      const int64_t rows = std::min<int64_t>(tm, t.M - t.m0), cols = std::min<int64_t>(tn, t.N - t.n0);
+      return depth[t.cblk] * ((rows + 15) / 16) * ((cols + 15) / 16);
+    };
+    std::vector<int64_t> key(tiles.size());
+    for (size_t i = 0; i < tiles.size(); ++i) key[i] = work(tiles[i]);
+    std::vector<size_t> ord(tiles.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return key[x] > key[y]; });
+    std::vector<TileDesc> sorted(tiles.size());
+    for (size_t i = 0; i < ord.size(); ++i) sorted[i] = tiles[ord[i]];
+    tiles.swap(sorted);
+  }
   return tiles;
 }
 

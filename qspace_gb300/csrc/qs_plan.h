@@ -77,12 +77,16 @@ struct ContractPlan {
 ContractPlan plan_contract(const QMeta &A, const char *ia, const QMeta &B,
                            const char *ib, const int32_t *perm, int32_t nperm);
 
-// Tiles of the grouped GEMM over the plan's output blocks.
+// Tiles of the grouped GEMM over the plan's output blocks; with `pairs`,
+// ordered by estimated work, largest first (the summed depth of the block
+// times the tile's 16 x 16 groups that hold outputs), so that the tail of
+// the launch is made of short tiles.
 std::vector<TileDesc> make_tiles(const std::vector<int64_t> &grp,
                                  const std::vector<int32_t> &blk_M,
                                  const std::vector<int32_t> &blk_N,
                                  const std::vector<int64_t> &c_off, int tm, int tn,
-                                 const std::vector<int32_t> *blk_ldc = nullptr);
+                                 const std::vector<int32_t> *blk_ldc = nullptr,
+                                 const std::vector<PairDesc> *pairs = nullptr);
 
 // Permutation descriptors: out block = permute(in block, perm) [+conj].
 std::vector<PermDesc> make_perm_descs(const QMeta &in, const std::vector<int> &perm,

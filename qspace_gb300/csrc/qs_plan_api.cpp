@@ -255,7 +255,7 @@ qs_status qs_grouped_plan_create(qs_ctx *ctx, const qs_pair_list *pairs, const q
     if (!p->main.pairs.empty()) {
       const GroupedPlan &m = p->main;
       std::vector<TileDesc> tiles =
-          make_tiles(m.grp, m.bM, m.bN, m.coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &m.bldc);
+          make_tiles(m.grp, m.bM, m.bN, m.coff, gemm_f64_tile_m(), gemm_f64_tile_n(), &m.bldc, &m.pairs);
       p->ntiles = (int64_t)tiles.size();
       QS_CUDA(cudaMalloc(&p->d_pairs, m.pairs.size() * sizeof(PairDesc)));
       QS_CUDA(cudaMemcpy(p->d_pairs, m.pairs.data(), m.pairs.size() * sizeof(PairDesc),
