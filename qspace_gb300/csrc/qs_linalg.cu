@@ -20,6 +20,7 @@
 #include <exception>
 #include <functional>
 #include <thread>
+#include <tuple>
 
 #include <algorithm>
 #include <cfloat>
@@ -1112,8 +1113,14 @@ static void svd_batched(Ctx *ctx, const std::vector<int64_t> &ids, const int64_t
   if (ids.empty()) return;
   const int64_t es = cplx ? 2 : 1;
   cusolverDnHandle_t h = solver_of(ctx);
-  std::map<std::pair<int64_t, int64_t>, std::vector<int64_t>> byshape;
-  for (int64_t i : ids) byshape[{m[i], n[i]}].push_back(i);
+  // (a group holds at most 32768 blocks: the copy kernels put one block per
+  // grid row, and gridDim.y stops at 65535)
+  std::map<std::tuple<int64_t, int64_t, int64_t>, std::vector<int64_t>> byshape;
+  std::map<std::pair<int64_t, int64_t>, int64_t> seen;
+  for (int64_t i : ids) {
+    const int64_t c = seen[{m[i], n[i]}]++;
+    byshape[{m[i], n[i], c / 32768}].push_back(i);
+  }
   gesvdjInfo_t params;
   QS_SOLVER(cusolverDnCreateGesvdjInfo(&params));
   struct ParamsGuard {
@@ -1123,7 +1130,7 @@ static void svd_batched(Ctx *ctx, const std::vector<int64_t> &ids, const int64_t
   QS_SOLVER(cusolverDnXgesvdjSetTolerance(params, 1e-15));
   QS_SOLVER(cusolverDnXgesvdjSetMaxSweeps(params, 100));
   for (auto &kv : byshape) {
-    const int mi = (int)kv.first.first, ni = (int)kv.first.second, k = std::min(mi, ni);
+    const int mi = (int)std::get<0>(kv.first), ni = (int)std::get<1>(kv.first), k = std::min(mi, ni);
     const int nb = (int)kv.second.size();
     // staging: A (m x n), U (m x m), V (n x n), S (k) per block, back to back
     std::vector<int64_t> so, ao, asz, uo, ud, usz, vo, vd, sso, sd, ssz;

@@ -93,6 +93,19 @@ def test_svd_blocks_complex(ctx):
         assert np.max(np.abs(Vt @ Vt.conj().T - np.eye(k))) <= 1e-12 * k
 
 
+def test_svd_many_small_blocks(ctx):
+    """40 000 blocks of one small shape (more than one batched-Jacobi group)
+    next to a few large ones (polar-decomposition solver on the lanes)."""
+    rng = np.random.default_rng(13)
+    blocks = [rng.standard_normal((3, 2)) for _ in range(40000)] + [rng.standard_normal((70, 45)),
+                                                                   rng.standard_normal((45, 70))]
+    Us, Ss, Vs = svd_blocks(blocks, ctx)
+    for i in list(range(0, 40000, 997)) + [39999, 40000, 40001]:
+        A, U, S, Vt = blocks[i], Us[i], Ss[i], Vs[i]
+        assert np.allclose(S, np.linalg.svd(A, compute_uv=False), rtol=1e-12, atol=1e-13)
+        assert np.max(np.abs((U * S[None, :]) @ Vt - A)) <= 1e-12 * max(1.0, np.abs(A).max()) * 10
+
+
 def test_svd_not_converged_is_an_error(ctx):
     """One Jacobi sweep at a tolerance of 1e-15 cannot diagonalise a dense
     random 120 x 90 block: the call reports QS_ERR_NUMERIC instead of
