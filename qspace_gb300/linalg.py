@@ -6,6 +6,13 @@
   rank-2 QSpace is diagonalised on the GPU in FP64, the global truncation
   (markSet) keeps the Nkeep lowest levels, and the kept / discarded
   eigenvectors come back as QSpaces AK / AD with eigenvalues EK / ED.
+* ``svdQS(PSI, idx, ...)`` / ``orthoQS(PSI, idx [, lrdir], ...)`` mirror the
+  abelian use of the MEX ``svdQS`` / ``orthoQS`` (Source/svdQS.cc:170-234,
+  Source/orthoQS.cc:156-310 -> SVD_Data::blockSVD / dmrgTruncate,
+  Source/mpsortho.cc:546-905): the blocks of each conserved label sum form
+  one matrix, all of them are decomposed on the GPU in one call, truncated
+  together, and U / S / Vd (A1 / A2) come back with the reference's labels,
+  block order and itags.
 * ``eig_blocks``, ``svd_blocks``, ``gs_reortho``: the raw block operations on
   device buffers (torch tensors used as plain device memory).
 """
@@ -549,7 +556,7 @@ def svdQS(PSI: QSpace, idx, Nkeep: int = -1, Nkmin: int = 0, stol: float | None 
     (Source/svdQS.cc:170-234): the legs ``idx`` (1-based) are split off into
     Vd, the others stay with U, PSI = U * S * Vd.  The blocks of one
     conserved label sum form one matrix; all of them are decomposed in one
-    batched SVD on the GPU (qs_svd_blocks_ex), truncated together
+    call on the GPU (qs_svd_blocks_ex), truncated together
     (qs_svd_keep: Nkeep, Nkmin, stol; stol defaults to 1e-8 without Nkeep)
     with the kept values rescaled to PSI's norm.  itags, block order and the
     direction of the new bond follow the reference.  ``info`` holds svd (all
