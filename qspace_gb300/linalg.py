@@ -291,16 +291,17 @@ def _groups(R: np.ndarray):
     """wbMatrix::groupRecs (Source/wbMatrix.cc:1733-1744): the sort
     permutation and the runs of equal rows -> (unique rows, member lists,
     group id of every row)."""
+    n = R.shape[0]
+    gid = np.empty(n, np.int64)
+    if n == 0:
+        return [], [], gid
     p = _lexsort(R)
-    uniq, members = [], []
-    gid = np.empty(R.shape[0], np.int64)
-    for i in p:
-        if not uniq or not np.array_equal(R[i], uniq[-1]):
-            uniq.append(R[i])
-            members.append([])
-        members[-1].append(int(i))
-        gid[i] = len(uniq) - 1
-    return uniq, members, gid
+    Rs = R[p]
+    new = np.ones(n, bool)
+    new[1:] = np.any(Rs[1:] != Rs[:-1], axis=1)
+    starts = np.flatnonzero(new)
+    gid[p] = np.cumsum(new) - 1
+    return [Rs[s] for s in starts], [m.tolist() for m in np.split(p, starts[1:])], gid
 
 
 class _SvdLayout:
