@@ -79,6 +79,16 @@ struct SolverLanes {
   cudaEvent_t ev[NLANES] = {};
 };
 
+// Joins the lane threads on every path out of a scope: a throw between two
+// thread launches must not destroy a joinable std::thread.
+struct ThreadJoiner {
+  std::vector<std::thread> &t;
+  ~ThreadJoiner() {
+    for (auto &x : t)
+      if (x.joinable()) x.join();
+  }
+};
+
 static SolverLanes *lanes_of(Ctx *ctx) {
   if (!ctx->solver_lanes) {
     auto L = new SolverLanes;
@@ -917,6 +927,7 @@ void eig_blocks(Ctx *ctx, int64_t nblk, const int64_t *n, const int64_t *offs, c
     // one host thread per lane: the solver synchronises with its stream
     // inside each call, so lanes driven from one thread would not overlap
     std::vector<std::thread> th;
+    ThreadJoiner joiner{th};
     std::vector<std::exception_ptr> errs(nl);
     const int dev = ctx->device;
     int64_t nlaunch = 0;
@@ -1279,6 +1290,7 @@ static void svd_polar_lanes(Ctx *ctx, const std::vector<int64_t> &ids, const int
     QS_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
     QS_CUDA(cudaEventRecord(fork, ctx->stream));
     std::vector<std::thread> th;
+    ThreadJoiner joiner{th};
     std::vector<std::exception_ptr> errs(nl);
     const int dev = ctx->device;
     int64_t base = 0;
