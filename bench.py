@@ -650,6 +650,63 @@ def main():
         tA.free()
         top.free()
 
+    # ---- two-site DMRG H*psi (the shape of the SU(2) Heisenberg config with
+    # U(1) 2Sz labels standing in): L psi W W R as four device-resident
+    # contractions, D = 4096 states per bond, MPO bond w = 5; the oracle's
+    # numpy chain on the host cores beside it
+    hpsi = None
+    if not a.no_extras:
+        from qspace_gb300 import upload
+        from qspace_gb300.qspace import contract_dev
+        from qspace_gb300.workloads import hpsi_chain
+        Lh, Ph, Wh, Rh = hpsi_chain(0, 4096)
+        tL, tP, tW, tR = (upload(x, ctx) for x in (Lh, Ph, Wh, Rh))
+        hpsi = {"workload": "two-site H*psi: L(a',w,a) psi(a,s1,s2,b) W W R(b',w,b), spin-1/2, U(1) 2Sz sectors "
+                            "in [-30,30], D=4096 per bond, w=5, FP64 (U(1) stand-in for the SU(2) chain)"}
+
+        def chain(pr):
+            x1 = contract_dev(tL, "3", tP, "1", prec=pr)
+            x2 = contract_dev(x1, "23", tW, "13", prec=pr)
+            x3 = contract_dev(x2, "25", tW, "31", prec=pr)
+            y = contract_dev(x3, "25", tR, "32", prec=pr)
+            for t_ in (x1, x2, x3):
+                t_.free()
+            return y
+
+        ys = {}
+        for pr in ("split", "fp64"):
+            chain(pr).free()
+            ctx.sync()
+            hts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                y_ = chain(pr)
+                ctx.sync()
+                hts.append(time.perf_counter() - t0)
+                if pr in ys:
+                    ys[pr].free()
+                ys[pr] = y_
+            hpsi[f"{pr}_ms"] = 1e3 * min(hts)
+        ds_, df_ = ys["split"].download(), ys["fp64"].download()
+        num_ = sum(float(np.sum(np.abs(np.asarray(x_) - np.asarray(y_)) ** 2)) for x_, y_ in zip(ds_.data, df_.data))
+        den_ = sum(float(np.sum(np.abs(np.asarray(y_)) ** 2)) for y_ in df_.data)
+        hpsi["rel_err_split_vs_fp64"] = (num_ / den_) ** 0.5
+        hpsi["psi_blocks"] = Ph.nblk
+        for t_ in list(ys.values()) + [tL, tP, tW, tR]:
+            t_.free()
+        if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+            from oracle import qs_oracle as orc_
+            t0 = time.perf_counter()
+            x_ = orc_.contract(Lh.to_dict(), 3, Ph.to_dict(), 1)
+            x_ = orc_.contract(x_, [2, 3], Wh.to_dict(), [1, 3])
+            x_ = orc_.contract(x_, [2, 5], Wh.to_dict(), [3, 1])
+            x_ = orc_.contract(x_, [2, 5], Rh.to_dict(), [3, 2])
+            hpsi["cpu_baseline"] = {"ms": 1e3 * (time.perf_counter() - t0), "kind": "port",
+                                    "cores": os.cpu_count(), "sample": "the whole chain once (numpy, BLAS threads)"}
+            num_ = sum(float(np.sum(np.abs(np.asarray(x__) - np.asarray(y_)) ** 2)) for x__, y_ in zip(x_["data"], df_.data))
+            hpsi["rel_err_fp64_vs_port"] = (num_ / den_) ** 0.5
+        del Lh, Ph, Wh, Rh
+
     # ---- permuteQS kernels on a device-resident two-site wave function
     permute = None if a.no_extras else permute_bench(ctx)
 
@@ -819,7 +876,7 @@ def main():
                 "latency_ms": {"p50": percentile(step_ms, 0.5), "p99": percentile(step_ms, 0.99)},
                 "plain_fp64": plain, "split_over_plain": (value / ws / plain["value"]) if plain else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "slices": slices, "rdm_latency": rdm, "shapes": shapes, "permute": permute, "eig": eig, "svd": svd, "nrg": nrg, "serving": serving,
+                "slices": slices, "rdm_latency": rdm, "shapes": shapes, "permute": permute, "hpsi": hpsi, "eig": eig, "svd": svd, "nrg": nrg, "serving": serving,
                 "clocks": ck}
         if shard_info is not None:
             line["shard"] = shard_info

@@ -181,3 +181,40 @@ def two_site_state(seed: int = 0, D: int = 512, complex_data: bool = False) -> Q
                 data.append(x + 1j * rng.standard_normal(shp) if complex_data else x)
     Q = [np.array([[r[k]] for r in recs], np.int32) for k in range(4)]
     return QSpace(Q, data, {"itags": ["L", "s1", "s2", "R"]})
+
+
+def hpsi_chain(seed: int = 0, D: int = 4096, qmax: int = 30, sigma: float = 8.0):
+    """Tensors of a two-site DMRG H*psi for a spin-1/2 chain with U(1)
+    (2Sz) labels: environments L(a', w, a) and R(b', w, b), MPO tensors
+    W(wl, s', s, wr) of bond dimension w = 5 (sectors 0 x3, +2, -2) and a
+    two-site state psi(a, s1, s2, b), bonds of D states over 2Sz sectors
+    q in [-qmax, qmax] with dims ~ exp(-q^2 / (2 sigma^2)).  Labels are
+    conserved as a' = a - w, b = a + s1 + s2, s' = s + wl - wr, b' = b - w,
+    so H*psi = L psi W W R keeps the labels of psi.  N(0,1) entries, no
+    itags.  The order of the contractions:
+        X1 = (L, 3; psi, 1)         -> (a', w1, s1, s2, b)
+        X2 = (X1, [2 3]; W, [1 3])  -> (a', s2, b, s1', w2)
+        X3 = (X2, [2 5]; W, [3 1])  -> (a', b, s1', s2', w3)
+        Y  = (X3, [2 5]; R, [3 2])  -> (a', s1', s2', b')."""
+    rng = np.random.default_rng(seed)
+    q = np.arange(-qmax, qmax + 1)
+    wq = np.exp(-q.astype(float) ** 2 / (2 * sigma * sigma))
+    d = np.maximum(np.rint(D * wq / wq.sum()).astype(np.int64), 1)
+    bond = {int(a): int(b) for a, b in zip(q, d)}
+    wsec = {0: 3, 2: 1, -2: 1}
+    spins = (-1, 1)
+
+    def build(recs, shape_of):
+        recs = sorted(recs)
+        data = [rng.standard_normal(shape_of(r)) for r in recs]
+        Q = [np.array([[r[k]] for r in recs], np.int32) for k in range(len(recs[0]))]
+        return QSpace(Q, data, {})
+
+    env = [(ap, w, a) for a in bond for w in wsec for ap in (a - w,) if ap in bond]
+    Lq = build(env, lambda r: (bond[r[0]], wsec[r[1]], bond[r[2]]))
+    Rq = build(env, lambda r: (bond[r[0]], wsec[r[1]], bond[r[2]]))
+    ps = [(a, s1, s2, a + s1 + s2) for a in bond for s1 in spins for s2 in spins if a + s1 + s2 in bond]
+    psi = build(ps, lambda r: (bond[r[0]], 1, 1, bond[r[3]]))
+    wt = [(wl, sp, s, wr) for wl in wsec for wr in wsec for s in spins for sp in spins if sp == s + wl - wr]
+    W = build(wt, lambda r: (wsec[r[0]], 1, 1, wsec[r[3]]))
+    return Lq, psi, W, Rq
