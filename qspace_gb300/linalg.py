@@ -268,7 +268,7 @@ def _tdual(t: str) -> str:
     n = _tname(t)
     n = n[:-1] if n.endswith("'") else n + "'"
     if len(n) > 8:
-        raise ValueError(f"svdQS: itag '{n}' longer than 8 characters")
+        raise ValueError(f"itag '{n}' longer than 8 characters")
     return n + ("*" if t.endswith("*") else "")
 
 
@@ -334,13 +334,13 @@ class _SvdLayout:
             # only ingoing legs may be fused into the outgoing bond; the other
             # group must point one way (blockSVD, Source/mpsortho.cc:557-573)
             if not self.tags:
-                raise ValueError("svdQS: got invalid orthonormalization (rank mismatch of itags)")
+                raise ValueError("got invalid orthonormalization (rank mismatch of itags)")
             qd = [not t.endswith("*") for t in self.tags]
             if not all(qd[:K]):
-                raise ValueError("svdQS: got invalid orthonormalization "
+                raise ValueError("got invalid orthonormalization "
                                  "(only ingoing indices can be fused into outgoing)")
             if any(q != qd[K] for q in qd[K + 1:]):
-                raise ValueError("svdQS: got invalid orthonormalization (2nd/right group is mixed in+out)")
+                raise ValueError("got invalid orthonormalization (2nd/right group is mixed in+out)")
         n, qdim = PSI.nblk, PSI.qdim
         Q = [np.asarray(PSI.Q[p], np.int64).reshape(n, qdim) for p in P]
         dims = [tuple(PSI.block_dims(i)[p] for p in P) for i in range(n)]
@@ -360,13 +360,13 @@ class _SvdLayout:
             seen = set()
             for b, i1, i2 in zip(blks, g1, g2):
                 if (i1, i2) in seen:
-                    raise ValueError("svdQS: block not unique (degenerate records)")
+                    raise ValueError("block not unique (degenerate records)")
                 seen.add((i1, i2))
                 for s, i, d in ((s1, i1, dims[b][:K]), (s2, i2, dims[b][K:])):
                     if s[i] is None:
                         s[i] = d
                     elif s[i] != d:
-                        raise ValueError("svdQS: block size mismatch")
+                        raise ValueError("block size mismatch")
             o1 = np.concatenate([[0], np.cumsum([int(np.prod(d)) for d in s1])]).astype(np.int64)
             o2 = np.concatenate([[0], np.cumsum([int(np.prod(d)) for d in s2])]).astype(np.int64)
             M = np.zeros((int(o1[-1]), int(o2[-1])), dt)
@@ -413,7 +413,7 @@ class _SvdLayout:
         # itags of U, S and Vd (Source/mpsortho.cc:737-779)
         T = self.tags
         if len(T) != r:
-            raise ValueError("svdQS: got invalid/empty itags")
+            raise ValueError("got invalid/empty itags")
         tu = _tname(itag or "")
         revert, i = False, -1
         if r - K == 1:
