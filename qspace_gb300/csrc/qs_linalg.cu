@@ -1231,7 +1231,10 @@ static void svd_polar_lanes(Ctx *ctx, const std::vector<int64_t> &ids, const int
   std::vector<int64_t> order(ids);
   auto cost = [&](int64_t i) { return svdp_ms(std::max(m[i], n[i]), std::min(m[i], n[i])); };
   std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return cost(x) > cost(y); });
-  const int nl = (int)std::min<size_t>(NLANES, order.size());
+  // QS_SVD_LANES (1..8) overrides the number of concurrent lanes
+  const char *sl = std::getenv("QS_SVD_LANES");
+  const int want = sl ? std::max(1, std::min(NLANES, std::atoi(sl))) : NLANES;
+  const int nl = (int)std::min<size_t>(want, order.size());
   std::vector<std::vector<int64_t>> part(nl);
   std::vector<double> load(nl, 0.0);
   for (int64_t i : order) {
