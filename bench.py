@@ -664,13 +664,17 @@ def main():
         hpsi = {"workload": "two-site H*psi: L(a',w,a) psi(a,s1,s2,b) W W R(b',w,b), spin-1/2, U(1) 2Sz sectors "
                             "in [-30,30], D=4096 per bond, w=5, FP64 (U(1) stand-in for the SU(2) chain)"}
 
+        flops_ = [0.0]
+
         def chain(pr):
-            x1 = contract_dev(tL, "3", tP, "1", prec=pr)
-            x2 = contract_dev(x1, "23", tW, "13", prec=pr)
-            x3 = contract_dev(x2, "25", tW, "31", prec=pr)
-            y = contract_dev(x3, "25", tR, "32", prec=pr)
+            sts_ = [{}, {}, {}, {}]
+            x1 = contract_dev(tL, "3", tP, "1", prec=pr, stats=sts_[0])
+            x2 = contract_dev(x1, "23", tW, "13", prec=pr, stats=sts_[1])
+            x3 = contract_dev(x2, "25", tW, "31", prec=pr, stats=sts_[2])
+            y = contract_dev(x3, "25", tR, "32", prec=pr, stats=sts_[3])
             for t_ in (x1, x2, x3):
                 t_.free()
+            flops_[0] = sum(d_.get("flops", 0.0) for d_ in sts_)
             return y
 
         ys = {}
@@ -687,11 +691,13 @@ def main():
                     ys[pr].free()
                 ys[pr] = y_
             hpsi[f"{pr}_ms"] = 1e3 * min(hts)
+            hpsi[f"{pr}_tflops"] = flops_[0] / min(hts) / 1e12
         ds_, df_ = ys["split"].download(), ys["fp64"].download()
         num_ = sum(float(np.sum(np.abs(np.asarray(x_) - np.asarray(y_)) ** 2)) for x_, y_ in zip(ds_.data, df_.data))
         den_ = sum(float(np.sum(np.abs(np.asarray(y_)) ** 2)) for y_ in df_.data)
         hpsi["rel_err_split_vs_fp64"] = (num_ / den_) ** 0.5
         hpsi["psi_blocks"] = Ph.nblk
+        hpsi["gflop_per_chain"] = flops_[0] / 1e9
         for t_ in list(ys.values()) + [tL, tP, tW, tR]:
             t_.free()
         if rank == 0 and ws == 1 and not a.no_cpu_baseline:
